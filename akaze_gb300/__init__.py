@@ -1,0 +1,263 @@
+"""akaze_gb300 - A-KAZE detect + M-LDB describe + 2-NN Hamming match on GB300.
+
+Python face of libakaze_gb300.so, mirroring the reference's API
+(libAKAZECU in src/lib/AKAZE.h and its Boost.Python module
+python/python_bindings.cpp): AKAZEOptions, AKAZE with
+Create_Nonlinear_Scale_Space / Feature_Detection / Compute_Descriptors, and
+Matcher with bfmatch / BFMatch.  Every call runs the CUDA library; there is
+no CPU fallback (loading fails loudly when the extension is missing).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (AkazeError, DMATCH_DTYPE, EXTREMUM_DTYPE, KEYPOINT_DTYPE, AkzOptions, AkzTiming, check, load)
+
+PM_G1, PM_G2, WEICKERT, CHARBONNIER = 0, 1, 2, 3
+SURF_UPRIGHT, SURF, MSURF_UPRIGHT, MSURF, MLDB_UPRIGHT, MLDB = range(6)
+PLANE_LT, PLANE_LSMOOTH, PLANE_LX, PLANE_LY = 0, 1, 3, 4
+_PLANES = {"Lt": PLANE_LT, "Lsmooth": PLANE_LSMOOTH, "Lx": PLANE_LX, "Ly": PLANE_LY}
+
+
+def compile_library(verbose=False, force=False):
+    """Compile libakaze_gb300.so in-tree (akaze_gb300/build.py)."""
+    import importlib
+    return importlib.import_module(__name__ + ".build").build(verbose=verbose, force=force)
+
+
+class AKAZEOptions(AkzOptions):
+    """AKAZEOptions (AKAZEConfig.h:84-172) with the reference defaults."""
+
+    def __init__(self, **kw):
+        super().__init__()
+        check(load().akz_options_default(ctypes.byref(self)))
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+    def setWidth(self, w):
+        self.img_width = int(w)
+
+    def setHeight(self, h):
+        self.img_height = int(h)
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class AKAZE:
+    """libAKAZECU::AKAZE (AKAZE.h:58-143) over the C ABI."""
+
+    def __init__(self, options):
+        self._lib = load()
+        self._h = ctypes.c_void_p()
+        self.options = options
+        check(self._lib.akz_create(ctypes.byref(options), ctypes.byref(self._h)))
+        self.width, self.height = options.img_width, options.img_height
+        self._n = 0
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.akz_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    def set_stream(self, stream_handle):
+        check(self._lib.akz_set_stream(self._h, ctypes.c_void_p(int(stream_handle) if stream_handle else 0)))
+
+    def Create_Nonlinear_Scale_Space(self, img):
+        """img: HxW uint8 (0..255) or float32 (0..1), host numpy array."""
+        img = np.ascontiguousarray(img)
+        if img.dtype == np.uint8:
+            dt = 0
+        elif img.dtype == np.float32:
+            dt = 1
+        else:
+            raise TypeError("image must be uint8 or float32")
+        h, w = img.shape
+        check(self._lib.akz_create_nonlinear_scale_space(self._h, _ptr(img), w, h, img.strides[0], dt, 0))
+        return 0
+
+    def create_from_device(self, dptr, pitch, dtype=0):
+        check(self._lib.akz_create_nonlinear_scale_space(self._h, ctypes.c_void_p(dptr), self.width, self.height,
+                                                         pitch, dtype, 1))
+
+    def Feature_Detection(self):
+        """Detector + suppression; returns the keypoint count (the reference
+        fills the keypoint vector only in Compute_Descriptors)."""
+        n = ctypes.c_int()
+        check(self._lib.akz_feature_detection(self._h, ctypes.byref(n)))
+        self._n = n.value
+        return n.value
+
+    def Compute_Descriptors(self):
+        """Orientation + M-LDB; returns (descriptors n x 61 uint8, keypoints)."""
+        n = self._n
+        kp = np.zeros(n, KEYPOINT_DTYPE)
+        d = np.zeros((n, 61), np.uint8)
+        m = ctypes.c_int()
+        check(self._lib.akz_compute_descriptors(self._h, _ptr(kp), _ptr(d), n, ctypes.byref(m)))
+        return d[: m.value], kp[: m.value]
+
+    def detect_and_compute(self, img):
+        self.Create_Nonlinear_Scale_Space(img)
+        self.Feature_Detection()
+        d, kp = self.Compute_Descriptors()
+        return kp, d
+
+    def Get_Computation_Times(self):
+        t = AkzTiming()
+        check(self._lib.akz_get_timing(self._h, ctypes.byref(t)))
+        return {f: getattr(t, f) for f, _ in AkzTiming._fields_}
+
+    # inspection -------------------------------------------------------------
+    @property
+    def nlevels(self):
+        n = ctypes.c_int()
+        check(self._lib.akz_num_levels(self._h, ctypes.byref(n)))
+        return n.value
+
+    def level_info(self, level):
+        w, h, o, s, n = (ctypes.c_int() for _ in range(5))
+        e = ctypes.c_float()
+        check(self._lib.akz_level_info(self._h, level, ctypes.byref(w), ctypes.byref(h), ctypes.byref(o),
+                                       ctypes.byref(s), ctypes.byref(e), ctypes.byref(n)))
+        return {"width": w.value, "height": h.value, "octave": o.value, "sublevel": s.value,
+                "esigma": e.value, "nsteps": n.value}
+
+    def plane(self, level, name="Lt"):
+        info = self.level_info(level)
+        out = np.empty((info["height"], info["width"]), np.float32)
+        check(self._lib.akz_get_level_plane(self._h, level, _PLANES[name], _ptr(out)))
+        return out
+
+    @property
+    def kcontrast(self):
+        k = ctypes.c_float()
+        check(self._lib.akz_get_kcontrast(self._h, ctypes.byref(k)))
+        return k.value
+
+    def extrema(self):
+        n = ctypes.c_int()
+        check(self._lib.akz_get_extrema(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, EXTREMUM_DTYPE)
+        check(self._lib.akz_get_extrema(self._h, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+
+class Matcher:
+    """libAKAZECU::Matcher (AKAZE.h:29-55): brute-force 2-NN Hamming."""
+
+    def __init__(self):
+        self._lib = load()
+        self._h = ctypes.c_void_p()
+        check(self._lib.akz_matcher_create(ctypes.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.akz_matcher_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    def set_stream(self, stream_handle):
+        check(self._lib.akz_matcher_set_stream(self._h, ctypes.c_void_p(int(stream_handle) if stream_handle else 0)))
+
+    def bfmatch(self, desc_query, desc_train):
+        """Matcher::bfmatch: (nq, 2) DMatch array, best then second best."""
+        q = np.ascontiguousarray(desc_query, np.uint8)
+        t = np.ascontiguousarray(desc_train, np.uint8)
+        if q.ndim != 2 or t.ndim != 2 or (t.shape[0] and q.shape[1] != t.shape[1]):
+            raise ValueError("descriptor matrices must be 2-D with equal row sizes")
+        nq = q.shape[0]
+        out = np.zeros(2 * nq, DMATCH_DTYPE)
+        if nq:
+            check(self._lib.akz_matcher_bfmatch(self._h, _ptr(q), nq, _ptr(t) if t.size else None, t.shape[0],
+                                                q.shape[1], _ptr(out)))
+        return out.reshape(nq, 2)
+
+    def BFMatch(self, desc_query, desc_train):
+        """Matcher::bfmatch_ (AKAZE.cpp:82-105): (nq, 8) float32 rows
+        [queryIdx, trainIdx, 0, distance] for the best and second match."""
+        m = self.bfmatch(desc_query, desc_train)
+        out = np.zeros((m.shape[0], 8), np.float32)
+        for k in range(2):
+            out[:, 4 * k + 0] = m[:, k]["queryIdx"]
+            out[:, 4 * k + 1] = m[:, k]["trainIdx"]
+            out[:, 4 * k + 3] = m[:, k]["distance"]
+        return out
+
+    def bfmatch_device(self, q64_ptr, nq, t64_ptr, nt, out_ptr):
+        check(self._lib.akz_matcher_bfmatch_device(self._h, ctypes.c_void_p(q64_ptr), nq, ctypes.c_void_p(t64_ptr), nt,
+                                                   ctypes.c_void_p(out_ptr)))
+
+
+class Batch:
+    """Many images of uneven sizes, one launch per stage (graph-replayed)."""
+
+    def __init__(self, options, sizes):
+        self._lib = load()
+        self.sizes = [(int(w), int(h)) for w, h in sizes]
+        ws = np.array([w for w, _ in self.sizes], np.int32)
+        hs = np.array([h for _, h in self.sizes], np.int32)
+        self._h = ctypes.c_void_p()
+        check(self._lib.akz_batch_create(ctypes.byref(options), len(self.sizes), _ptr(ws), _ptr(hs), ctypes.byref(self._h)))
+        self.n = len(self.sizes)
+        self.options = options
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.akz_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    def set_stream(self, stream_handle):
+        check(self._lib.akz_batch_set_stream(self._h, ctypes.c_void_p(int(stream_handle) if stream_handle else 0)))
+
+    def upload(self, images):
+        imgs = [np.ascontiguousarray(im, np.uint8) for im in images]
+        for im, (w, h) in zip(imgs, self.sizes):
+            assert im.shape == (h, w)
+        ptrs = (ctypes.c_void_p * self.n)(*[im.ctypes.data for im in imgs])
+        strides = (ctypes.c_size_t * self.n)(*[im.strides[0] for im in imgs])
+        self._keep = imgs
+        check(self._lib.akz_batch_upload(self._h, ptrs, strides, 0))
+
+    def input_ptr(self, i):
+        p = ctypes.c_void_p()
+        pitch = ctypes.c_size_t()
+        check(self._lib.akz_batch_input(self._h, i, ctypes.byref(p), ctypes.byref(pitch)))
+        return p.value, pitch.value
+
+    def run(self):
+        check(self._lib.akz_batch_run(self._h))
+
+    def counts(self):
+        c = np.zeros(self.n, np.int32)
+        check(self._lib.akz_batch_counts(self._h, _ptr(c)))
+        return c
+
+    def results(self, i):
+        n = ctypes.c_int()
+        check(self._lib.akz_batch_results(self._h, i, None, None, 0, ctypes.byref(n)))
+        kp = np.zeros(n.value, KEYPOINT_DTYPE)
+        d = np.zeros((n.value, 61), np.uint8)
+        check(self._lib.akz_batch_results(self._h, i, _ptr(kp), _ptr(d), n.value, ctypes.byref(n)))
+        return kp, d
+
+    def device_results(self, i):
+        kp = ctypes.c_void_p()
+        d = ctypes.c_void_p()
+        check(self._lib.akz_batch_device_results(self._h, i, ctypes.byref(kp), ctypes.byref(d)))
+        return kp.value, d.value
+
+    def plane(self, i, level, name="Lt", shape=None):
+        out = np.empty(shape, np.float32)
+        check(self._lib.akz_batch_level_plane(self._h, i, level, _PLANES[name], _ptr(out)))
+        return out

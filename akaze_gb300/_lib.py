@@ -1,0 +1,110 @@
+"""Loads libakaze_gb300.so (built in-tree by akaze_gb300/build.py) and
+declares the C ABI of include/akaze_gb300.h for ctypes."""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libakaze_gb300.so")
+
+AKZ_OK, AKZ_ERR_INVALID_ARG, AKZ_ERR_OOM, AKZ_ERR_CUDA, AKZ_ERR_OVERFLOW, AKZ_ERR_TIMEOUT, AKZ_ERR_UNSUPPORTED, AKZ_ERR_STATE = range(8)
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "OVERFLOW", 5: "TIMEOUT", 6: "UNSUPPORTED", 7: "STATE"}
+
+KEYPOINT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("size", "<f4"), ("angle", "<f4"),
+                           ("response", "<f4"), ("octave", "<i4"), ("class_id", "<i4")])
+DMATCH_DTYPE = np.dtype([("queryIdx", "<i4"), ("trainIdx", "<i4"), ("imgIdx", "<i4"), ("distance", "<f4")])
+EXTREMUM_DTYPE = np.dtype([("x", "<i4"), ("y", "<i4"), ("level", "<i4"), ("octave", "<i4"),
+                           ("response", "<f4"), ("size", "<f4"), ("octsub", "<f4"), ("dst1", "<f4")])
+
+# every symbol include/akaze_gb300.h declares
+EXPORTS = [
+    "akz_version", "akz_last_error", "akz_options_default", "akz_create", "akz_destroy", "akz_set_stream",
+    "akz_create_nonlinear_scale_space", "akz_feature_detection", "akz_compute_descriptors", "akz_get_timing",
+    "akz_num_levels", "akz_level_info", "akz_get_level_plane", "akz_get_kcontrast", "akz_get_extrema",
+    "akz_batch_create", "akz_batch_destroy", "akz_batch_set_stream", "akz_batch_upload", "akz_batch_input",
+    "akz_batch_run", "akz_batch_counts", "akz_batch_results", "akz_batch_device_results",
+    "akz_batch_detect_describe", "akz_batch_level_plane",
+    "akz_matcher_create", "akz_matcher_destroy", "akz_matcher_set_stream", "akz_matcher_bfmatch",
+    "akz_matcher_bfmatch_device",
+]
+
+
+class AkzOptions(ctypes.Structure):
+    _fields_ = [
+        ("omin", ctypes.c_int), ("omax", ctypes.c_int), ("nsublevels", ctypes.c_int),
+        ("img_width", ctypes.c_int), ("img_height", ctypes.c_int),
+        ("soffset", ctypes.c_float), ("derivative_factor", ctypes.c_float), ("sderivatives", ctypes.c_float),
+        ("diffusivity", ctypes.c_int), ("dthreshold", ctypes.c_float), ("min_dthreshold", ctypes.c_float),
+        ("descriptor", ctypes.c_int), ("descriptor_size", ctypes.c_int), ("descriptor_channels", ctypes.c_int),
+        ("descriptor_pattern_size", ctypes.c_int), ("kcontrast", ctypes.c_float),
+        ("kcontrast_percentile", ctypes.c_float), ("kcontrast_nbins", ctypes.c_size_t),
+        ("save_scale_space", ctypes.c_int), ("save_keypoints", ctypes.c_int), ("verbosity", ctypes.c_int),
+        ("ncudaimages", ctypes.c_int), ("maxkeypoints", ctypes.c_int),
+    ]
+
+
+class AkzTiming(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("kcontrast", "scale", "derivatives", "detector", "extrema", "subpixel", "descriptor")]
+
+
+class AkazeError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load():
+    """The loaded library; raises if the CUDA extension has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with python -m akaze_gb300.build "
+                          "(the library has no CPU fallback)")
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, S = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
+    IP = ctypes.POINTER(ctypes.c_int)
+    sig = {
+        "akz_version": ([], ctypes.c_char_p), "akz_last_error": ([], ctypes.c_char_p),
+        "akz_options_default": ([ctypes.POINTER(AkzOptions)], I),
+        "akz_create": ([ctypes.POINTER(AkzOptions), ctypes.POINTER(P)], I),
+        "akz_destroy": ([P], I), "akz_set_stream": ([P, P], I),
+        "akz_create_nonlinear_scale_space": ([P, P, I, I, S, I, I], I),
+        "akz_feature_detection": ([P, IP], I),
+        "akz_compute_descriptors": ([P, P, P, I, IP], I),
+        "akz_get_timing": ([P, ctypes.POINTER(AkzTiming)], I),
+        "akz_num_levels": ([P, IP], I),
+        "akz_level_info": ([P, I, IP, IP, IP, IP, ctypes.POINTER(ctypes.c_float), IP], I),
+        "akz_get_level_plane": ([P, I, I, P], I),
+        "akz_get_kcontrast": ([P, ctypes.POINTER(ctypes.c_float)], I),
+        "akz_get_extrema": ([P, P, I, IP], I),
+        "akz_batch_create": ([ctypes.POINTER(AkzOptions), I, P, P, ctypes.POINTER(P)], I),
+        "akz_batch_destroy": ([P], I), "akz_batch_set_stream": ([P, P], I),
+        "akz_batch_upload": ([P, P, P, I], I),
+        "akz_batch_input": ([P, I, ctypes.POINTER(P), ctypes.POINTER(S)], I),
+        "akz_batch_run": ([P], I), "akz_batch_counts": ([P, P], I),
+        "akz_batch_results": ([P, I, P, P, I, IP], I),
+        "akz_batch_device_results": ([P, I, ctypes.POINTER(P), ctypes.POINTER(P)], I),
+        "akz_batch_detect_describe": ([P, P, P, P, P, P, P], I),
+        "akz_batch_level_plane": ([P, I, I, I, P], I),
+        "akz_matcher_create": ([ctypes.POINTER(P)], I), "akz_matcher_destroy": ([P], I),
+        "akz_matcher_set_stream": ([P, P], I),
+        "akz_matcher_bfmatch": ([P, P, I, P, I, I, P], I),
+        "akz_matcher_bfmatch_device": ([P, P, I, P, I, P], I),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != AKZ_OK:
+        raise AkazeError(status, load().akz_last_error().decode(errors="replace"))

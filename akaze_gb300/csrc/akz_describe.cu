@@ -1,0 +1,226 @@
+/*
+ * akz_describe.cu - orientation and M-LDB, one warp per keypoint.
+ *
+ * Orientation (cuda_akaze.cu:2114-2167): 109 gradient samples of radius < 6
+ * on a grid of spacing round(size/2) >> octave, Gaussian weights sigma 2.5,
+ * 42 angular bins, the strongest 7-bin circular window, atan2 in [0, 2 pi).
+ * M-LDB (cuda_akaze.cu:1420-1533, :1786-1807, :2034-2111): a 21x21 grid of
+ * samples rotated by the orientation at spacing round(size/2 / 2^octave),
+ * three channels (L, rotated dx, rotated dy) summed into 2x2, 3x3 and 4x4
+ * cells (87 sums) and 486 pairwise comparisons, written as 64-byte rows
+ * (bits 486..511 zero) that the matcher reads directly.
+ *
+ * Sums are formed in a fixed order (sample order for the orientation bins,
+ * raster order of the window for the cells), which is the order of the CPU
+ * restatement, so angles and descriptors are reproducible bit for bit.
+ */
+#include <cuda_runtime.h>
+
+#include "akz_device.cuh"
+#include "akz_fmath.h"
+
+#define AKZ_DESC_WARPS 4
+#define AKZ_CV_PI 3.1415926535897932384626433832795
+
+/* orientation samples in the reference's thread order: tx = 16*(j+6) + (i+6) */
+__constant__ signed char c_oi[109], c_oj[109], c_or2[109];
+/* comparison pairs (cell*3 + channel) in bit order */
+__constant__ unsigned char c_cmp1[486], c_cmp2[486];
+
+struct akz_warp_smem {
+  float s[3][441];
+  float v[87];
+  float bx[42], by[42];
+  float wx[42], wy[42];
+  unsigned char bin[112];
+};
+
+__global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_params p)
+{
+  __shared__ akz_warp_smem sm_all[AKZ_DESC_WARPS];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  akz_warp_smem &S = sm_all[wib];
+  const int nwarps = gridDim.x * AKZ_DESC_WARPS;
+  int total = 0;
+  for (int b = 0; b < p.t.nimg; b++) total += p.t.stats[b].nkp;
+  const int ps = p.pattern_size;
+  const int size2 = ps, size3 = (int)ceilf(2.0f * (float)ps / 3.0f), size4 = (int)ceilf(0.5f * (float)ps);
+  const int win = max(3 * size3, 4 * size4);
+  for (int g = blockIdx.x * AKZ_DESC_WARPS + wib; g < total; g += nwarps) {
+    int img = 0, k = g;
+    while (k >= p.t.stats[img].nkp) {
+      k -= p.t.stats[img].nkp;
+      img++;
+    }
+    const akz_image_desc I = p.t.im[img];
+    akz_kp *kpp = p.kp + I.kp_base + k;
+    const akz_kp kp = *kpp;
+    const akz_level_desc L = p.t.lv[I.first_level + kp.class_id];
+    const int W = L.width, H = L.height, pitch = L.pitch;
+    const float *lxp = p.t.planes + L.lx, *lyp = p.t.planes + L.ly, *ltp = p.t.planes + L.lt;
+    float angle = 0.0f;
+    if (!p.upright) {
+      const int octave = kp.octave;
+      const int step = (int)(0.5f * kp.size + 0.5f) >> octave;
+      const int x = (int)(kp.x + 0.5f) >> octave;
+      const int y = (int)(kp.y + 0.5f) >> octave;
+      for (int s = lane; s < 109; s += 32) {
+        const int r2 = c_or2[s];
+        const int sx = akz_clampi(x + step * c_oi[s], 0, W - 1), sy = akz_clampi(y + step * c_oj[s], 0, H - 1);
+        const long long pos = (long long)sy * pitch + sx;
+        const float dx = p.gw[r2] * __ldg(lxp + pos);
+        const float dy = p.gw[r2] * __ldg(lyp + pos);
+        const float a = akz_atan2f(dy, dx);
+        int bin = (int)((double)a * (21 / AKZ_CV_PI)) + 21;
+        bin = bin > 41 ? 41 : (bin < 0 ? 0 : bin);
+        S.s[0][s] = dx;
+        S.s[1][s] = dy;
+        S.bin[s] = (unsigned char)bin;
+      }
+      __syncwarp();
+      for (int b = lane; b < 42; b += 32) {
+        float rx = 0.0f, ry = 0.0f;
+        for (int s = 0; s < 109; s++)
+          if (S.bin[s] == b) {
+            rx += S.s[0][s];
+            ry += S.s[1][s];
+          }
+        S.bx[b] = rx;
+        S.by[b] = ry;
+      }
+      __syncwarp();
+      float best = -1.0f;
+      int bk = 0;
+      for (int t = lane; t < 42; t += 32) {
+        float ex = S.bx[t], ey = S.by[t];
+        for (int q = t + 1; q < t + 7; q++) {
+          ex += S.bx[q < 42 ? q : q - 42];
+          ey += S.by[q < 42 ? q : q - 42];
+        }
+        S.wx[t] = ex;
+        S.wy[t] = ey;
+        const float r = ex * ex + ey * ey;
+        if (r > best) {
+          best = r;
+          bk = t;
+        }
+      }
+      /* the reference keeps the first k with r > maxr (maxr starts at 0) */
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+        if (ob > best || (ob == best && ok < bk)) {
+          best = ob;
+          bk = ok;
+        }
+      }
+      if (!(best > 0.0f)) bk = 0;
+      __syncwarp();
+      const float a = akz_atan2f(S.wy[bk], S.wx[bk]);
+      angle = a < 0.0f ? (float)((double)a + 2.0 * AKZ_CV_PI) : a;
+      if (lane == 0) kpp->angle = angle;
+      __syncwarp();
+    }
+    /* M-LDB samples */
+    float co = 1.0f, si = 0.0f;
+    if (!p.upright) akz_sincosf(angle, &si, &co);
+    const float iratio = 1.0f / (float)(1 << kp.octave);
+    const int scale = (int)(0.5f * kp.size * iratio + 0.5f);
+    const float xf = kp.x * iratio, yf = kp.y * iratio;
+    const float fs = (float)scale;
+    for (int s = lane; s < win * win; s += 32) {
+      const int yy = s / win, xx = s - yy * win;
+      const int l = xx - size2, kk = yy - size2;
+      int xp = (int)(xf + fs * ((float)kk * co - (float)l * si) + 0.5f);
+      int yp = (int)(yf + fs * ((float)kk * si + (float)l * co) + 0.5f);
+      xp = akz_clampi(xp, 0, W - 1);
+      yp = akz_clampi(yp, 0, H - 1);
+      const long long pos = (long long)yp * pitch + xp;
+      const float im = __ldg(ltp + pos), dx = __ldg(lxp + pos), dy = __ldg(lyp + pos);
+      S.s[0][s] = im;
+      S.s[1][s] = -dx * si + dy * co;
+      S.s[2][s] = dx * co + dy * si;
+    }
+    __syncwarp();
+    for (int q = lane; q < 87; q += 32) {
+      const int cell = q / 3, ch = q - 3 * cell;
+      int sz, cx, cy;
+      if (cell < 4) {
+        sz = size2;
+        cx = cell & 1;
+        cy = cell >> 1;
+      } else if (cell < 13) {
+        sz = size3;
+        cx = (cell - 4) % 3;
+        cy = (cell - 4) / 3;
+      } else {
+        sz = size4;
+        cx = (cell - 13) & 3;
+        cy = (cell - 13) >> 2;
+      }
+      const float *src = S.s[ch];
+      float acc = 0.0f;
+      for (int yy = cy * sz; yy < (cy + 1) * sz; yy++)
+        for (int xx = cx * sz; xx < (cx + 1) * sz; xx++) acc += src[yy * win + xx];
+      S.v[q] = acc;
+    }
+    __syncwarp();
+    if (lane < 16) {
+      uint32_t word = 0;
+      for (int b = 0; b < 32; b++) {
+        const int bit = lane * 32 + b;
+        if (bit < 486 && S.v[c_cmp1[bit]] > S.v[c_cmp2[bit]]) word |= 1u << b;
+      }
+      p.desc[(long long)(I.kp_base + k) * 16 + lane] = word;
+    }
+    __syncwarp();
+  }
+}
+
+static int akz_describe_tables_ready = -1;
+
+static cudaError_t akz_init_describe_tables()
+{
+  signed char oi[109], oj[109], orr[109];
+  int n = 0;
+  for (int tx = 0; tx < 208; tx++) {
+    const int i = (tx & 15) - 6, j = (tx / 16) - 6;
+    if (i * i + j * j < 36) {
+      oi[n] = (signed char)i;
+      oj[n] = (signed char)j;
+      orr[n] = (signed char)(i * i + j * j);
+      n++;
+    }
+  }
+  unsigned char c1[486], c2[486];
+  int m = 0;
+  const int g0[3] = {0, 4, 13}, g1[3] = {4, 13, 29};
+  for (int grid = 0; grid < 3; grid++)
+    for (int ch = 0; ch < 3; ch++)
+      for (int j = g0[grid]; j < g1[grid] - 1; j++)
+        for (int i = j + 1; i < g1[grid]; i++) {
+          c1[m] = (unsigned char)(3 * j + ch);
+          c2[m] = (unsigned char)(3 * i + ch);
+          m++;
+        }
+  cudaError_t e;
+  if ((e = cudaMemcpyToSymbol(c_oi, oi, sizeof(oi))) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_oj, oj, sizeof(oj))) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_or2, orr, sizeof(orr))) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_cmp1, c1, sizeof(c1))) != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_cmp2, c2, sizeof(c2));
+}
+
+cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaStream_t s)
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (akz_describe_tables_ready != dev) {
+    const cudaError_t e = akz_init_describe_tables();
+    if (e != cudaSuccess) return e;
+    akz_describe_tables_ready = dev;
+  }
+  if (nblocks <= 0) return cudaSuccess;
+  k_describe<<<nblocks, 32 * AKZ_DESC_WARPS, 0, s>>>(p);
+  return cudaGetLastError();
+}

@@ -1,0 +1,441 @@
+/*
+ * akz_detect.cu - Hessian detector, extrema, ordering and suppression.
+ *
+ *   k_detect   one fused tile kernel per launch over every (image, level):
+ *              Lsmooth tile -> scaled Scharr derivatives Lx, Ly with step
+ *              sigma_size and reflect-101 border (cuda_akaze.cu:651-671,
+ *              written to HBM for orientation and M-LDB) -> Hessian
+ *              determinant in shared memory (:673-701) -> strict 3x3 maxima
+ *              above the threshold inside the border (:727-743), recorded as
+ *              one bit per pixel plus a per-row count.
+ *   k_rowscan  exclusive scan of the row counts of each image: the raw
+ *              extrema come out in (level, y, x) order, which is the order
+ *              the reference's per-level bitonic sort gives (:884-939),
+ *              with no per-level cap.
+ *   k_extract  one warp per row: subpixel fit and record (:744-769), the
+ *              determinant recomputed from Lx, Ly at the 3x3 neighbourhood.
+ *   k_nms      one CTA per image: the reference's round-based suppression
+ *              (:1005-1224) with an exact per-slot minimum (atomicMin), then
+ *              the 2048-slot chunked emission and subpixel restore
+ *              (:1227-1316).
+ */
+#include <cuda_runtime.h>
+
+#include <climits>
+
+#include "akz_device.cuh"
+#include "akz_fmath.h"
+
+/* ------------------------------------------------------------------------ */
+
+__global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_step)
+{
+  constexpr int TW = AKZ_DETECT_TW, TH = AKZ_DETECT_TH;
+  extern __shared__ float sm[];
+  const int tid = threadIdx.x;
+  const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
+  const akz_tile_seg sg = p.segs[si];
+  const akz_level_desc L = p.t.lv[sg.level_desc];
+  const int W = L.width, H = L.height, st = L.deriv_step;
+  const int lt = blockIdx.x - sg.tile_begin;
+  const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
+  const int tx1 = min(tx0 + TW, W), ty1 = min(ty0 + TH, H);
+  const int sx0 = max(tx0 - 2 * st - 1, 0), sx1 = min(tx1 + 2 * st + 1, W);
+  const int sy0 = max(ty0 - 2 * st - 1, 0), sy1 = min(ty1 + 2 * st + 1, H);
+  const int dx0 = max(tx0 - st - 1, 0), dx1 = min(tx1 + st + 1, W);
+  const int dy0 = max(ty0 - st - 1, 0), dy1 = min(ty1 + st + 1, H);
+  const int ex0 = max(tx0 - 1, 0), ex1 = min(tx1 + 1, W), ey0 = max(ty0 - 1, 0), ey1 = min(ty1 + 1, H);
+  const int sw = sx1 - sx0, dw = dx1 - dx0, ew = ex1 - ex0;
+  const int SM = (TW + 4 * max_step + 2) * (TH + 4 * max_step + 2);
+  const int DM = (TW + 2 * max_step + 2) * (TH + 2 * max_step + 2);
+  float *sS = sm, *sX = sm + SM, *sY = sX + DM, *sD = sY + DM;
+
+  const float *ls = p.t.planes + L.ls;
+  for (int i = tid; i < (sy1 - sy0) * sw; i += 256) {
+    const int y = sy0 + i / sw, x = sx0 + i % sw;
+    sS[i] = __ldg(ls + (long long)y * L.pitch + x);
+  }
+  __syncthreads();
+  const akz_smem_acc S{sS, sx0, sy0, sw};
+  float *lxp = p.t.planes + L.lx, *lyp = p.t.planes + L.ly;
+  for (int i = tid; i < (dy1 - dy0) * dw; i += 256) {
+    const int y = dy0 + i / dw, x = dx0 + i % dw;
+    float a, b;
+    akz_deriv_at(S, W, H, st, x, y, p.fac1, p.fac2, &a, &b);
+    sX[i] = a;
+    sY[i] = b;
+    if (x >= tx0 && x < tx1 && y >= ty0 && y < ty1) {
+      lxp[(long long)y * L.pitch + x] = a;
+      lyp[(long long)y * L.pitch + x] = b;
+    }
+  }
+  __syncthreads();
+  const akz_smem_acc X{sX, dx0, dy0, dw}, Y{sY, dx0, dy0, dw};
+  for (int i = tid; i < (ey1 - ey0) * ew; i += 256) {
+    const int y = ey0 + i / ew, x = ex0 + i % ew;
+    sD[i] = akz_det_at(X, Y, W, H, st, x, y, p.fac1, p.fac2);
+  }
+  __syncthreads();
+  const float border = L.border;
+  for (int i = tid; i < (ty1 - ty0) * (tx1 - tx0); i += 256) {
+    const int y = ty0 + i / (tx1 - tx0), x = tx0 + i % (tx1 - tx0);
+    const int left_x = (int)((float)x - border + 0.5f) - 1;
+    const int right_x = (int)((float)x + border + 0.5f) + 1;
+    const int up_y = (int)((float)y - border + 0.5f) - 1;
+    const int down_y = (int)((float)y + border + 0.5f) + 1;
+    if (left_x < 0 || right_x >= W || up_y < 0 || down_y >= H) continue;
+    const float *c = sD + (y - ey0) * ew + (x - ex0);
+    const float v = c[0];
+    if (v > p.thr && v > c[-ew - 1] && v > c[ew + 1] && v > c[ew - 1] && v > c[-ew + 1] && v > c[-1] && v > c[1] &&
+        v > c[ew] && v > c[-ew]) {
+      atomicOr(&p.bitmap[L.bitmap + (long long)y * L.bitmap_pitch + (x >> 5)], 1u << (x & 31));
+      atomicAdd(&p.rowcnt[L.rows + y], 1);
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Exclusive scan of each image's row counts (rows of all its levels,
+ * concatenated, plus one closing entry).                                   */
+
+__global__ void __launch_bounds__(1024) k_rowscan(akz_tables t, const int *rowcnt, int *rowscan)
+{
+  __shared__ int sWarp[32];
+  __shared__ int sCarry;
+  const akz_image_desc I = t.im[blockIdx.x];
+  const int n = I.rows_total;
+  const int *c = rowcnt + I.rows_base;
+  int *o = rowscan + I.rows_base;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) sCarry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += 1024) {
+    const int i = base + threadIdx.x;
+    const int v = i < n ? c[i] : 0;
+    int x = v;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) sWarp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int w = sWarp[lane];
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, d);
+        if (lane >= d) w += y;
+      }
+      sWarp[lane] = w;
+    }
+    __syncthreads();
+    const int incl = x + (wid > 0 ? sWarp[wid - 1] : 0);
+    if (i < n) o[i] = sCarry + incl - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) sCarry += incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    o[n] = sCarry;
+    akz_image_stats *s = &t.stats[blockIdx.x];
+    s->nraw = sCarry;
+    s->overflow = sCarry > I.raw_cap ? 1 : 0;
+    if (s->overflow) s->status = 4; /* AKZ_ERR_OVERFLOW */
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+
+__global__ void __launch_bounds__(256) k_extract(akz_extract_params p, int nrows)
+{
+  const int lane = threadIdx.x & 31;
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= nrows) return;
+  const int si = akz_find_seg(p.segs, p.nsegs, r);
+  const akz_tile_seg sg = p.segs[si];
+  const akz_level_desc L = p.t.lv[sg.level_desc];
+  const akz_image_desc I = p.t.im[L.image];
+  const int y = r - sg.tile_begin;
+  const int W = L.width, H = L.height, st = L.deriv_step;
+  const int words = L.bitmap_pitch;
+  const uint32_t *row = p.bitmap + L.bitmap + (long long)y * words;
+  const int rank0 = p.rowscan[L.rows + y];
+  akz_raw *out = p.raw + I.raw_base;
+  const akz_plane_acc X{p.t.planes + L.lx, L.pitch}, Y{p.t.planes + L.ly, L.pitch};
+  const int ratio = 1 << L.octave;
+  int running = 0;
+  for (int w0 = 0; w0 < words; w0 += 32) {
+    const int w = w0 + lane;
+    uint32_t bits = w < words ? row[w] : 0u;
+    const int cnt = __popc(bits);
+    int pre = cnt;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, pre, d);
+      if (lane >= d) pre += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, pre, 31);
+    int k = running + pre - cnt;
+    while (bits) {
+      const int b = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const int x = w * 32 + b;
+      const int idx = rank0 + k++;
+      if (idx >= I.raw_cap) continue;
+      float D[3][3];
+      for (int j = -1; j <= 1; j++)
+        for (int i = -1; i <= 1; i++) D[j + 1][i + 1] = akz_det_at(X, Y, W, H, st, x + i, y + j, p.fac1, p.fac2);
+      const float v = D[1][1];
+      const float dx = 0.5f * (D[1][2] - D[1][0]);
+      const float dy = 0.5f * (D[2][1] - D[0][1]);
+      const float dxx = D[1][2] + D[1][0] - 2.0f * v;
+      const float dyy = D[2][1] + D[0][1] - 2.0f * v;
+      const float dxy = 0.25f * (D[2][2] + D[0][0] - D[2][0] - D[0][2]);
+      const float det = dxx * dyy - dxy * dxy;
+      const float idet = (det != 0.0f ? 1.0f / det : 0.0f);
+      const float dst0 = idet * (dxy * dy - dyy * dx);
+      const float dst1 = idet * (dxy * dx - dxx * dy);
+      const bool weak = !(dst0 >= -1.0f && dst0 <= 1.0f && dst1 >= -1.0f && dst1 <= 1.0f);
+      akz_raw e;
+      e.x = x;
+      e.y = y;
+      e.level = L.level;
+      e.octave = L.octave;
+      e.response = v;
+      e.size = (float)((weak ? -1 : 1) * 2.0 * (double)L.size);
+      const float octsub = (float)(dst0 < 0 ? -1 : 1) * ((float)L.octave + fabsf(dst0));
+      e.octsub = weak ? (float)L.octave : octsub;
+      e.dst1 = dst1;
+      out[idx] = e;
+    }
+    running += total;
+  }
+  (void)ratio;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Suppression.                                                             */
+
+struct akz_nms_ctx {
+  const akz_raw *R;
+  const int *state;
+  const int *rs; /* image-local row scan */
+  const akz_level_desc *lv;
+  int first_level;
+  long long rows_base;
+};
+
+/* Decision of unsettled point i: 0 wait (an earlier neighbour is unsettled),
+ * 1 take its own slot, 2 challenge *target (the settled neighbour with the
+ * smallest slot value). Neighbours: FindNeighbors, cuda_akaze.cu:1005-1070. */
+__device__ int akz_nms_decide(const akz_nms_ctx &c, int i, int *target)
+{
+  const akz_raw e = c.R[i];
+  const float size = e.size;
+  if (!(size >= 0.0f)) return 1; /* weak points have no neighbours */
+  const float hs = size * .5f;
+  const float lim = size * size * 0.25f;
+  const akz_level_desc L = c.lv[c.first_level + e.level];
+  const int r = 1 << e.octave;
+  const float px = (float)(r * e.x), py = (float)(r * e.y);
+  const long long rowb = L.rows - c.rows_base;
+  int best = -1, bestv = INT_MAX;
+  /* same level: earlier points whose rows are within hs */
+  for (int yy = e.y; yy >= 0; yy--) {
+    const float pyj = (float)(r * yy);
+    if (py - pyj > hs) break;
+    const int j0 = c.rs[rowb + yy];
+    const int j1 = yy == e.y ? i : c.rs[rowb + yy + 1];
+    for (int j = j0; j < j1; j++) {
+      const float ddx = px - (float)(r * c.R[j].x), ddy = py - pyj;
+      const float dist = ddx * ddx + ddy * ddy;
+      if (dist < lim) {
+        const int s = c.state[j];
+        if (s == -1) return 0;
+        if (s >= 0 && s < bestv) {
+          bestv = s;
+          best = j;
+        }
+      }
+    }
+  }
+  /* previous level: points whose rows are within hs either way */
+  if (e.level > 0) {
+    const akz_level_desc P = c.lv[c.first_level + e.level - 1];
+    const int rp = 1 << P.octave;
+    const long long rowp = P.rows - c.rows_base;
+    const int ylo = max((int)floorf((py - hs) / (float)rp) - 1, 0);
+    const int yhi = min((int)floorf((py + hs) / (float)rp) + 1, P.height - 1);
+    for (int yy = ylo; yy <= yhi; yy++) {
+      const float pyj = (float)(rp * yy);
+      if (pyj - py > hs) continue;
+      if (py - pyj > hs) continue;
+      const int j0 = c.rs[rowp + yy], j1 = c.rs[rowp + yy + 1];
+      for (int j = j0; j < j1; j++) {
+        const float ddx = px - (float)(rp * c.R[j].x), ddy = py - pyj;
+        const float dist = ddx * ddx + ddy * ddy;
+        if (dist < lim) {
+          const int s = c.state[j];
+          if (s == -1) return 0;
+          if (s >= 0 && s < bestv) {
+            bestv = s;
+            best = j;
+          }
+        }
+      }
+    }
+  }
+  if (best < 0) return 1;
+  *target = best;
+  return 2;
+}
+
+__device__ __forceinline__ void akz_bitonic2048(int *v)
+{
+  const int t = threadIdx.x; /* 1024 threads */
+  for (int k = 2; k <= 2048; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+      const int l = i | j;
+      const bool up = (i & k) == 0;
+      const int a = v[i], b = v[l];
+      if ((a > b) == up) {
+        v[i] = b;
+        v[l] = a;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(AKZ_NMS_THREADS) k_nms(akz_nms_params p)
+{
+  __shared__ int sv[2048];
+  const int img = blockIdx.x;
+  const int tid = threadIdx.x;
+  const akz_image_desc I = p.t.im[img];
+  akz_image_stats *stats = &p.t.stats[img];
+  if (stats->overflow) {
+    if (tid == 0) stats->nkp = 0;
+    return;
+  }
+  const int n = stats->nraw;
+  const akz_raw *R = p.raw + I.raw_base;
+  int *state = p.state + I.raw_base;
+  int *minc = p.aux + I.raw_base;
+  signed char *dec = p.decision + I.raw_base;
+  for (int i = tid; i < n; i += AKZ_NMS_THREADS) {
+    state[i] = -1;
+    minc[i] = INT_MAX;
+  }
+  __syncthreads();
+  const akz_nms_ctx c{R, state, p.rowscan + I.rows_base, p.t.lv, I.first_level, I.rows_base};
+  int rounds = 0;
+  for (;;) {
+    int any = 0;
+    for (int i = tid; i < n; i += AKZ_NMS_THREADS) {
+      if (state[i] != -1) continue;
+      any = 1;
+      int target = -1;
+      const int d = akz_nms_decide(c, i, &target);
+      dec[i] = (signed char)d;
+      if (d == 2) atomicMin(&minc[target], i);
+    }
+    if (!__syncthreads_or(any)) break;
+    for (int i = tid; i < n; i += AKZ_NMS_THREADS)
+      if (state[i] == -1 && dec[i] == 1) state[i] = i;
+    __syncthreads();
+    for (int s = tid; s < n; s += AKZ_NMS_THREADS) {
+      const int ch = minc[s];
+      if (ch != INT_MAX) {
+        minc[s] = INT_MAX;
+        if (R[ch].response > R[s].response) {
+          state[ch] = s;
+          state[s] = -2;
+        } else {
+          state[ch] = -2;
+        }
+      }
+    }
+    __syncthreads();
+    if (++rounds > p.max_rounds) {
+      if (tid == 0) stats->status = 5; /* AKZ_ERR_TIMEOUT */
+      break;
+    }
+  }
+  /* emission in chunks of 2048 slots, each chunk's slot values ascending */
+  akz_kp *kp = p.kp + I.kp_base;
+  int out = 0;
+  for (int cs = 0; cs < n; cs += 2048) {
+    for (int k = tid; k < 2048; k += AKZ_NMS_THREADS) {
+      const int s = cs + k;
+      int v = INT_MAX;
+      if (s < n) {
+        const int st = state[s];
+        if (st >= 0 && R[st].size >= 0.0f) v = st;
+      }
+      sv[k] = v;
+    }
+    __syncthreads();
+    akz_bitonic2048(sv);
+    const int c0 = __syncthreads_count(sv[tid] != INT_MAX);
+    const int c1 = __syncthreads_count(sv[tid + 1024] != INT_MAX);
+    for (int k = tid; k < c0 + c1; k += AKZ_NMS_THREADS) {
+      const akz_raw e = R[sv[k]];
+      const float octsub = fabsf(e.octsub);
+      const int octave = (int)octsub;
+      const float subp = (float)(e.octsub < 0 ? -1 : 1) * (octsub - (float)octave);
+      const float ratio = (float)(1 << octave);
+      const int r0 = 1 << e.octave;
+      const float px = (float)(r0 * e.x), py = (float)(r0 * e.y);
+      akz_kp o;
+      o.y = ratio * ((float)(int)(0.5f + py / ratio) + e.dst1);
+      o.x = ratio * ((float)(int)(0.5f + px / ratio) + subp);
+      o.class_id = e.level;
+      o.octave = octave;
+      o.response = e.response;
+      o.size = e.size;
+      o.angle = 0.0f;
+      kp[out + k] = o;
+    }
+    out += c0 + c1;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    stats->nkp = out;
+    stats->nms_rounds = rounds;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+
+cudaError_t akz_launch_detect(const akz_detect_params &p, int ntiles, int max_step, cudaStream_t s)
+{
+  if (ntiles <= 0) return cudaSuccess;
+  const size_t SM = (size_t)(AKZ_DETECT_TW + 4 * max_step + 2) * (AKZ_DETECT_TH + 4 * max_step + 2);
+  const size_t DM = (size_t)(AKZ_DETECT_TW + 2 * max_step + 2) * (AKZ_DETECT_TH + 2 * max_step + 2);
+  const size_t EM = (size_t)(AKZ_DETECT_TW + 2) * (AKZ_DETECT_TH + 2);
+  const size_t smem = (SM + 2 * DM + EM) * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(k_detect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_detect<<<ntiles, 256, smem, s>>>(p, max_step);
+  return cudaGetLastError();
+}
+
+cudaError_t akz_launch_rowscan(const akz_tables &t, const int *rowcnt, int *rowscan, cudaStream_t s)
+{
+  k_rowscan<<<t.nimg, 1024, 0, s>>>(t, rowcnt, rowscan);
+  return cudaGetLastError();
+}
+
+cudaError_t akz_launch_extract(const akz_extract_params &p, int nrows, cudaStream_t s)
+{
+  if (nrows <= 0) return cudaSuccess;
+  const int warps_per_block = 8;
+  k_extract<<<(nrows + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, s>>>(p, nrows);
+  return cudaGetLastError();
+}
+
+cudaError_t akz_launch_nms(const akz_nms_params &p, cudaStream_t s)
+{
+  k_nms<<<p.t.nimg, AKZ_NMS_THREADS, 0, s>>>(p);
+  return cudaGetLastError();
+}

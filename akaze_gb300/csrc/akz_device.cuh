@@ -1,0 +1,103 @@
+/*
+ * akz_device.cuh - small device helpers shared by the kernels.
+ *
+ * All kernels are compiled with -fmad=false: every float expression is
+ * evaluated as written, with one rounding per operation, so the GPU results
+ * equal the CPU restatement of the reference operation for operation.
+ */
+#ifndef AKZ_DEVICE_CUH
+#define AKZ_DEVICE_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "akz_internal.h"
+#include "akz_kernels.h"
+
+__device__ __forceinline__ int akz_clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+/* cv::BORDER_REFLECT_101 for offsets of at most n-1. */
+__device__ __forceinline__ int akz_refl101(int i, int n)
+{
+  if (n == 1) return 0;
+  if (i < 0) return -i;
+  if (i >= n) return 2 * n - 2 - i;
+  return i;
+}
+
+/* Segment of a tiled launch that owns tile t (segments sorted by tile_begin). */
+__device__ __forceinline__ int akz_find_seg(const akz_tile_seg *segs, int nsegs, int t)
+{
+  int lo = 0, hi = nsegs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&segs[mid].tile_begin) <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+/* Input pixel of image img as float in [0,1]: u8 * (float)(1/255) or f32. */
+__device__ __forceinline__ float akz_fetch_input(const akz_tables &t, const akz_image_desc &I, int x, int y, float inv255)
+{
+  if (t.input_f32) return __ldg(t.f32 + (I.u8_off >> 2) + (long long)y * (I.u8_pitch >> 2) + x);
+  return (float)__ldg(t.u8 + I.u8_off + (long long)y * I.u8_pitch + x) * inv255;
+}
+
+/* Detector derivative pair at (x, y) from a plane s with reflect-101 offsets
+ * of +-step (cuda_akaze.cu:651-671):
+ *   dx = fac1*(ur + lr - ul - ll) + fac2*(cr - cl)
+ *   dy = fac1*(lr + ll - ur - ul) + fac2*(lc - uc)
+ * The accessor A(x, y) returns the plane value. */
+template <class A>
+__device__ __forceinline__ void akz_deriv_at(const A &s, int W, int H, int step, int x, int y, float fac1, float fac2,
+                                             float *dx, float *dy)
+{
+  const int xl = x < step ? step - x : x - step;
+  const int xh = x >= W - step ? 2 * W - x - step - 2 : x + step;
+  const int yl = y < step ? step - y : y - step;
+  const int yh = y >= H - step ? 2 * H - y - step - 2 : y + step;
+  const float ul = s(xl, yl), ur = s(xh, yl), ll = s(xl, yh), lr = s(xh, yh);
+  const float cl = s(xl, y), cr = s(xh, y), uc = s(x, yl), lc = s(x, yh);
+  *dx = fac1 * (ur + lr - ul - ll) + fac2 * (cr - cl);
+  *dy = fac1 * (lr + ll - ur - ul) + fac2 * (lc - uc);
+}
+
+/* Hessian determinant at (x, y) from Lx, Ly accessors (cuda_akaze.cu:673-701). */
+template <class A>
+__device__ __forceinline__ float akz_det_at(const A &lx, const A &ly, int W, int H, int step, int x, int y, float fac1, float fac2)
+{
+  const int xl = x < step ? step - x : x - step;
+  const int xh = x >= W - step ? 2 * W - x - step - 2 : x + step;
+  const int yl = y < step ? step - y : y - step;
+  const int yh = y >= H - step ? 2 * H - y - step - 2 : y + step;
+  float ul = lx(xl, yl), ur = lx(xh, yl), ll = lx(xl, yh), lr = lx(xh, yh);
+  const float cl = lx(xl, y), cr = lx(xh, y);
+  const float lxx = fac1 * (ur + lr - ul - ll) + fac2 * (cr - cl);
+  float uc = lx(x, yl), lc = lx(x, yh);
+  const float lyx = fac1 * (lr + ll - ur - ul) + fac2 * (lc - uc);
+  ul = ly(xl, yl);
+  ur = ly(xh, yl);
+  ll = ly(xl, yh);
+  lr = ly(xh, yh);
+  uc = ly(x, yl);
+  lc = ly(x, yh);
+  const float lyy = fac1 * (lr + ll - ur - ul) + fac2 * (lc - uc);
+  return lxx * lyy - lyx * lyx;
+}
+
+struct akz_plane_acc {
+  const float *p;
+  int pitch;
+  __device__ __forceinline__ float operator()(int x, int y) const { return __ldg(p + (long long)y * pitch + x); }
+};
+
+struct akz_smem_acc {
+  const float *p;
+  int x0, y0, stride;
+  __device__ __forceinline__ float operator()(int x, int y) const { return p[(y - y0) * stride + (x - x0)]; }
+};
+
+#endif

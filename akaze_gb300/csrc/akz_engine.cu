@@ -1,0 +1,1204 @@
+/*
+ * akz_engine.cu - host side of libakaze_gb300: options, level plan, HBM
+ * arena, stage launches, CUDA-graph replay and the C ABI of
+ * include/akaze_gb300.h.
+ *
+ * Level geometry and FED schedule follow src/lib/AKAZE.cpp:146-197 and
+ * src/lib/fed.cpp:41-148 of the reference; Gaussian taps and the contrast
+ * pipeline follow src/lib/nldiffusion_functions.cpp.  Nothing here falls
+ * back to CPU computation: every stage of the path runs as a kernel.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/akaze_gb300.h"
+#include "akz_fmath.h"
+#include "akz_kernels.h"
+
+cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit, cudaStream_t s);
+int akz_match_splits(int nq, int nt, int nsm);
+size_t akz_match_partial_bytes(int nq, int nsplit);
+
+/* ------------------------------------------------------------------------ */
+/* errors                                                                   */
+
+static thread_local std::string g_last_error;
+
+static akz_status akz_fail(akz_status s, const char *fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return s;
+}
+
+static akz_status akz_fail_cuda(cudaError_t e, const char *expr, const char *file, int line)
+{
+  return akz_fail(e == cudaErrorMemoryAllocation ? AKZ_ERR_OOM : AKZ_ERR_CUDA, "%s failed: %s (%s:%d)", expr,
+                  cudaGetErrorString(e), file, line);
+}
+
+#define CK(x)                                                                 \
+  do {                                                                        \
+    cudaError_t e_ = (x);                                                     \
+    if (e_ != cudaSuccess) return akz_fail_cuda(e_, #x, __FILE__, __LINE__); \
+  } while (0)
+
+/* ------------------------------------------------------------------------ */
+/* plan                                                                     */
+
+struct akz_geo {
+  int w, h, octave, sublevel, deriv_step, nsteps;
+  float esigma, etime, size, border;
+};
+
+static bool akz_is_prime(int number)
+{
+  if (number <= 1) return false;
+  if (number == 2 || number == 3 || number == 5 || number == 7) return true;
+  if ((number % 2) == 0 || (number % 3) == 0 || (number % 5) == 0 || (number % 7) == 0) return false;
+  const int upper = (int)std::sqrt(number + 1.0);
+  for (int d = 11; d <= upper; d += 2)
+    if (number % d == 0) return false;
+  return true;
+}
+
+/* fed.cpp:41-119 */
+static int akz_fed_tau(float T, float tau_max, std::vector<float> &tau)
+{
+  const float t = T / 1.0f;
+  const int n = (int)(std::ceil(std::sqrt(3.0 * t / tau_max + 0.25f) - 0.5f - 1.0e-8f) + 0.5f);
+  const float scale = (float)(3.0 * t / (tau_max * (float)(n * (n + 1))));
+  if (n <= 0) return 0;
+  std::vector<float> tauh(n);
+  const float c = 1.0f / (4.0f * (float)n + 2.0f);
+  const float d = scale * tau_max / 2.0f;
+  for (int k = 0; k < n; ++k) {
+    const float h = (float)std::cos(M_PI * (double)(2.0f * (float)k + 1.0f) * (double)c);
+    tauh[k] = d / (h * h);
+  }
+  tau.assign(n, 0.0f);
+  if (n == 1) {
+    tau[0] = tauh[0];
+    return 1;
+  }
+  const int kappa = n / 2;
+  int prime = n + 1;
+  while (!akz_is_prime(prime)) prime++;
+  for (int k = 0, l = 0; l < n; ++k, ++l) {
+    int index;
+    while ((index = ((k + 1) * kappa) % prime - 1) >= n) k++;
+    tau[l] = tauh[index];
+  }
+  return n;
+}
+
+/* AKAZE.cpp:146-197 */
+static void akz_plan_levels(const akz_options &o, int W, int H, std::vector<akz_geo> &L, std::vector<std::vector<float>> &tau)
+{
+  L.clear();
+  tau.clear();
+  for (int i = 0; i <= o.omax - 1; i++) {
+    const float rfactor = (float)(1.0 / std::pow(2.0, i));
+    const int lh = (int)((float)H * rfactor);
+    const int lw = (int)((float)W * rfactor);
+    if ((lw < 80 || lh < 40) && i != 0) break;
+    for (int j = 0; j < o.nsublevels; j++) {
+      akz_geo g;
+      g.w = lw;
+      g.h = lh;
+      g.octave = i;
+      g.sublevel = j;
+      g.esigma = o.soffset * powf(2.0f, (float)j / (float)o.nsublevels + (float)i);
+      g.etime = (float)(0.5 * (double)(g.esigma * g.esigma));
+      const float ratio = powf(2.0f, (float)i);
+      g.deriv_step = (int)(g.esigma * o.derivative_factor / ratio + 0.5f);
+      g.size = g.esigma * o.derivative_factor;
+      const float smax = (float)(10.0 * (double)sqrtf(2.0f));
+      g.border = smax * (float)(int)(g.size / ratio + 0.5f);
+      g.nsteps = 0;
+      L.push_back(g);
+    }
+  }
+  tau.resize(L.size());
+  for (size_t i = 1; i < L.size(); i++) {
+    const float ttime = L[i].etime - L[i - 1].etime;
+    L[i].nsteps = akz_fed_tau(ttime, 0.25f, tau[i]);
+  }
+}
+
+/* nldiffusion_functions.cpp:33-43 size rule; normalised exp(-x^2/2s^2) taps
+ * computed in double and rounded to float. */
+static int akz_gauss_taps(float sigma, float *taps)
+{
+  long ks = (long)std::ceil(2.0 * (1.0 + (sigma - 0.8) / (0.3)));
+  if (ks % 2 == 0) ks += 1;
+  const int R = (int)(ks / 2);
+  if (R > (AKZ_MAX_TAPS - 1) / 2) return -1;
+  double k[AKZ_MAX_TAPS];
+  const double scale2 = -0.5 / ((double)sigma * (double)sigma);
+  double sum = 0;
+  for (int i = 0; i <= 2 * R; i++) {
+    const double x = i - R;
+    k[i] = std::exp(scale2 * x * x);
+    sum += k[i];
+  }
+  for (int i = 0; i <= 2 * R; i++) taps[i] = (float)(k[i] / sum);
+  return R;
+}
+
+/* Per-axis INTER_AREA tables (same construction as the CPU restatement). */
+static void akz_area_tab(int ssize, int dsize, std::vector<int> &start, std::vector<int> &si, std::vector<float> &alpha)
+{
+  const double scale = (double)ssize / dsize;
+  for (int dx = 0; dx < dsize; dx++) {
+    start.push_back((int)si.size());
+    const double fsx1 = dx * scale;
+    const double fsx2 = fsx1 + scale;
+    const double cellWidth = std::min(scale, ssize - fsx1);
+    int sx1 = (int)std::ceil(fsx1), sx2 = (int)std::floor(fsx2);
+    sx2 = std::min(sx2, ssize - 1);
+    sx1 = std::min(sx1, sx2);
+    if (sx1 - fsx1 > 1e-3) {
+      si.push_back(sx1 - 1);
+      alpha.push_back((float)((sx1 - fsx1) / cellWidth));
+    }
+    for (int sx = sx1; sx < sx2; sx++) {
+      si.push_back(sx);
+      alpha.push_back((float)(1.0 / cellWidth));
+    }
+    if (fsx2 - sx2 > 1e-3) {
+      si.push_back(sx2);
+      alpha.push_back((float)(std::min(std::min(fsx2 - sx2, 1.), cellWidth) / cellWidth));
+    }
+  }
+  start.push_back((int)si.size());
+}
+
+static akz_status akz_validate(const akz_options *o)
+{
+  if (!o) return akz_fail(AKZ_ERR_INVALID_ARG, "options are NULL");
+  if (o->omax < 1 || o->nsublevels < 1 || o->omax * o->nsublevels > AKZ_MAX_LEVELS)
+    return akz_fail(AKZ_ERR_INVALID_ARG, "omax*nsublevels must be in [1, %d]", AKZ_MAX_LEVELS);
+  if (!(o->soffset >= 0.65f) || !(o->soffset <= 5.5f)) return akz_fail(AKZ_ERR_INVALID_ARG, "soffset must be in [0.65, 5.5]");
+  if (!(o->derivative_factor > 0.0f)) return akz_fail(AKZ_ERR_INVALID_ARG, "derivative_factor must be positive");
+  if (o->diffusivity < 0 || o->diffusivity > 3) return akz_fail(AKZ_ERR_INVALID_ARG, "unknown diffusivity %d", o->diffusivity);
+  if (o->descriptor != AKZ_MLDB && o->descriptor != AKZ_MLDB_UPRIGHT)
+    return akz_fail(AKZ_ERR_UNSUPPORTED, "descriptor %d is not implemented (MLDB and MLDB_UPRIGHT are)", o->descriptor);
+  if (o->descriptor_size != 0)
+    return akz_fail(AKZ_ERR_UNSUPPORTED, "descriptor_size %d: only the full 486-bit M-LDB is implemented", o->descriptor_size);
+  if (o->descriptor_pattern_size < 1 || o->descriptor_pattern_size > 10)
+    return akz_fail(AKZ_ERR_INVALID_ARG, "descriptor_pattern_size must be in [1, 10]");
+  if (o->kcontrast_nbins < 1 || o->kcontrast_nbins > AKZ_MAX_NBINS)
+    return akz_fail(AKZ_ERR_INVALID_ARG, "kcontrast_nbins must be in [1, %d]", AKZ_MAX_NBINS);
+  if (!(o->kcontrast_percentile >= 0.0f && o->kcontrast_percentile <= 1.0f))
+    return akz_fail(AKZ_ERR_INVALID_ARG, "kcontrast_percentile must be in [0, 1]");
+  if (o->maxkeypoints < 1) return akz_fail(AKZ_ERR_INVALID_ARG, "maxkeypoints must be positive");
+  return AKZ_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* batch                                                                    */
+
+struct akz_fed_launch {
+  int seg_off, nsegs, ntiles, tw, th;
+  akz_fed_params p;
+};
+
+struct akz_area_launch {
+  int seg_off, nsegs, maxw, maxh;
+};
+
+struct akz_batch {
+  akz_options opt;
+  int nimg = 0;
+  std::vector<int> W, H;
+  std::vector<akz_image_desc> im;
+  std::vector<akz_level_desc> lv;
+  std::vector<std::vector<akz_geo>> geo;
+  std::vector<std::vector<float>> tau; /* per level index */
+  int maxlev = 0, max_step = 1;
+  float taps0[AKZ_MAX_TAPS], taps1[AKZ_MAX_TAPS];
+  int R0 = 0;
+  /* launches */
+  std::vector<akz_tile_seg> segs;
+  int contrast_off = 0, contrast_n = 0, contrast_tiles = 0;
+  int gauss_off = 0, gauss_n = 0, gauss_tiles = 0;
+  int detect_off = 0, detect_n = 0, detect_tiles = 0;
+  int extract_off = 0, extract_n = 0, extract_rows = 0;
+  std::vector<std::vector<akz_fed_launch>> fed;  /* per level index */
+  std::vector<akz_area_launch> area;              /* per level index (nsegs 0 when none) */
+  std::vector<akz_area_seg> area_segs;
+  std::vector<int> area_start, area_si;
+  std::vector<float> area_alpha;
+  /* device */
+  char *arena = nullptr;
+  size_t arena_bytes = 0;
+  float *planes = nullptr;
+  uint8_t *u8 = nullptr;
+  float *f32 = nullptr;
+  size_t staging_elems = 0;
+  akz_level_desc *d_lv = nullptr;
+  akz_image_desc *d_im = nullptr;
+  akz_image_stats *d_stats = nullptr;
+  akz_tile_seg *d_segs = nullptr;
+  akz_area_seg *d_area_segs = nullptr;
+  int *d_area_start = nullptr, *d_area_si = nullptr;
+  float *d_area_alpha = nullptr;
+  unsigned int *d_hist = nullptr;
+  float2 *d_kc = nullptr;
+  uint32_t *d_bitmap = nullptr;
+  size_t bitmap_words = 0;
+  int *d_rowcnt = nullptr, *d_rowscan = nullptr;
+  size_t rows_all = 0;
+  akz_raw *d_raw = nullptr;
+  int *d_state = nullptr, *d_aux = nullptr;
+  signed char *d_dec = nullptr;
+  akz_kp *d_kp = nullptr;
+  uint32_t *d_desc = nullptr;
+  size_t raw_all = 0;
+  int input_f32 = 0;
+  cudaStream_t stream = nullptr, own_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_f32 = -1;
+  cudaStream_t graph_stream = nullptr;
+  akz_image_stats *h_stats = nullptr;
+  int nsm = 152;
+  cudaEvent_t ev[8] = {};
+};
+
+static size_t akz_align(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+static akz_tables akz_make_tables(const akz_batch *b)
+{
+  akz_tables t;
+  t.lv = b->d_lv;
+  t.im = b->d_im;
+  t.stats = b->d_stats;
+  t.planes = b->planes;
+  t.u8 = b->u8;
+  t.f32 = b->f32;
+  t.input_f32 = b->input_f32;
+  t.nimg = b->nimg;
+  return t;
+}
+
+static void akz_batch_free(akz_batch *b)
+{
+  if (!b) return;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->arena) cudaFree(b->arena);
+  if (b->f32) cudaFree(b->f32);
+  if (b->h_stats) cudaFreeHost(b->h_stats);
+  for (auto &e : b->ev)
+    if (e) cudaEventDestroy(e);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+}
+
+static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, const int *Hs, akz_batch **out)
+{
+  akz_status st = akz_validate(opt);
+  if (st != AKZ_OK) return st;
+  if (n < 1 || !Ws || !Hs || !out) return akz_fail(AKZ_ERR_INVALID_ARG, "batch needs at least one image and size arrays");
+  akz_batch *b = new (std::nothrow) akz_batch();
+  if (!b) return akz_fail(AKZ_ERR_OOM, "host allocation failed");
+  b->opt = *opt;
+  b->nimg = n;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev);
+  b->R0 = akz_gauss_taps(opt->soffset, b->taps0);
+  if (akz_gauss_taps(1.0f, b->taps1) != 2 || b->R0 < 0) {
+    akz_batch_free(b);
+    return akz_fail(AKZ_ERR_INVALID_ARG, "Gaussian radius out of range");
+  }
+  /* geometry */
+  b->geo.resize(n);
+  for (int i = 0; i < n; i++) {
+    if (Ws[i] < 16 || Hs[i] < 16 || Ws[i] > 32768 || Hs[i] > 32768) {
+      akz_batch_free(b);
+      return akz_fail(AKZ_ERR_INVALID_ARG, "image %d: size %dx%d outside [16, 32768]", i, Ws[i], Hs[i]);
+    }
+    b->W.push_back(Ws[i]);
+    b->H.push_back(Hs[i]);
+    std::vector<std::vector<float>> tau;
+    akz_plan_levels(*opt, Ws[i], Hs[i], b->geo[i], tau);
+    if ((int)b->geo[i].size() > b->maxlev) {
+      b->maxlev = (int)b->geo[i].size();
+      b->tau = tau;
+    }
+    for (auto &g : b->geo[i]) {
+      if (g.deriv_step < 1 || g.w < 2 * g.deriv_step + 2 || g.h < 2 * g.deriv_step + 2) {
+        akz_batch_free(b);
+        return akz_fail(AKZ_ERR_INVALID_ARG, "image %d: level %dx%d too small for derivative step %d", i, g.w, g.h, g.deriv_step);
+      }
+      b->max_step = std::max(b->max_step, g.deriv_step);
+    }
+  }
+  if (b->max_step > 16) {
+    akz_batch_free(b);
+    return akz_fail(AKZ_ERR_UNSUPPORTED, "derivative step %d above 16", b->max_step);
+  }
+  /* arena layout */
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = akz_align(off + bytes, 256);
+    return o;
+  };
+  size_t plane_floats = 0;
+  long long rows = 0;
+  size_t bitmap = 0, raw = 0, staging = 0;
+  for (int i = 0; i < n; i++) {
+    akz_image_desc I;
+    memset(&I, 0, sizeof(I));
+    I.width = Ws[i];
+    I.height = Hs[i];
+    I.nlev = (int)b->geo[i].size();
+    I.first_level = (int)b->lv.size();
+    I.u8_pitch = (int)akz_align(Ws[i], 16);
+    I.u8_off = (long long)staging;
+    staging += (size_t)I.u8_pitch * Hs[i];
+    I.rows_base = rows;
+    int rt = 0;
+    for (int l = 0; l < I.nlev; l++) {
+      const akz_geo &g = b->geo[i][l];
+      akz_level_desc L;
+      memset(&L, 0, sizeof(L));
+      L.width = g.w;
+      L.height = g.h;
+      L.pitch = (int)akz_align(g.w, 32);
+      L.image = i;
+      L.level = l;
+      L.octave = g.octave;
+      L.sublevel = g.sublevel;
+      L.deriv_step = g.deriv_step;
+      L.border = g.border;
+      L.size = g.size;
+      const size_t pf = (size_t)L.pitch * g.h;
+      L.lt = (long long)plane_floats;
+      plane_floats += pf;
+      if (l == 0) {
+        L.ls = L.lt;
+      } else {
+        L.ls = (long long)plane_floats;
+        plane_floats += pf;
+      }
+      L.lx = (long long)plane_floats;
+      plane_floats += pf;
+      L.ly = (long long)plane_floats;
+      plane_floats += pf;
+      L.rows = rows + rt;
+      rt += g.h;
+      L.bitmap_pitch = (g.w + 31) / 32;
+      L.bitmap = (long long)bitmap;
+      bitmap += (size_t)L.bitmap_pitch * g.h;
+      b->lv.push_back(L);
+    }
+    I.rows_total = rt;
+    rows += rt + 1;
+    const size_t p0 = (size_t)akz_align(Ws[i], 32) * Hs[i];
+    I.t1 = (long long)plane_floats;
+    plane_floats += p0;
+    I.t2 = (long long)plane_floats;
+    plane_floats += p0;
+    I.g = (long long)plane_floats;
+    plane_floats += p0;
+    I.raw_cap = opt->maxkeypoints;
+    I.kp_cap = opt->maxkeypoints;
+    I.raw_base = (long long)raw;
+    I.kp_base = (long long)raw;
+    raw += (size_t)opt->maxkeypoints;
+    b->im.push_back(I);
+  }
+  b->rows_all = (size_t)rows;
+  b->bitmap_words = bitmap;
+  b->raw_all = raw;
+  b->staging_elems = staging;
+
+  /* launch segments */
+  auto add_tiles = [&](int ld_or_img, int w, int h, int tw, int th, int aux, int &ntiles) {
+    akz_tile_seg s;
+    s.level_desc = ld_or_img;
+    s.tiles_x = (w + tw - 1) / tw;
+    s.tile_begin = ntiles;
+    s.aux = aux;
+    ntiles += s.tiles_x * ((h + th - 1) / th);
+    b->segs.push_back(s);
+  };
+  b->contrast_off = (int)b->segs.size();
+  for (int i = 0; i < n; i++) add_tiles(i, Ws[i], Hs[i], AKZ_CONTRAST_TW, AKZ_CONTRAST_TH, 0, b->contrast_tiles);
+  b->contrast_n = (int)b->segs.size() - b->contrast_off;
+  b->gauss_off = (int)b->segs.size();
+  for (int i = 0; i < n; i++) add_tiles(b->im[i].first_level, Ws[i], Hs[i], AKZ_GAUSS_TW, AKZ_GAUSS_TH, 0, b->gauss_tiles);
+  b->gauss_n = (int)b->segs.size() - b->gauss_off;
+
+  b->fed.resize(b->maxlev);
+  b->area.resize(b->maxlev);
+  for (int l = 1; l < b->maxlev; l++) {
+    const int nsteps = (int)b->tau[l].size();
+    const int nch = std::max(1, (nsteps + 7) / 8);
+    /* area tables for octave starts whose predecessor is not exactly 2x */
+    akz_area_launch al{(int)b->area_segs.size(), 0, 0, 0};
+    for (int i = 0; i < n; i++) {
+      if (b->im[i].nlev <= l) continue;
+      const akz_geo &g = b->geo[i][l], &gp = b->geo[i][l - 1];
+      if (g.octave > gp.octave && !(gp.w == 2 * g.w && gp.h == 2 * g.h)) {
+        akz_area_seg as;
+        as.ld = b->im[i].first_level + l;
+        as.xs = (int)b->area_start.size();
+        akz_area_tab(gp.w, g.w, b->area_start, b->area_si, b->area_alpha);
+        as.ys = (int)b->area_start.size();
+        akz_area_tab(gp.h, g.h, b->area_start, b->area_si, b->area_alpha);
+        as.pad = 0;
+        b->area_segs.push_back(as);
+        al.nsegs++;
+        al.maxw = std::max(al.maxw, g.w);
+        al.maxh = std::max(al.maxh, g.h);
+      }
+    }
+    b->area[l] = al;
+    int done = 0;
+    for (int c = 0; c < nch; c++) {
+      const int steps = (nsteps - done + (nch - c) - 1) / (nch - c);
+      akz_fed_launch fl;
+      memset(&fl, 0, sizeof(fl));
+      fl.tw = steps <= 4 ? 128 : 64;
+      fl.th = 32;
+      fl.seg_off = (int)b->segs.size();
+      for (int i = 0; i < n; i++) {
+        if (b->im[i].nlev <= l) continue;
+        const akz_geo &g = b->geo[i][l], &gp = b->geo[i][l - 1];
+        int src = 0;
+        if (g.octave > gp.octave) src = (gp.w == 2 * g.w && gp.h == 2 * g.h) ? 1 : 2;
+        add_tiles(b->im[i].first_level + l, g.w, g.h, fl.tw, fl.th, src, fl.ntiles);
+      }
+      fl.nsegs = (int)b->segs.size() - fl.seg_off;
+      fl.p.steps = steps;
+      fl.p.first = c == 0;
+      fl.p.src = c == 0 ? 0 : ((c - 1) % 2 == 0 ? 1 : 2);
+      fl.p.dst = c == nch - 1 ? 0 : (c % 2 == 0 ? 1 : 2);
+      fl.p.write_g = (c == 0 && nch > 1) ? 1 : 0;
+      fl.p.diffusivity = opt->diffusivity;
+      for (int k = 0; k < 5; k++) fl.p.taps1[k] = b->taps1[k];
+      for (int k = 0; k < steps; k++) fl.p.h[k] = 0.5f * b->tau[l][done + k];
+      done += steps;
+      b->fed[l].push_back(fl);
+    }
+  }
+  b->detect_off = (int)b->segs.size();
+  for (int i = 0; i < n; i++)
+    for (int l = 0; l < b->im[i].nlev; l++)
+      add_tiles(b->im[i].first_level + l, b->geo[i][l].w, b->geo[i][l].h, AKZ_DETECT_TW, AKZ_DETECT_TH, 0, b->detect_tiles);
+  b->detect_n = (int)b->segs.size() - b->detect_off;
+  b->extract_off = (int)b->segs.size();
+  for (int i = 0; i < n; i++)
+    for (int l = 0; l < b->im[i].nlev; l++) {
+      akz_tile_seg s;
+      s.level_desc = b->im[i].first_level + l;
+      s.tiles_x = 1;
+      s.tile_begin = b->extract_rows;
+      s.aux = 0;
+      b->extract_rows += b->geo[i][l].h;
+      b->segs.push_back(s);
+    }
+  b->extract_n = (int)b->segs.size() - b->extract_off;
+
+  /* arena */
+  const size_t o_planes = take(plane_floats * sizeof(float));
+  const size_t o_u8 = take(staging);
+  const size_t o_lv = take(b->lv.size() * sizeof(akz_level_desc));
+  const size_t o_im = take(b->im.size() * sizeof(akz_image_desc));
+  const size_t o_stats = take((size_t)n * sizeof(akz_image_stats));
+  const size_t o_segs = take(b->segs.size() * sizeof(akz_tile_seg));
+  const size_t o_aseg = take(std::max<size_t>(1, b->area_segs.size()) * sizeof(akz_area_seg));
+  const size_t o_astart = take(std::max<size_t>(1, b->area_start.size()) * sizeof(int));
+  const size_t o_asi = take(std::max<size_t>(1, b->area_si.size()) * sizeof(int));
+  const size_t o_aalpha = take(std::max<size_t>(1, b->area_alpha.size()) * sizeof(float));
+  const size_t o_hist = take((size_t)n * opt->kcontrast_nbins * sizeof(unsigned int));
+  const size_t o_kc = take((size_t)n * 16 * sizeof(float2));
+  const size_t o_bitmap = take(bitmap * sizeof(uint32_t));
+  const size_t o_rowcnt = take(b->rows_all * sizeof(int));
+  const size_t o_rowscan = take(b->rows_all * sizeof(int));
+  const size_t o_raw = take(raw * sizeof(akz_raw));
+  const size_t o_state = take(raw * sizeof(int));
+  const size_t o_aux = take(raw * sizeof(int));
+  const size_t o_dec = take(raw);
+  const size_t o_kp = take(raw * sizeof(akz_kp));
+  const size_t o_desc = take(raw * 64);
+  b->arena_bytes = off;
+  cudaError_t e = cudaMalloc(&b->arena, b->arena_bytes);
+  if (e != cudaSuccess) {
+    akz_batch_free(b);
+    return akz_fail(AKZ_ERR_OOM, "cudaMalloc of %.1f MB failed: %s", b->arena_bytes / 1048576.0, cudaGetErrorString(e));
+  }
+  char *a = b->arena;
+  b->planes = (float *)(a + o_planes);
+  b->u8 = (uint8_t *)(a + o_u8);
+  b->d_lv = (akz_level_desc *)(a + o_lv);
+  b->d_im = (akz_image_desc *)(a + o_im);
+  b->d_stats = (akz_image_stats *)(a + o_stats);
+  b->d_segs = (akz_tile_seg *)(a + o_segs);
+  b->d_area_segs = (akz_area_seg *)(a + o_aseg);
+  b->d_area_start = (int *)(a + o_astart);
+  b->d_area_si = (int *)(a + o_asi);
+  b->d_area_alpha = (float *)(a + o_aalpha);
+  b->d_hist = (unsigned int *)(a + o_hist);
+  b->d_kc = (float2 *)(a + o_kc);
+  b->d_bitmap = (uint32_t *)(a + o_bitmap);
+  b->d_rowcnt = (int *)(a + o_rowcnt);
+  b->d_rowscan = (int *)(a + o_rowscan);
+  b->d_raw = (akz_raw *)(a + o_raw);
+  b->d_state = (int *)(a + o_state);
+  b->d_aux = (int *)(a + o_aux);
+  b->d_dec = (signed char *)(a + o_dec);
+  b->d_kp = (akz_kp *)(a + o_kp);
+  b->d_desc = (uint32_t *)(a + o_desc);
+  e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_stats, (size_t)n * sizeof(akz_image_stats));
+  for (auto &ev : b->ev)
+    if (e == cudaSuccess) e = cudaEventCreate(&ev);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_lv, b->lv.data(), b->lv.size() * sizeof(akz_level_desc), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_im, b->im.data(), b->im.size() * sizeof(akz_image_desc), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_segs, b->segs.data(), b->segs.size() * sizeof(akz_tile_seg), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !b->area_segs.empty()) {
+    e = cudaMemcpy(b->d_area_segs, b->area_segs.data(), b->area_segs.size() * sizeof(akz_area_seg), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_area_start, b->area_start.data(), b->area_start.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_area_si, b->area_si.data(), b->area_si.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_area_alpha, b->area_alpha.data(), b->area_alpha.size() * sizeof(float), cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) e = cudaMemset(b->u8, 0, staging);
+  if (e != cudaSuccess) {
+    akz_batch_free(b);
+    return akz_fail_cuda(e, "batch set-up", __FILE__, __LINE__);
+  }
+  b->stream = b->own_stream;
+  *out = b;
+  return AKZ_OK;
+}
+
+/* stage groups ------------------------------------------------------------ */
+
+static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s)
+{
+  const akz_tables t = akz_make_tables(b);
+  CK(cudaMemsetAsync(b->d_stats, 0, (size_t)b->nimg * sizeof(akz_image_stats), s));
+  CK(cudaMemsetAsync(b->d_hist, 0, (size_t)b->nimg * b->opt.kcontrast_nbins * sizeof(unsigned int), s));
+  akz_contrast_params cp;
+  cp.t = t;
+  cp.segs = b->d_segs + b->contrast_off;
+  cp.nsegs = b->contrast_n;
+  cp.nbins = (int)b->opt.kcontrast_nbins;
+  cp.hist = b->d_hist;
+  cp.inv255 = (float)(1.0 / 255.0);
+  for (int k = 0; k < 5; k++) cp.taps[k] = b->taps1[k];
+  CK(akz_launch_contrast(cp, b->contrast_tiles, 0, s));
+  CK(akz_launch_contrast(cp, b->contrast_tiles, 1, s));
+  CK(akz_launch_contrast_final(t, b->d_hist, cp.nbins, b->opt.kcontrast_percentile, b->d_kc, s));
+  akz_gauss_params gp;
+  gp.t = t;
+  gp.segs = b->d_segs + b->gauss_off;
+  gp.nsegs = b->gauss_n;
+  gp.inv255 = cp.inv255;
+  gp.R = b->R0;
+  for (int k = 0; k <= 2 * b->R0; k++) gp.taps[k] = b->taps0[k];
+  CK(akz_launch_gauss0(gp, b->gauss_tiles, s));
+  for (int l = 1; l < b->maxlev; l++) {
+    if (b->area[l].nsegs > 0) {
+      akz_area_params ap;
+      ap.t = t;
+      ap.segs = b->d_area_segs + b->area[l].seg_off;
+      ap.nsegs = b->area[l].nsegs;
+      ap.start = b->d_area_start;
+      ap.si = b->d_area_si;
+      ap.alpha = b->d_area_alpha;
+      CK(akz_launch_area(ap, b->area[l].maxw, b->area[l].maxh, s));
+    }
+    for (auto &fl : b->fed[l]) {
+      akz_fed_params p = fl.p;
+      p.t = t;
+      p.segs = b->d_segs + fl.seg_off;
+      p.nsegs = fl.nsegs;
+      p.kc = b->d_kc;
+      CK(akz_launch_fed(p, fl.ntiles, fl.tw, fl.th, s));
+    }
+  }
+  return AKZ_OK;
+}
+
+static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s)
+{
+  const akz_tables t = akz_make_tables(b);
+  const float w = (float)(10.0 / 3.0);
+  const float fac1 = (float)(1.0 / (2.0 * ((double)w + 2.0)));
+  const float fac2 = w * fac1;
+  CK(cudaMemsetAsync(b->d_bitmap, 0, b->bitmap_words * sizeof(uint32_t), s));
+  CK(cudaMemsetAsync(b->d_rowcnt, 0, b->rows_all * sizeof(int), s));
+  akz_detect_params dp;
+  dp.t = t;
+  dp.segs = b->d_segs + b->detect_off;
+  dp.nsegs = b->detect_n;
+  dp.bitmap = b->d_bitmap;
+  dp.rowcnt = b->d_rowcnt;
+  dp.thr = std::max(b->opt.dthreshold, b->opt.min_dthreshold);
+  dp.fac1 = fac1;
+  dp.fac2 = fac2;
+  CK(akz_launch_detect(dp, b->detect_tiles, b->max_step, s));
+  CK(akz_launch_rowscan(t, b->d_rowcnt, b->d_rowscan, s));
+  akz_extract_params ep;
+  ep.t = t;
+  ep.segs = b->d_segs + b->extract_off;
+  ep.nsegs = b->extract_n;
+  ep.bitmap = b->d_bitmap;
+  ep.rowscan = b->d_rowscan;
+  ep.raw = b->d_raw;
+  ep.fac1 = fac1;
+  ep.fac2 = fac2;
+  CK(akz_launch_extract(ep, b->extract_rows, s));
+  akz_nms_params np;
+  np.t = t;
+  np.rowscan = b->d_rowscan;
+  np.raw = b->d_raw;
+  np.state = b->d_state;
+  np.aux = b->d_aux;
+  np.decision = b->d_dec;
+  np.kp = b->d_kp;
+  np.max_rounds = 1 << 20;
+  CK(akz_launch_nms(np, s));
+  return AKZ_OK;
+}
+
+static akz_status akz_stage_describe(akz_batch *b, cudaStream_t s)
+{
+  akz_describe_params p;
+  p.t = akz_make_tables(b);
+  p.kp = b->d_kp;
+  p.desc = b->d_desc;
+  p.upright = b->opt.descriptor == AKZ_MLDB_UPRIGHT;
+  p.pattern_size = b->opt.descriptor_pattern_size;
+  /* exp(-r2/12.5) with the shared deterministic exp (the CPU restatement
+   * uses the same routine), so the weights are identical on every host */
+  for (int r2 = 0; r2 < 36; r2++) p.gw[r2] = akz_expf((float)(-r2) / (2.5f * 2.5f * 2.0f));
+  CK(akz_launch_describe(p, 4 * b->nsm, s));
+  return AKZ_OK;
+}
+
+static akz_status akz_run_all(akz_batch *b, cudaStream_t s)
+{
+  akz_status st = akz_stage_scale(b, s);
+  if (st == AKZ_OK) st = akz_stage_detect(b, s);
+  if (st == AKZ_OK) st = akz_stage_describe(b, s);
+  return st;
+}
+
+/* Whole-batch run, captured once into a CUDA graph and replayed. */
+static akz_status akz_batch_launch(akz_batch *b)
+{
+  cudaStream_t s = b->stream;
+  if (b->graph && (b->graph_f32 != b->input_f32 || b->graph_stream != s)) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  if (!b->graph) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    akz_status st = akz_run_all(b, s);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (st != AKZ_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (e != cudaSuccess) return akz_fail_cuda(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      b->graph = nullptr;
+      return akz_fail_cuda(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    }
+    b->graph_f32 = b->input_f32;
+    b->graph_stream = s;
+  }
+  CK(cudaGraphLaunch(b->graph, s));
+  return AKZ_OK;
+}
+
+static akz_status akz_batch_sync_stats(akz_batch *b)
+{
+  CK(cudaMemcpyAsync(b->h_stats, b->d_stats, (size_t)b->nimg * sizeof(akz_image_stats), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < b->nimg; i++) {
+    if (b->h_stats[i].overflow)
+      return akz_fail(AKZ_ERR_OVERFLOW, "image %d: %d raw extrema exceed maxkeypoints=%d", i, b->h_stats[i].nraw, b->opt.maxkeypoints);
+    if (b->h_stats[i].status == AKZ_ERR_TIMEOUT) return akz_fail(AKZ_ERR_TIMEOUT, "image %d: suppression did not settle", i);
+  }
+  return AKZ_OK;
+}
+
+static akz_status akz_copy_results(akz_batch *b, int i, akz_keypoint *kpts, uint8_t *desc, int capacity, int *n)
+{
+  const int nk = b->h_stats[i].nkp;
+  const int m = std::min(nk, std::max(capacity, 0));
+  const akz_image_desc &I = b->im[i];
+  if (m > 0 && kpts) CK(cudaMemcpyAsync(kpts, b->d_kp + I.kp_base, (size_t)m * sizeof(akz_kp), cudaMemcpyDeviceToHost, b->stream));
+  if (m > 0 && desc)
+    CK(cudaMemcpy2DAsync(desc, 61, (const uint8_t *)b->d_desc + (size_t)I.kp_base * 64, 64, 61, m, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  if (n) *n = nk;
+  return AKZ_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* single-image context                                                     */
+
+struct akz_context {
+  akz_batch *b = nullptr;
+  int have_scale = 0, have_detect = 0;
+  akz_timing timing;
+  float *f32 = nullptr;
+};
+
+#define AKZ_GUARD(c)                                                                  \
+  do {                                                                                \
+    if (!(c)) return akz_fail(AKZ_ERR_INVALID_ARG, "%s: NULL handle", __func__); \
+  } while (0)
+
+extern "C" {
+
+AKZ_API const char *akz_version(void) { return "akaze_gb300 0.1 (sm_103a)"; }
+AKZ_API const char *akz_last_error(void) { return g_last_error.c_str(); }
+
+AKZ_API akz_status akz_options_default(akz_options *o)
+{
+  if (!o) return akz_fail(AKZ_ERR_INVALID_ARG, "options are NULL");
+  memset(o, 0, sizeof(*o));
+  o->soffset = 1.6f;
+  o->derivative_factor = 1.5f;
+  o->omax = 4;
+  o->nsublevels = 4;
+  o->dthreshold = 0.001f;
+  o->min_dthreshold = 0.00001f;
+  o->diffusivity = AKZ_PM_G2;
+  o->descriptor = AKZ_MLDB;
+  o->descriptor_size = 0;
+  o->descriptor_channels = 3;
+  o->descriptor_pattern_size = 10;
+  o->sderivatives = 1.0f;
+  o->kcontrast = 0.001f;
+  o->kcontrast_percentile = 0.7f;
+  o->kcontrast_nbins = 300;
+  o->ncudaimages = 4;
+  o->maxkeypoints = 16 * 8192;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_create(const akz_options *opt, akz_context **out)
+{
+  if (!opt || !out) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_create: NULL argument");
+  akz_context *c = new (std::nothrow) akz_context();
+  if (!c) return akz_fail(AKZ_ERR_OOM, "host allocation failed");
+  memset(&c->timing, 0, sizeof(c->timing));
+  const int w = opt->img_width, h = opt->img_height;
+  akz_status st = akz_batch_build(opt, 1, &w, &h, &c->b);
+  if (st != AKZ_OK) {
+    delete c;
+    return st;
+  }
+  *out = c;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_destroy(akz_context *c)
+{
+  if (!c) return AKZ_OK;
+  if (c->f32) cudaFree(c->f32);
+  akz_batch_free(c->b);
+  delete c;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_set_stream(akz_context *c, void *stream)
+{
+  AKZ_GUARD(c);
+  c->b->stream = stream ? (cudaStream_t)stream : c->b->own_stream;
+  return AKZ_OK;
+}
+
+static float akz_ms(cudaEvent_t a, cudaEvent_t b)
+{
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+AKZ_API akz_status akz_create_nonlinear_scale_space(akz_context *c, const void *img, int width, int height, size_t stride,
+                                                    int dtype, int on_device)
+{
+  AKZ_GUARD(c);
+  akz_batch *b = c->b;
+  if (!img) return akz_fail(AKZ_ERR_INVALID_ARG, "image is NULL");
+  if (width != b->W[0] || height != b->H[0])
+    return akz_fail(AKZ_ERR_INVALID_ARG, "image is %dx%d but the context was created for %dx%d", width, height, b->W[0], b->H[0]);
+  if (dtype != AKZ_U8 && dtype != AKZ_F32) return akz_fail(AKZ_ERR_INVALID_ARG, "unknown dtype %d", dtype);
+  const size_t elem = dtype == AKZ_U8 ? 1 : 4;
+  if (stride < (size_t)width * elem) return akz_fail(AKZ_ERR_INVALID_ARG, "stride %zu below the row size", stride);
+  cudaStream_t s = b->stream;
+  const akz_image_desc &I = b->im[0];
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (dtype == AKZ_U8) {
+    CK(cudaMemcpy2DAsync(b->u8 + I.u8_off, I.u8_pitch, img, stride, width, height, kind, s));
+    b->input_f32 = 0;
+  } else {
+    if (!b->f32) CK(cudaMalloc(&b->f32, b->staging_elems * sizeof(float)));
+    CK(cudaMemcpy2DAsync(b->f32 + I.u8_off, (size_t)I.u8_pitch * 4, img, stride, (size_t)width * 4, height, kind, s));
+    b->input_f32 = 1;
+  }
+  CK(cudaEventRecord(b->ev[0], s));
+  akz_status st = akz_stage_scale(b, s);
+  if (st != AKZ_OK) return st;
+  CK(cudaEventRecord(b->ev[1], s));
+  CK(cudaEventSynchronize(b->ev[1]));
+  c->timing.kcontrast = 0.0;
+  c->timing.scale = akz_ms(b->ev[0], b->ev[1]);
+  c->have_scale = 1;
+  c->have_detect = 0;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_feature_detection(akz_context *c, int *n)
+{
+  AKZ_GUARD(c);
+  if (!c->have_scale) return akz_fail(AKZ_ERR_STATE, "Feature_Detection before Create_Nonlinear_Scale_Space");
+  akz_batch *b = c->b;
+  CK(cudaEventRecord(b->ev[2], b->stream));
+  akz_status st = akz_stage_detect(b, b->stream);
+  if (st != AKZ_OK) return st;
+  CK(cudaEventRecord(b->ev[3], b->stream));
+  st = akz_batch_sync_stats(b);
+  if (st != AKZ_OK) return st;
+  c->timing.detector = akz_ms(b->ev[2], b->ev[3]);
+  c->timing.derivatives = 0.0;
+  c->timing.extrema = c->timing.detector;
+  c->have_detect = 1;
+  if (n) *n = b->h_stats[0].nkp;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_compute_descriptors(akz_context *c, akz_keypoint *kpts, uint8_t *desc, int capacity, int *n)
+{
+  AKZ_GUARD(c);
+  if (!c->have_detect) return akz_fail(AKZ_ERR_STATE, "Compute_Descriptors before Feature_Detection");
+  akz_batch *b = c->b;
+  CK(cudaEventRecord(b->ev[4], b->stream));
+  akz_status st = akz_stage_describe(b, b->stream);
+  if (st != AKZ_OK) return st;
+  CK(cudaEventRecord(b->ev[5], b->stream));
+  st = akz_copy_results(b, 0, kpts, desc, capacity, n);
+  if (st != AKZ_OK) return st;
+  c->timing.descriptor = akz_ms(b->ev[4], b->ev[5]);
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_get_timing(akz_context *c, akz_timing *t)
+{
+  AKZ_GUARD(c);
+  if (!t) return akz_fail(AKZ_ERR_INVALID_ARG, "timing is NULL");
+  *t = c->timing;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_num_levels(const akz_context *c, int *n)
+{
+  AKZ_GUARD(c);
+  if (n) *n = c->b->im[0].nlev;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_level_info(const akz_context *c, int level, int *w, int *h, int *octave, int *sublevel, float *esigma, int *nsteps)
+{
+  AKZ_GUARD(c);
+  const akz_batch *b = c->b;
+  if (level < 0 || level >= b->im[0].nlev) return akz_fail(AKZ_ERR_INVALID_ARG, "level %d out of range", level);
+  const akz_geo &g = b->geo[0][level];
+  if (w) *w = g.w;
+  if (h) *h = g.h;
+  if (octave) *octave = g.octave;
+  if (sublevel) *sublevel = g.sublevel;
+  if (esigma) *esigma = g.esigma;
+  if (nsteps) *nsteps = g.nsteps;
+  return AKZ_OK;
+}
+
+static akz_status akz_plane_out(akz_batch *b, int i, int level, int plane, float *out)
+{
+  if (i < 0 || i >= b->nimg) return akz_fail(AKZ_ERR_INVALID_ARG, "image %d out of range", i);
+  if (level < 0 || level >= b->im[i].nlev) return akz_fail(AKZ_ERR_INVALID_ARG, "level %d out of range", level);
+  if (!out) return akz_fail(AKZ_ERR_INVALID_ARG, "output is NULL");
+  const akz_level_desc &L = b->lv[b->im[i].first_level + level];
+  long long off;
+  switch (plane) {
+    case AKZ_PLANE_LT: off = L.lt; break;
+    case AKZ_PLANE_LSMOOTH: off = L.ls; break;
+    case AKZ_PLANE_LX: off = L.lx; break;
+    case AKZ_PLANE_LY: off = L.ly; break;
+    default: return akz_fail(AKZ_ERR_INVALID_ARG, "unknown plane %d", plane);
+  }
+  CK(cudaMemcpy2DAsync(out, (size_t)L.width * 4, b->planes + off, (size_t)L.pitch * 4, (size_t)L.width * 4, L.height,
+                       cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_get_level_plane(akz_context *c, int level, int plane, float *out)
+{
+  AKZ_GUARD(c);
+  if (!c->have_scale) return akz_fail(AKZ_ERR_STATE, "no scale space yet");
+  return akz_plane_out(c->b, 0, level, plane, out);
+}
+
+AKZ_API akz_status akz_get_kcontrast(akz_context *c, float *k)
+{
+  AKZ_GUARD(c);
+  if (!c->have_scale) return akz_fail(AKZ_ERR_STATE, "no scale space yet");
+  akz_image_stats s;
+  CK(cudaMemcpyAsync(&s, c->b->d_stats, sizeof(s), cudaMemcpyDeviceToHost, c->b->stream));
+  CK(cudaStreamSynchronize(c->b->stream));
+  if (k) *k = s.kcontrast;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_get_extrema(akz_context *c, akz_extremum *out, int cap, int *n)
+{
+  AKZ_GUARD(c);
+  if (!c->have_detect) return akz_fail(AKZ_ERR_STATE, "no detection yet");
+  akz_batch *b = c->b;
+  const int nr = b->h_stats[0].nraw;
+  const int m = std::min(nr, std::max(cap, 0));
+  if (m > 0 && out) {
+    CK(cudaMemcpyAsync(out, b->d_raw + b->im[0].raw_base, (size_t)m * sizeof(akz_raw), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+  }
+  if (n) *n = nr;
+  return AKZ_OK;
+}
+
+/* ---- batch ---------------------------------------------------------------- */
+
+AKZ_API akz_status akz_batch_create(const akz_options *opt, int n, const int *w, const int *h, akz_batch **out)
+{
+  if (!out) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_batch_create: NULL output");
+  return akz_batch_build(opt, n, w, h, out);
+}
+
+AKZ_API akz_status akz_batch_destroy(akz_batch *b)
+{
+  akz_batch_free(b);
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_batch_set_stream(akz_batch *b, void *stream)
+{
+  AKZ_GUARD(b);
+  b->stream = stream ? (cudaStream_t)stream : b->own_stream;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_batch_upload(akz_batch *b, const uint8_t *const *images, const size_t *strides, int on_device)
+{
+  AKZ_GUARD(b);
+  if (!images || !strides) return akz_fail(AKZ_ERR_INVALID_ARG, "images/strides are NULL");
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  for (int i = 0; i < b->nimg; i++) {
+    if (!images[i] || strides[i] < (size_t)b->W[i]) return akz_fail(AKZ_ERR_INVALID_ARG, "image %d: bad pointer or stride", i);
+    const akz_image_desc &I = b->im[i];
+    CK(cudaMemcpy2DAsync(b->u8 + I.u8_off, I.u8_pitch, images[i], strides[i], b->W[i], b->H[i], kind, b->stream));
+  }
+  b->input_f32 = 0;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_batch_input(akz_batch *b, int i, uint8_t **dptr, size_t *pitch)
+{
+  AKZ_GUARD(b);
+  if (i < 0 || i >= b->nimg) return akz_fail(AKZ_ERR_INVALID_ARG, "image %d out of range", i);
+  if (dptr) *dptr = b->u8 + b->im[i].u8_off;
+  if (pitch) *pitch = (size_t)b->im[i].u8_pitch;
+  b->input_f32 = 0;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_batch_run(akz_batch *b)
+{
+  AKZ_GUARD(b);
+  return akz_batch_launch(b);
+}
+
+AKZ_API akz_status akz_batch_counts(akz_batch *b, int *counts)
+{
+  AKZ_GUARD(b);
+  akz_status st = akz_batch_sync_stats(b);
+  if (st != AKZ_OK) return st;
+  if (counts)
+    for (int i = 0; i < b->nimg; i++) counts[i] = b->h_stats[i].nkp;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_batch_results(akz_batch *b, int i, akz_keypoint *kpts, uint8_t *desc, int capacity, int *n)
+{
+  AKZ_GUARD(b);
+  if (i < 0 || i >= b->nimg) return akz_fail(AKZ_ERR_INVALID_ARG, "image %d out of range", i);
+  akz_status st = akz_batch_sync_stats(b);
+  if (st != AKZ_OK) return st;
+  return akz_copy_results(b, i, kpts, desc, capacity, n);
+}
+
+AKZ_API akz_status akz_batch_device_results(akz_batch *b, int i, akz_keypoint **kpts, uint8_t **desc64)
+{
+  AKZ_GUARD(b);
+  if (i < 0 || i >= b->nimg) return akz_fail(AKZ_ERR_INVALID_ARG, "image %d out of range", i);
+  if (kpts) *kpts = (akz_keypoint *)(b->d_kp + b->im[i].kp_base);
+  if (desc64) *desc64 = (uint8_t *)b->d_desc + (size_t)b->im[i].kp_base * 64;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_batch_detect_describe(akz_batch *b, const uint8_t *const *images, const size_t *strides,
+                                             akz_keypoint *const *kpts, uint8_t *const *desc, const int *caps, int *counts)
+{
+  AKZ_GUARD(b);
+  akz_status st = akz_batch_upload(b, images, strides, 0);
+  if (st == AKZ_OK) st = akz_batch_launch(b);
+  if (st == AKZ_OK) st = akz_batch_sync_stats(b);
+  if (st != AKZ_OK) return st;
+  for (int i = 0; i < b->nimg; i++) {
+    const int nk = b->h_stats[i].nkp;
+    const int m = std::min(nk, caps ? std::max(caps[i], 0) : 0);
+    const akz_image_desc &I = b->im[i];
+    if (m > 0 && kpts && kpts[i])
+      CK(cudaMemcpyAsync(kpts[i], b->d_kp + I.kp_base, (size_t)m * sizeof(akz_kp), cudaMemcpyDeviceToHost, b->stream));
+    if (m > 0 && desc && desc[i])
+      CK(cudaMemcpy2DAsync(desc[i], 61, (const uint8_t *)b->d_desc + (size_t)I.kp_base * 64, 64, 61, m, cudaMemcpyDeviceToHost, b->stream));
+    if (counts) counts[i] = nk;
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_batch_level_plane(akz_batch *b, int i, int level, int plane, float *out)
+{
+  AKZ_GUARD(b);
+  return akz_plane_out(b, i, level, plane, out);
+}
+
+/* ---- matcher ------------------------------------------------------------ */
+
+struct akz_matcher {
+  cudaStream_t stream = nullptr, own = nullptr;
+  void *dq = nullptr, *dt = nullptr, *dout = nullptr, *dpart = nullptr;
+  size_t capq = 0, capt = 0, capout = 0, cappart = 0;
+  int nsm = 152;
+};
+
+AKZ_API akz_status akz_matcher_create(akz_matcher **out)
+{
+  if (!out) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_matcher_create: NULL output");
+  akz_matcher *m = new (std::nothrow) akz_matcher();
+  if (!m) return akz_fail(AKZ_ERR_OOM, "host allocation failed");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&m->nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaStreamCreateWithFlags(&m->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete m;
+    return akz_fail_cuda(e, "cudaStreamCreate", __FILE__, __LINE__);
+  }
+  m->stream = m->own;
+  *out = m;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_matcher_destroy(akz_matcher *m)
+{
+  if (!m) return AKZ_OK;
+  cudaFree(m->dq);
+  cudaFree(m->dt);
+  cudaFree(m->dout);
+  cudaFree(m->dpart);
+  if (m->own) cudaStreamDestroy(m->own);
+  delete m;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_matcher_set_stream(akz_matcher *m, void *stream)
+{
+  AKZ_GUARD(m);
+  m->stream = stream ? (cudaStream_t)stream : m->own;
+  return AKZ_OK;
+}
+
+static akz_status akz_grow(void **p, size_t *cap, size_t need)
+{
+  if (need <= *cap) return AKZ_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  const size_t n = std::max<size_t>(need, 4096);
+  CK(cudaMalloc(p, n));
+  *cap = n;
+  return AKZ_OK;
+}
+
+static akz_status akz_match_device(akz_matcher *m, const void *dq, int nq, const void *dt, int nt, void *dout)
+{
+  const int ns = akz_match_splits(nq, nt, m->nsm);
+  if (ns > 1) {
+    akz_status st = akz_grow(&m->dpart, &m->cappart, akz_match_partial_bytes(nq, ns));
+    if (st != AKZ_OK) return st;
+  }
+  CK(akz_match_run(dq, nq, dt, nt, dout, m->dpart, ns, m->stream));
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_matcher_bfmatch(akz_matcher *m, const uint8_t *q, int nq, const uint8_t *t, int nt, int row_bytes, akz_dmatch *out)
+{
+  AKZ_GUARD(m);
+  if (nq < 0 || nt < 0 || row_bytes < 1 || row_bytes > 64) return akz_fail(AKZ_ERR_INVALID_ARG, "bad matcher sizes");
+  if ((nq > 0 && (!q || !out)) || (nt > 0 && !t)) return akz_fail(AKZ_ERR_INVALID_ARG, "NULL matcher buffer");
+  if (nq == 0) return AKZ_OK;
+  akz_status st = akz_grow(&m->dq, &m->capq, (size_t)nq * 64);
+  if (st == AKZ_OK) st = akz_grow(&m->dt, &m->capt, (size_t)std::max(nt, 1) * 64);
+  if (st == AKZ_OK) st = akz_grow(&m->dout, &m->capout, (size_t)nq * 2 * sizeof(akz_dmatch));
+  if (st != AKZ_OK) return st;
+  CK(cudaMemsetAsync(m->dq, 0, (size_t)nq * 64, m->stream));
+  CK(cudaMemcpy2DAsync(m->dq, 64, q, row_bytes, row_bytes, nq, cudaMemcpyHostToDevice, m->stream));
+  if (nt > 0) {
+    CK(cudaMemsetAsync(m->dt, 0, (size_t)nt * 64, m->stream));
+    CK(cudaMemcpy2DAsync(m->dt, 64, t, row_bytes, row_bytes, nt, cudaMemcpyHostToDevice, m->stream));
+  }
+  st = akz_match_device(m, m->dq, nq, m->dt, nt, m->dout);
+  if (st != AKZ_OK) return st;
+  CK(cudaMemcpyAsync(out, m->dout, (size_t)nq * 2 * sizeof(akz_dmatch), cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *q64, int nq, const uint8_t *t64, int nt, akz_dmatch *out)
+{
+  AKZ_GUARD(m);
+  if (nq < 0 || nt < 0) return akz_fail(AKZ_ERR_INVALID_ARG, "bad matcher sizes");
+  if (nq == 0) return AKZ_OK;
+  if (!q64 || !out || (nt > 0 && !t64)) return akz_fail(AKZ_ERR_INVALID_ARG, "NULL matcher buffer");
+  return akz_match_device(m, q64, nq, t64, nt, out);
+}
+
+} /* extern "C" */

@@ -1,0 +1,136 @@
+/*
+ * akz_kernels.h - launch parameters and launchers of the akaze_gb300 kernels.
+ * Every launcher enqueues on the given stream and returns the launch error.
+ */
+#ifndef AKZ_KERNELS_H
+#define AKZ_KERNELS_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "akz_internal.h"
+
+#define AKZ_MAX_TAPS 33 /* Gaussian radius up to 16 */
+#define AKZ_MAX_CHUNK 32
+
+struct akz_tables {
+  const akz_level_desc *lv;
+  const akz_image_desc *im;
+  akz_image_stats *stats;
+  float *planes;
+  const uint8_t *u8;
+  const float *f32;    /* float input staging (when the input is f32) */
+  int input_f32;
+  int nimg;
+};
+
+struct akz_contrast_params {
+  akz_tables t;
+  const akz_tile_seg *segs;
+  int nsegs;
+  int nbins;
+  unsigned int *hist; /* nimg x nbins */
+  float inv255;
+  float taps[5];      /* sigma 1, radius 2 */
+};
+
+struct akz_gauss_params {
+  akz_tables t;
+  const akz_tile_seg *segs;
+  int nsegs;
+  float inv255;
+  int R;
+  float taps[AKZ_MAX_TAPS];
+};
+
+struct akz_fed_params {
+  akz_tables t;
+  const akz_tile_seg *segs;
+  int nsegs;
+  const float2 *kc;   /* per image x 16 octaves: (k, 1/k^2) */
+  int steps;          /* FED steps in this launch */
+  int first;          /* 1: start from the predecessor (copy / 2x half-sample / prepared T2) */
+  int src;            /* first: 0 predecessor Lt, 1 2x half-sample of it, 2 prepared T2; else 1 T1, 2 T2 */
+  int dst;            /* 0 Lt of the level, 1 T1, 2 T2 */
+  int write_g;        /* store the conductance for later launches */
+  int diffusivity;
+  float taps1[5];
+  float h[AKZ_MAX_CHUNK]; /* 0.5 * tau per step */
+};
+
+/* INTER_AREA tables of one octave start: start[] indices are absolute into
+ * si/alpha; xs/ys are offsets of the per-axis start arrays in start[]. */
+struct akz_area_seg {
+  int ld; /* level descriptor of the octave-start level */
+  int xs, ys;
+  int pad;
+};
+
+struct akz_area_params {
+  akz_tables t;
+  const akz_area_seg *segs;
+  int nsegs;
+  const int *start;
+  const int *si;
+  const float *alpha;
+};
+
+struct akz_detect_params {
+  akz_tables t;
+  const akz_tile_seg *segs;
+  int nsegs;
+  uint32_t *bitmap;
+  int *rowcnt;
+  float thr, fac1, fac2;
+};
+
+struct akz_extract_params {
+  akz_tables t;
+  const akz_tile_seg *segs; /* one entry per (image, level); tiles = rows */
+  int nsegs;
+  const uint32_t *bitmap;
+  const int *rowscan;
+  akz_raw *raw;
+  float fac1, fac2;
+};
+
+struct akz_nms_params {
+  akz_tables t;
+  const int *rowscan;
+  const akz_raw *raw;
+  int *state;
+  int *aux; /* minimum challenger per slot */
+  signed char *decision;
+  akz_kp *kp;
+  int max_rounds;
+};
+
+struct akz_describe_params {
+  akz_tables t;
+  akz_kp *kp;
+  uint32_t *desc; /* 16 words per keypoint */
+  int upright;
+  int pattern_size;
+  float gw[36];   /* Gaussian weights exp(-r2/12.5) of the orientation samples */
+};
+
+cudaError_t akz_launch_contrast(const akz_contrast_params &p, int ntiles, int pass, cudaStream_t s);
+cudaError_t akz_launch_contrast_final(const akz_tables &t, const unsigned int *hist, int nbins, float perc, float2 *kc, cudaStream_t s);
+cudaError_t akz_launch_gauss0(const akz_gauss_params &p, int ntiles, cudaStream_t s);
+cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int tw, int th, cudaStream_t s);
+size_t akz_fed_smem_bytes(int tw, int th, int steps, int first);
+cudaError_t akz_launch_area(const akz_area_params &p, int maxw, int maxh, cudaStream_t s);
+cudaError_t akz_launch_detect(const akz_detect_params &p, int ntiles, int max_step, cudaStream_t s);
+cudaError_t akz_launch_rowscan(const akz_tables &t, const int *rowcnt, int *rowscan, cudaStream_t s);
+cudaError_t akz_launch_extract(const akz_extract_params &p, int nrows, cudaStream_t s);
+cudaError_t akz_launch_nms(const akz_nms_params &p, cudaStream_t s);
+cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaStream_t s);
+
+#define AKZ_DETECT_TW 32
+#define AKZ_DETECT_TH 32
+#define AKZ_GAUSS_TW 64
+#define AKZ_GAUSS_TH 32
+#define AKZ_CONTRAST_TW 64
+#define AKZ_CONTRAST_TH 32
+
+#endif

@@ -1,0 +1,125 @@
+/*
+ * akz_match.cu - brute-force 2-NN Hamming matcher on 64-byte rows.
+ *
+ * Reference: MatchDescriptors, cuda_akaze.cu:1843-1967, and Matcher::bfmatch,
+ * AKAZE.cpp:36-79.  For every query the closest and second-closest train rows
+ * by Hamming distance; equal distances go to the lower train index (the
+ * cv::BFMatcher knnMatch rule), a missing candidate is {trainIdx 0,
+ * distance 512}.
+ *
+ * Layout: one query per thread (its 512 bits in 16 registers), train rows
+ * staged through shared memory 256 at a time and read as broadcasts, 16
+ * xor+popc per pair.  The train set is split across blockIdx.y so that small
+ * query sets still fill the GPU; the per-split top-2 lists are merged in
+ * split order with a (distance, index) comparison, which equals one
+ * sequential scan.
+ */
+#include <cuda_runtime.h>
+
+#include "akz_device.cuh"
+
+#define AKZ_MQ 256
+#define AKZ_MT 256
+
+struct akz_top2 {
+  int bd, bi, sd, si;
+};
+
+__device__ __forceinline__ bool akz_lex_less(int d1, int i1, int d2, int i2) { return d1 < d2 || (d1 == d2 && i1 < i2); }
+
+__global__ void __launch_bounds__(AKZ_MQ) k_match(const uint4 *__restrict__ q, const uint4 *__restrict__ t, int nq, int nt,
+                                                  int split_len, int nsplit, akz_top2 *partial, int4 *out)
+{
+  __shared__ uint4 sT[AKZ_MT * 4];
+  const int qi = blockIdx.x * AKZ_MQ + threadIdx.x;
+  uint4 a0 = make_uint4(0, 0, 0, 0), a1 = a0, a2 = a0, a3 = a0;
+  if (qi < nq) {
+    a0 = __ldg(q + (long long)qi * 4 + 0);
+    a1 = __ldg(q + (long long)qi * 4 + 1);
+    a2 = __ldg(q + (long long)qi * 4 + 2);
+    a3 = __ldg(q + (long long)qi * 4 + 3);
+  }
+  const int j0 = blockIdx.y * split_len, j1 = min(nt, j0 + split_len);
+  int bd = 512, bi = 0, sd = 512, si = 0;
+  for (int tile = j0; tile < j1; tile += AKZ_MT) {
+    const int cnt = min(AKZ_MT, j1 - tile);
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt * 4; i += AKZ_MQ) sT[i] = __ldg(t + (long long)tile * 4 + i);
+    __syncthreads();
+#pragma unroll 4
+    for (int r = 0; r < cnt; r++) {
+      const uint4 b0 = sT[r * 4 + 0], b1 = sT[r * 4 + 1], b2 = sT[r * 4 + 2], b3 = sT[r * 4 + 3];
+      int d = __popc(a0.x ^ b0.x) + __popc(a0.y ^ b0.y) + __popc(a0.z ^ b0.z) + __popc(a0.w ^ b0.w);
+      d += __popc(a1.x ^ b1.x) + __popc(a1.y ^ b1.y) + __popc(a1.z ^ b1.z) + __popc(a1.w ^ b1.w);
+      d += __popc(a2.x ^ b2.x) + __popc(a2.y ^ b2.y) + __popc(a2.z ^ b2.z) + __popc(a2.w ^ b2.w);
+      d += __popc(a3.x ^ b3.x) + __popc(a3.y ^ b3.y) + __popc(a3.z ^ b3.z) + __popc(a3.w ^ b3.w);
+      const int j = tile + r;
+      if (d < bd) {
+        sd = bd;
+        si = bi;
+        bd = d;
+        bi = j;
+      } else if (d < sd) {
+        sd = d;
+        si = j;
+      }
+    }
+  }
+  if (qi >= nq) return;
+  if (nsplit == 1) {
+    out[2 * qi] = make_int4(qi, bi, 0, __float_as_int((float)bd));
+    out[2 * qi + 1] = make_int4(qi, si, 0, __float_as_int((float)sd));
+  } else {
+    partial[(long long)qi * nsplit + blockIdx.y] = akz_top2{bd, bi, sd, si};
+  }
+}
+
+__global__ void k_match_merge(const akz_top2 *partial, int nq, int nsplit, int4 *out)
+{
+  const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (qi >= nq) return;
+  akz_top2 r = partial[(long long)qi * nsplit];
+  for (int s = 1; s < nsplit; s++) {
+    const akz_top2 o = partial[(long long)qi * nsplit + s];
+    /* candidates: r.b, r.s, o.b, o.s ; r entries come from lower indices */
+    int c[4][2] = {{r.bd, r.bi}, {r.sd, r.si}, {o.bd, o.bi}, {o.sd, o.si}};
+    int b = 0;
+    for (int k = 1; k < 4; k++)
+      if (akz_lex_less(c[k][0], c[k][1], c[b][0], c[b][1])) b = k;
+    int s2 = b == 0 ? 1 : 0;
+    for (int k = 0; k < 4; k++)
+      if (k != b && akz_lex_less(c[k][0], c[k][1], c[s2][0], c[s2][1])) s2 = k;
+    r = akz_top2{c[b][0], c[b][1], c[s2][0], c[s2][1]};
+  }
+  out[2 * qi] = make_int4(qi, r.bi, 0, __float_as_int((float)r.bd));
+  out[2 * qi + 1] = make_int4(qi, r.si, 0, __float_as_int((float)r.sd));
+}
+
+/* out: 2*nq records {queryIdx, trainIdx, imgIdx, distance(float bits)};
+ * partial: scratch of nq*nsplit top-2 records (may be null when nsplit==1). */
+cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit, cudaStream_t s)
+{
+  if (nq <= 0) return cudaSuccess;
+  if (nsplit < 1) nsplit = 1;
+  const int split_len = nt > 0 ? (nt + nsplit - 1) / nsplit : 0;
+  const dim3 grid((nq + AKZ_MQ - 1) / AKZ_MQ, nsplit);
+  k_match<<<grid, AKZ_MQ, 0, s>>>((const uint4 *)dq, (const uint4 *)dt, nq, nt, split_len, nsplit, (akz_top2 *)partial,
+                                  (int4 *)dout);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || nsplit == 1) return e;
+  k_match_merge<<<(nq + 255) / 256, 256, 0, s>>>((const akz_top2 *)partial, nq, nsplit, (int4 *)dout);
+  return cudaGetLastError();
+}
+
+/* Number of train splits so that the grid covers the GPU. */
+int akz_match_splits(int nq, int nt, int nsm)
+{
+  const int qb = (nq + AKZ_MQ - 1) / AKZ_MQ;
+  int ns = (2 * nsm + qb - 1) / qb;
+  const int maxs = (nt + 1023) / 1024;
+  if (ns > maxs) ns = maxs;
+  if (ns < 1) ns = 1;
+  return ns;
+}
+
+size_t akz_match_partial_bytes(int nq, int nsplit) { return (size_t)nq * nsplit * sizeof(akz_top2); }

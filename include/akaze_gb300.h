@@ -1,0 +1,190 @@
+/*
+ * akaze_gb300.h - C ABI of the GB300 A-KAZE library (libakaze_gb300.so).
+ *
+ * Drop-in boundary for the libAKAZECU API of francoto/akaze
+ * (src/lib/AKAZE.h, src/lib/AKAZEConfig.h): plain pointers and sizes, every
+ * call returns an akz_status and never exits the process (the reference's
+ * safeCall exits, src/lib/cudautils.h:15-20).  A header-only C++ wrapper with
+ * the reference's class signatures lives in include/libAKAZECU/AKAZE.h.
+ *
+ * Threading: contexts, batches and matchers are independent; each owns its
+ * device memory and its stream.  One object must not be used from two host
+ * threads at once.
+ */
+#ifndef AKAZE_GB300_H
+#define AKAZE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define AKZ_API __attribute__((visibility("default")))
+#else
+#define AKZ_API
+#endif
+
+typedef enum akz_status {
+  AKZ_OK = 0,
+  AKZ_ERR_INVALID_ARG = 1,
+  AKZ_ERR_OOM = 2,
+  AKZ_ERR_CUDA = 3,
+  AKZ_ERR_OVERFLOW = 4,   /* more raw extrema than maxkeypoints: reported, never silently capped */
+  AKZ_ERR_TIMEOUT = 5,    /* a bounded device loop gave up */
+  AKZ_ERR_UNSUPPORTED = 6,
+  AKZ_ERR_STATE = 7       /* call order (e.g. descriptors before detection) */
+} akz_status;
+
+/* DIFFUSIVITY_TYPE, AKAZEConfig.h:52-57 */
+enum { AKZ_PM_G1 = 0, AKZ_PM_G2 = 1, AKZ_WEICKERT = 2, AKZ_CHARBONNIER = 3 };
+/* DESCRIPTOR_TYPE, AKAZEConfig.h:41-48 (MLDB and MLDB_UPRIGHT are implemented) */
+enum { AKZ_SURF_UPRIGHT = 0, AKZ_SURF = 1, AKZ_MSURF_UPRIGHT = 2, AKZ_MSURF = 3, AKZ_MLDB_UPRIGHT = 4, AKZ_MLDB = 5 };
+/* input pixel types */
+enum { AKZ_U8 = 0, AKZ_F32 = 1 };
+/* planes of a scale-space level (for inspection) */
+enum { AKZ_PLANE_LT = 0, AKZ_PLANE_LSMOOTH = 1, AKZ_PLANE_LX = 3, AKZ_PLANE_LY = 4 };
+
+/* AKAZEOptions, AKAZEConfig.h:84-172, field for field (bool fields as int). */
+typedef struct akz_options {
+  int omin;
+  int omax;
+  int nsublevels;
+  int img_width;
+  int img_height;
+  float soffset;
+  float derivative_factor;
+  float sderivatives;
+  int diffusivity;
+  float dthreshold;
+  float min_dthreshold;
+  int descriptor;
+  int descriptor_size;
+  int descriptor_channels;
+  int descriptor_pattern_size;
+  float kcontrast;
+  float kcontrast_percentile;
+  size_t kcontrast_nbins;
+  int save_scale_space;
+  int save_keypoints;
+  int verbosity;
+  int ncudaimages;
+  int maxkeypoints; /* capacity of raw extrema per image */
+} akz_options;
+
+/* cv::KeyPoint layout (28 bytes): pt.x, pt.y, size, angle, response, octave, class_id. */
+typedef struct akz_keypoint {
+  float x, y, size, angle, response;
+  int32_t octave, class_id;
+} akz_keypoint;
+
+/* cv::DMatch layout (16 bytes). */
+typedef struct akz_dmatch {
+  int32_t queryIdx, trainIdx, imgIdx;
+  float distance;
+} akz_dmatch;
+
+/* AKAZETiming, AKAZEConfig.h:61-80 (milliseconds, device time of each stage). */
+typedef struct akz_timing {
+  double kcontrast, scale, derivatives, detector, extrema, subpixel, descriptor;
+} akz_timing;
+
+/* A raw scale-space extremum as the reference's FindExtrema stores it
+ * (cuda_akaze.cu:758-769), before suppression; for inspection. */
+typedef struct akz_extremum {
+  int32_t x, y, level, octave;
+  float response, size, octsub, dst1;
+} akz_extremum;
+
+typedef struct akz_context akz_context;
+typedef struct akz_batch akz_batch;
+typedef struct akz_matcher akz_matcher;
+
+AKZ_API const char *akz_version(void);
+/* Message of the last failing call on this host thread. */
+AKZ_API const char *akz_last_error(void);
+
+/* setDefaultAKAZEOptions / AKAZEOptions::AKAZEOptions (AKAZEConfig.h:86-111). */
+AKZ_API akz_status akz_options_default(akz_options *opt);
+
+/* ---- single image: libAKAZECU::AKAZE (AKAZE.h:58-143) ---------------- */
+
+/* AKAZE::AKAZE(options) + Allocate_Memory_Evolution (AKAZE.cpp:126-208):
+ * level geometry for options.img_width x img_height, device memory. */
+AKZ_API akz_status akz_create(const akz_options *opt, akz_context **out);
+/* AKAZE::~AKAZE (AKAZE.cpp:140-143). */
+AKZ_API akz_status akz_destroy(akz_context *ctx);
+/* Run on a caller stream (cudaStream_t); NULL restores the context's own. */
+AKZ_API akz_status akz_set_stream(akz_context *ctx, void *stream);
+/* AKAZE::Create_Nonlinear_Scale_Space (AKAZE.cpp:211-276). img: width x height
+ * pixels of AKZ_U8 (0..255) or AKZ_F32 (0..1), rows stride_bytes apart, in host
+ * memory (on_device = 0) or device memory (on_device = 1). The size must equal
+ * the size the context was created for. */
+AKZ_API akz_status akz_create_nonlinear_scale_space(akz_context *ctx, const void *img, int width, int height,
+                                                    size_t stride_bytes, int dtype, int on_device);
+/* AKAZE::Feature_Detection (AKAZE.cpp:316-378): detector, extrema,
+ * suppression; returns the number of keypoints. */
+AKZ_API akz_status akz_feature_detection(akz_context *ctx, int *nkeypoints);
+/* AKAZE::Compute_Descriptors (AKAZE.cpp:405-449): orientation + M-LDB;
+ * copies min(n, capacity) keypoints and 61-byte descriptor rows to host
+ * memory (either pointer may be NULL) and returns n. */
+AKZ_API akz_status akz_compute_descriptors(akz_context *ctx, akz_keypoint *kpts, uint8_t *desc, int capacity, int *nkeypoints);
+/* AKAZE::Get_Computation_Times (AKAZE.h:140-142). */
+AKZ_API akz_status akz_get_timing(akz_context *ctx, akz_timing *t);
+
+/* Inspection of the scale space and detector of a context. */
+AKZ_API akz_status akz_num_levels(const akz_context *ctx, int *nlevels);
+AKZ_API akz_status akz_level_info(const akz_context *ctx, int level, int *width, int *height, int *octave, int *sublevel,
+                                  float *esigma, int *nsteps);
+AKZ_API akz_status akz_get_level_plane(akz_context *ctx, int level, int plane, float *out);
+AKZ_API akz_status akz_get_kcontrast(akz_context *ctx, float *kcontrast);
+AKZ_API akz_status akz_get_extrema(akz_context *ctx, akz_extremum *out, int capacity, int *n);
+
+/* ---- many images per launch (persistent, graph-replayed stages) -------- */
+
+/* A batch of nimages images of the given sizes (each >= 8x8), processed by
+ * one launch per stage. */
+AKZ_API akz_status akz_batch_create(const akz_options *opt, int nimages, const int *widths, const int *heights, akz_batch **out);
+AKZ_API akz_status akz_batch_destroy(akz_batch *b);
+AKZ_API akz_status akz_batch_set_stream(akz_batch *b, void *stream);
+/* Copy u8 images (host pointers, rows strides[i] bytes apart; on_device = 1
+ * for device pointers) into the batch's device staging. Asynchronous. */
+AKZ_API akz_status akz_batch_upload(akz_batch *b, const uint8_t *const *images, const size_t *strides, int on_device);
+/* Device address of image i's staging area (u8, pitch in bytes), for
+ * producers that write the input on the device themselves. */
+AKZ_API akz_status akz_batch_input(akz_batch *b, int i, uint8_t **dptr, size_t *pitch);
+/* Detect + describe every staged image. Asynchronous on the batch stream. */
+AKZ_API akz_status akz_batch_run(akz_batch *b);
+/* Per-image keypoint counts (synchronises the stream). */
+AKZ_API akz_status akz_batch_counts(akz_batch *b, int *counts);
+/* Copy image i's keypoints and 61-byte descriptors to host memory (sync). */
+AKZ_API akz_status akz_batch_results(akz_batch *b, int i, akz_keypoint *kpts, uint8_t *desc, int capacity, int *n);
+/* Device addresses of image i's keypoints and 64-byte descriptor rows. */
+AKZ_API akz_status akz_batch_device_results(akz_batch *b, int i, akz_keypoint **kpts, uint8_t **desc64);
+/* Whole job: upload (host u8), run, counts, copy results out. */
+AKZ_API akz_status akz_batch_detect_describe(akz_batch *b, const uint8_t *const *images, const size_t *strides,
+                                             akz_keypoint *const *kpts, uint8_t *const *desc, const int *capacities,
+                                             int *counts);
+/* Scale-space level plane of image i (inspection). */
+AKZ_API akz_status akz_batch_level_plane(akz_batch *b, int i, int level, int plane, float *out);
+
+/* ---- matcher: libAKAZECU::Matcher (AKAZE.h:29-55) ---------------------- */
+
+AKZ_API akz_status akz_matcher_create(akz_matcher **out);
+AKZ_API akz_status akz_matcher_destroy(akz_matcher *m);
+AKZ_API akz_status akz_matcher_set_stream(akz_matcher *m, void *stream);
+/* Matcher::bfmatch (AKAZE.cpp:36-79): nq x row_bytes query rows against
+ * nt x row_bytes train rows (host memory, row_bytes <= 64, zero-padded to
+ * 64 bytes on the device); out receives 2*nq matches, best then second. */
+AKZ_API akz_status akz_matcher_bfmatch(akz_matcher *m, const uint8_t *query, int nq, const uint8_t *train, int nt,
+                                       int row_bytes, akz_dmatch *out);
+/* Same on device buffers of 64-byte rows; out is device memory of 2*nq. */
+AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *query64, int nq, const uint8_t *train64,
+                                              int nt, akz_dmatch *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
