@@ -272,6 +272,7 @@ __global__ void __launch_bounds__(256) k_fed(akz_fed_params p)
   const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
   const int tx1 = min(tx0 + TW, W), ty1 = min(ty0 + TH, H);
   const int d = p.steps;
+  const int srck = p.first ? sg.aux : p.src; /* first chunk: per-image source kind */
   const int rx0 = max(tx0 - d, 0), rx1 = min(tx1 + d, W), ry0 = max(ty0 - d, 0), ry1 = min(ty1 + d, H);
   const int rw = rx1 - rx0;
   float *planes = p.t.planes;
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(256) k_fed(akz_fed_params p)
     gbuf = sS + SWm * SHm;
     const int pw = px1 - px0, sw = sx1 - sx0;
     /* predecessor: same-size copy, exact 2x half-sample, or a prepared plane */
-    if (p.src == 1) {
+    if (srck == 1) {
       const akz_level_desc Lp = p.t.lv[sg.level_desc - 1];
       const float *pp = planes + Lp.lt;
       for (int i = tid; i < (py1 - py0) * pw; i += 256) {
@@ -300,7 +301,7 @@ __global__ void __launch_bounds__(256) k_fed(akz_fed_params p)
     } else {
       const float *pp;
       long long pitch;
-      if (p.src == 0) {
+      if (srck == 0) {
         const akz_level_desc Lp = p.t.lv[sg.level_desc - 1];
         pp = planes + Lp.lt;
         pitch = Lp.pitch;
