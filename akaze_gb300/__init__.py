@@ -257,6 +257,39 @@ class Batch:
         check(self._lib.akz_batch_device_results(self._h, i, ctypes.byref(kp), ctypes.byref(d)))
         return kp.value, d.value
 
+    def kernel_count(self):
+        n = ctypes.c_int()
+        check(self._lib.akz_batch_kernel_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def profile(self):
+        """Per-stage device ms of one run (contrast, level 0, levels, detector,
+        scan+extract, suppression, orientation+M-LDB)."""
+        ms = np.zeros(7, np.float32)
+        check(self._lib.akz_batch_profile(self._h, _ptr(ms), 7))
+        return ms
+
+    def detect_describe(self, images, capacity=None):
+        """Whole job through the C ABI: host u8 in, host keypoints/descriptors out."""
+        imgs = [np.ascontiguousarray(im, np.uint8) for im in images]
+        cap = capacity or self.options.maxkeypoints
+        if not hasattr(self, "_out") or self._out[0] != cap:
+            kps = [np.zeros(cap, KEYPOINT_DTYPE) for _ in range(self.n)]
+            ds = [np.zeros((cap, 61), np.uint8) for _ in range(self.n)]
+            self._out = (cap, kps, ds)
+        _, kps, ds = self._out
+        return self.detect_describe_into(imgs, kps, ds)
+
+    def detect_describe_into(self, imgs, kps, ds):
+        ptrs = (ctypes.c_void_p * self.n)(*[im.ctypes.data for im in imgs])
+        strides = (ctypes.c_size_t * self.n)(*[im.strides[0] for im in imgs])
+        kp_p = (ctypes.c_void_p * self.n)(*[k.ctypes.data for k in kps])
+        d_p = (ctypes.c_void_p * self.n)(*[d.ctypes.data for d in ds])
+        caps = np.array([len(k) for k in kps], np.int32)
+        counts = np.zeros(self.n, np.int32)
+        check(self._lib.akz_batch_detect_describe(self._h, ptrs, strides, kp_p, d_p, _ptr(caps), _ptr(counts)))
+        return counts
+
     def plane(self, i, level, name="Lt", shape=None):
         out = np.empty(shape, np.float32)
         check(self._lib.akz_batch_level_plane(self._h, i, level, _PLANES[name], _ptr(out)))

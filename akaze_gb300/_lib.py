@@ -24,7 +24,7 @@ EXPORTS = [
     "akz_num_levels", "akz_level_info", "akz_get_level_plane", "akz_get_kcontrast", "akz_get_extrema",
     "akz_batch_create", "akz_batch_destroy", "akz_batch_set_stream", "akz_batch_upload", "akz_batch_input",
     "akz_batch_run", "akz_batch_counts", "akz_batch_results", "akz_batch_device_results",
-    "akz_batch_detect_describe", "akz_batch_level_plane",
+    "akz_batch_detect_describe", "akz_batch_level_plane", "akz_batch_kernel_count", "akz_batch_profile",
     "akz_matcher_create", "akz_matcher_destroy", "akz_matcher_set_stream", "akz_matcher_bfmatch",
     "akz_matcher_bfmatch_device",
 ]
@@ -92,6 +92,8 @@ def load():
         "akz_batch_device_results": ([P, I, ctypes.POINTER(P), ctypes.POINTER(P)], I),
         "akz_batch_detect_describe": ([P, P, P, P, P, P, P], I),
         "akz_batch_level_plane": ([P, I, I, I, P], I),
+        "akz_batch_kernel_count": ([P, IP], I),
+        "akz_batch_profile": ([P, P, I], I),
         "akz_matcher_create": ([ctypes.POINTER(P)], I), "akz_matcher_destroy": ([P], I),
         "akz_matcher_set_stream": ([P, P], I),
         "akz_matcher_bfmatch": ([P, P, I, P, I, I, P], I),

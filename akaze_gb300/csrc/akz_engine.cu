@@ -55,6 +55,13 @@ static akz_status akz_fail_cuda(cudaError_t e, const char *expr, const char *fil
     if (e_ != cudaSuccess) return akz_fail_cuda(e_, #x, __FILE__, __LINE__); \
   } while (0)
 
+static float akz_ms(cudaEvent_t a, cudaEvent_t b)
+{
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
 /* ------------------------------------------------------------------------ */
 /* plan                                                                     */
 
@@ -591,7 +598,7 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
 
 /* stage groups ------------------------------------------------------------ */
 
-static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s)
+static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe = nullptr)
 {
   const akz_tables t = akz_make_tables(b);
   CK(cudaMemsetAsync(b->d_stats, 0, (size_t)b->nimg * sizeof(akz_image_stats), s));
@@ -607,6 +614,7 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s)
   CK(akz_launch_contrast(cp, b->contrast_tiles, 0, s));
   CK(akz_launch_contrast(cp, b->contrast_tiles, 1, s));
   CK(akz_launch_contrast_final(t, b->d_hist, cp.nbins, b->opt.kcontrast_percentile, b->d_kc, s));
+  if (pe) CK(cudaEventRecord(pe[1], s));
   akz_gauss_params gp;
   gp.t = t;
   gp.segs = b->d_segs + b->gauss_off;
@@ -615,6 +623,7 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s)
   gp.R = b->R0;
   for (int k = 0; k <= 2 * b->R0; k++) gp.taps[k] = b->taps0[k];
   CK(akz_launch_gauss0(gp, b->gauss_tiles, s));
+  if (pe) CK(cudaEventRecord(pe[2], s));
   for (int l = 1; l < b->maxlev; l++) {
     if (b->area[l].nsegs > 0) {
       akz_area_params ap;
@@ -638,7 +647,7 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s)
   return AKZ_OK;
 }
 
-static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s)
+static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s, cudaEvent_t *pe = nullptr)
 {
   const akz_tables t = akz_make_tables(b);
   const float w = (float)(10.0 / 3.0);
@@ -656,6 +665,7 @@ static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s)
   dp.fac1 = fac1;
   dp.fac2 = fac2;
   CK(akz_launch_detect(dp, b->detect_tiles, b->max_step, s));
+  if (pe) CK(cudaEventRecord(pe[4], s));
   CK(akz_launch_rowscan(t, b->d_rowcnt, b->d_rowscan, s));
   akz_extract_params ep;
   ep.t = t;
@@ -667,6 +677,7 @@ static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s)
   ep.fac1 = fac1;
   ep.fac2 = fac2;
   CK(akz_launch_extract(ep, b->extract_rows, s));
+  if (pe) CK(cudaEventRecord(pe[5], s));
   akz_nms_params np;
   np.t = t;
   np.rowscan = b->d_rowscan;
@@ -833,13 +844,6 @@ AKZ_API akz_status akz_set_stream(akz_context *c, void *stream)
   AKZ_GUARD(c);
   c->b->stream = stream ? (cudaStream_t)stream : c->b->own_stream;
   return AKZ_OK;
-}
-
-static float akz_ms(cudaEvent_t a, cudaEvent_t b)
-{
-  float ms = 0.0f;
-  cudaEventElapsedTime(&ms, a, b);
-  return ms;
 }
 
 AKZ_API akz_status akz_create_nonlinear_scale_space(akz_context *c, const void *img, int width, int height, size_t stride,
@@ -1098,6 +1102,44 @@ AKZ_API akz_status akz_batch_level_plane(akz_batch *b, int i, int level, int pla
 {
   AKZ_GUARD(b);
   return akz_plane_out(b, i, level, plane, out);
+}
+
+/* Number of kernels one akz_batch_run launches. */
+static int akz_batch_nkernels(const akz_batch *b)
+{
+  int n = 3 + 1 + 1 + 1 + 1 + 1 + 1; /* contrast x3, level 0, detect, scan, extract, nms, describe */
+  for (int l = 1; l < b->maxlev; l++) n += (int)b->fed[l].size() + (b->area[l].nsegs > 0 ? 1 : 0);
+  return n;
+}
+
+AKZ_API akz_status akz_batch_kernel_count(const akz_batch *b, int *n)
+{
+  AKZ_GUARD(b);
+  if (n) *n = akz_batch_nkernels(b);
+  return AKZ_OK;
+}
+
+/* One run without the graph, with events between stage groups; stage_ms
+ * receives up to 7 entries: contrast, level 0, levels 1.., detector,
+ * scan+extract, suppression, orientation+M-LDB. */
+AKZ_API akz_status akz_batch_profile(akz_batch *b, float *stage_ms, int n)
+{
+  AKZ_GUARD(b);
+  cudaStream_t s = b->stream;
+  cudaEvent_t *pe = b->ev;
+  CK(cudaEventRecord(pe[0], s));
+  akz_status st = akz_stage_scale(b, s, pe);
+  if (st != AKZ_OK) return st;
+  CK(cudaEventRecord(pe[3], s));
+  st = akz_stage_detect(b, s, pe);
+  if (st != AKZ_OK) return st;
+  CK(cudaEventRecord(pe[6], s));
+  st = akz_stage_describe(b, s);
+  if (st != AKZ_OK) return st;
+  CK(cudaEventRecord(pe[7], s));
+  CK(cudaEventSynchronize(pe[7]));
+  for (int k = 0; k < 7 && k < n; k++) stage_ms[k] = akz_ms(pe[k], pe[k + 1]);
+  return AKZ_OK;
 }
 
 /* ---- matcher ------------------------------------------------------------ */

@@ -1,0 +1,326 @@
+#!/usr/bin/env python3
+"""Throughput of A-KAZE detect + M-LDB on 1920x1080 u8 images, on GB300.
+
+Workload (one step): a batch of --batch seeded synthetic 1920x1080 images
+(40 Gaussian blobs, 3 gratings, +-8 noise), default options (4 octaves x 4
+sublevels, PM-g2, contrast percentile 0.7, threshold 0.001, full 486-bit
+M-LDB), every stage of the path on the GPU: contrast factor, 16 levels with
+their 166 FED steps, Hessian detector, extrema, suppression, orientation,
+descriptors.  One graph replay per step.
+
+  value   images/s with the input already in HBM (all ranks; replicas only)
+  e2e     images/s through akz_batch_detect_describe: pinned host u8 in,
+          host keypoints + 61-byte descriptors out, copies inside the timing
+  roofline  HBM roofline of the level (FED) stage, the dominant stage
+  cpu_baseline  the CPU oracle on this host's cores (OpenMP), bounded sample
+
+--impl reference times the reference's CPU path as restated by the oracle
+(the reference itself needs OpenCV/Boost and an sm_30 toolchain; only its
+fed.cpp compiles here) on the host cores, with the same metric and config.
+Multi-GPU: replicas only, one process per GPU under torchrun, each rank its
+own images, no collective on the data path; the max time over ranks counts.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "1080p images/s detect+MLDB, surrogate vs plain FED at fixed repeatability"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+def level_sizes(w, h, omax=4, nsub=4):
+    out = []
+    for i in range(omax):
+        lw, lh = int(w / 2 ** i), int(h / 2 ** i)
+        if (lw < 80 or lh < 40) and i:
+            break
+        out += [(lw, lh)] * nsub
+    return out
+
+
+def fed_algorithmic_bytes(w, h):
+    """Compulsory HBM bytes of the level stage per image: read the
+    predecessor level (4 B/px of its size) and write the evolved level
+    (4 B/px), for every level >= 1."""
+    L = level_sizes(w, h)
+    return sum(4 * L[i - 1][0] * L[i - 1][1] + 4 * L[i][0] * L[i][1] for i in range(1, len(L)))
+
+
+def image_algorithmic_bytes(w, h, nkp):
+    """Whole-pipeline compulsory bytes per image: u8 read twice (contrast and
+    level 0) + per level: write Lt, read the predecessor, re-read the
+    pre-diffusion smoothing for the detector, write Lx and Ly; + 5384 B per
+    keypoint (441 samples x 3 planes x 4 B, a 64 B row and a 28 B record)."""
+    L = level_sizes(w, h)
+    b = 2 * w * h
+    for i, (lw, lh) in enumerate(L):
+        p = lw * lh
+        b += 4 * p + (4 * L[i - 1][0] * L[i - 1][1] if i else 0) + 4 * p + 8 * p
+    return b + 5384 * nkp
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_oracle_rate(w, h, seconds, seed=900):
+    """Images/s of the CPU oracle (all host cores) on a bounded sample."""
+    from akaze_gb300 import synth
+    from oracle import oracle_ctypes as oc
+    oc.build()
+    cores = os.cpu_count() or 1
+    oc.set_threads(cores)
+    img = synth.synth_image(seed, w, h)
+    o = oc.Oracle(w, h)
+    o.run(img)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.run(img)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 50:
+            break
+    return n / el, cores, f"{n} runs of one {w}x{h} synthetic image, {cores} OpenMP threads, {el:.1f} s"
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup(args)
+    if rank != 0:
+        return 0
+    from akaze_gb300 import synth  # noqa: F401
+    from oracle import oracle_ctypes as oc
+    oc.build()
+    cores = os.cpu_count() or 1
+    oc.set_threads(cores)
+    w, h = args.width, args.height
+    o = oc.Oracle(w, h)
+    from akaze_gb300 import synth as sy
+    imgs = [sy.synth_image(1000 + i, w, h) for i in range(min(4, args.steps + args.warmup))]
+    for k in range(args.warmup):
+        o.run(imgs[k % len(imgs)])
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        o.run(imgs[k % len(imgs)])
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "images/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"plain A-KAZE detect+MLDB, {w}x{h} u8, 4 octaves x 4 sublevels, one image per step",
+                   "images_per_step": 1},
+        "cpu_baseline": {"value": v, "unit": "images/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} images of {w}x{h}, one per step, {cores} OpenMP threads"},
+        "e2e": {"value": v, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("the reference's own sources need OpenCV, Boost.Python and sm_30 (no build here); this arm times "
+                 "the CPU restatement of its path (oracle/), whose FED schedule is pinned to its fed.cpp"),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    ws, rank, local = dist_setup(args)
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import akaze_gb300 as akz
+    from akaze_gb300 import synth
+
+    B, W, H = args.batch, args.width, args.height
+    imgs = [synth.synth_image(10000 * rank + i, W, H) for i in range(B)]
+    opt = akz.AKAZEOptions()
+    batch = akz.Batch(opt, [(W, H)] * B)
+    stream = torch.cuda.Stream()
+    batch.set_stream(stream.cuda_stream)
+    batch.upload(imgs)
+    torch.cuda.synchronize()
+
+    # device-resident throughput
+    for _ in range(max(args.warmup, 3)):
+        batch.run()
+    counts = batch.counts()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms_max = float(t.item())
+    value = B * ws * args.steps / (ms_max / 1000.0)
+
+    # stage profile (one non-graph run) for the roofline of the level stage
+    stage = [float(x) for x in batch.profile()]
+    fed_ms = stage[2]
+    fed_bytes = fed_algorithmic_bytes(W, H) * B
+    pk, pk_kind = peaks()
+    achieved = fed_bytes / (fed_ms / 1000.0) / 1e9
+    n_launch = batch.kernel_count()
+
+    # end to end through the C ABI: pinned host u8 in, host results out
+    pin_in = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(B)]
+    for p, im in zip(pin_in, imgs):
+        p.numpy()[:] = im
+    cap = int(max(counts)) + 64
+    kps = [torch.empty(cap * 28, dtype=torch.uint8).pin_memory().numpy().view(akz.KEYPOINT_DTYPE) for _ in range(B)]
+    ds = [torch.empty(cap * 61, dtype=torch.uint8).pin_memory().numpy().reshape(cap, 61) for _ in range(B)]
+    np_in = [p.numpy() for p in pin_in]
+    for _ in range(2):
+        c2 = batch.detect_describe_into(np_in, kps, ds)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e_steps = max(1, min(args.steps, 10))
+    for _ in range(e_steps):
+        c2 = batch.detect_describe_into(np_in, kps, ds)
+    el = time.perf_counter() - t0
+    te = torch.tensor([el], device="cuda")
+    if dist:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e = B * ws * e_steps / float(te.item())
+    h2d = B * W * H
+    d2h = int(sum(c2)) * (28 + 61) + B * 32
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    cpu_v, cores, sample = cpu_oracle_rate(W, H, args.cpu_seconds)
+    nkp = float(np.mean(counts))
+    line = {
+        "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"plain A-KAZE detect+MLDB, {W}x{H} u8, 4 octaves x 4 sublevels, default options",
+                   "fed": "plain (the learned surrogate path is not built)",
+                   "images_per_step_per_gpu": B, "parallelism": f"replicas x{ws}",
+                   "l2": "inputs and working set larger than L2 (~%.1f GB per step)" % (B * image_algorithmic_bytes(W, H, 0) / 1e9),
+                   "keypoints_per_image": nkp},
+        "roofline": {"bound": "hbm", "kernel": "k_fed (level stage: 15 levels, 166 FED steps)",
+                     "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                     "algorithmic_bytes_per_image": fed_algorithmic_bytes(W, H), "launch_ms": fed_ms,
+                     "peak_kind": f"{pk_kind} hbm_gbs"},
+        "pipeline_roofline": {"achieved": image_algorithmic_bytes(W, H, nkp) * value / 1e9,
+                              "frac": image_algorithmic_bytes(W, H, nkp) * value / 1e9 / pk["hbm_gbs"],
+                              "bytes_per_image": image_algorithmic_bytes(W, H, nkp)},
+        "stage_ms": dict(zip(["contrast", "level0", "levels", "detector", "scan_extract", "suppression", "describe"], stage)),
+        "cpu_baseline": {"value": cpu_v, "unit": "images/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": e2e, "unit": "images/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": n_launch * args.steps,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -169,6 +169,14 @@ AKZ_API akz_status akz_batch_detect_describe(akz_batch *b, const uint8_t *const 
                                              int *counts);
 /* Scale-space level plane of image i (inspection). */
 AKZ_API akz_status akz_batch_level_plane(akz_batch *b, int i, int level, int plane, float *out);
+/* Number of kernels one akz_batch_run launches (no counterpart in the
+ * reference; for launch accounting). */
+AKZ_API akz_status akz_batch_kernel_count(const akz_batch *b, int *n);
+/* One run without graph replay, timed per stage group with CUDA events on the
+ * batch stream (no counterpart in the reference; the AKAZETiming of a batch):
+ * stage_ms[0..6] = contrast, level 0, levels >= 1, detector, scan+extract,
+ * suppression, orientation+M-LDB. Synchronises. */
+AKZ_API akz_status akz_batch_profile(akz_batch *b, float *stage_ms, int n);
 
 /* ---- matcher: libAKAZECU::Matcher (AKAZE.h:29-55) ---------------------- */
 
