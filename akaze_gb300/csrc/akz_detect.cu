@@ -50,35 +50,62 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   const int DM = (TW + 2 * max_step + 2) * (TH + 2 * max_step + 2);
   float *sS = sm, *sX = sm + SM, *sY = sX + DM, *sD = sY + DM;
 
+  const int lane = tid & 31, warp = tid >> 5;
   const float *ls = p.t.planes + L.ls;
-  for (int i = tid; i < (sy1 - sy0) * sw; i += 256) {
-    const int y = sy0 + i / sw, x = sx0 + i % sw;
-    sS[i] = __ldg(ls + (long long)y * L.pitch + x);
-  }
+  for (int y = sy0 + warp; y < sy1; y += 8)
+    for (int x = sx0 + lane; x < sx1; x += 32) sS[(y - sy0) * sw + (x - sx0)] = __ldg(ls + (long long)y * L.pitch + x);
   __syncthreads();
-  const akz_smem_acc S{sS, sx0, sy0, sw};
   float *lxp = p.t.planes + L.lx, *lyp = p.t.planes + L.ly;
-  for (int i = tid; i < (dy1 - dy0) * dw; i += 256) {
-    const int y = dy0 + i / dw, x = dx0 + i % dw;
-    float a, b;
-    akz_deriv_at(S, W, H, st, x, y, p.fac1, p.fac2, &a, &b);
-    sX[i] = a;
-    sY[i] = b;
-    if (x >= tx0 && x < tx1 && y >= ty0 && y < ty1) {
-      lxp[(long long)y * L.pitch + x] = a;
-      lyp[(long long)y * L.pitch + x] = b;
+  const float fac1 = p.fac1, fac2 = p.fac2;
+  /* Lx, Ly on the tile +- (step+1): scaled Scharr with step sigma_size and
+   * reflect-101 offsets (cuda_akaze.cu:651-671) */
+  for (int y = dy0 + warp; y < dy1; y += 8) {
+    const int yl = y < st ? st - y : y - st;
+    const int yh = y >= H - st ? 2 * H - y - st - 2 : y + st;
+    const float *su = sS + (yl - sy0) * sw - sx0, *sc = sS + (y - sy0) * sw - sx0, *sd = sS + (yh - sy0) * sw - sx0;
+    float *ox = sX + (y - dy0) * dw - dx0, *oy = sY + (y - dy0) * dw - dx0;
+    const bool yt = y >= ty0 && y < ty1;
+    for (int x = dx0 + lane; x < dx1; x += 32) {
+      const int xl = x < st ? st - x : x - st;
+      const int xh = x >= W - st ? 2 * W - x - st - 2 : x + st;
+      const float ul = su[xl], ur = su[xh], ll = sd[xl], lr = sd[xh];
+      const float cl = sc[xl], cr = sc[xh], uc = su[x], lc = sd[x];
+      const float a = fac1 * (ur + lr - ul - ll) + fac2 * (cr - cl);
+      const float b = fac1 * (lr + ll - ur - ul) + fac2 * (lc - uc);
+      ox[x] = a;
+      oy[x] = b;
+      if (yt && x >= tx0 && x < tx1) {
+        lxp[(long long)y * L.pitch + x] = a;
+        lyp[(long long)y * L.pitch + x] = b;
+      }
     }
   }
   __syncthreads();
-  const akz_smem_acc X{sX, dx0, dy0, dw}, Y{sY, dx0, dy0, dw};
-  for (int i = tid; i < (ey1 - ey0) * ew; i += 256) {
-    const int y = ey0 + i / ew, x = ex0 + i % ew;
-    sD[i] = akz_det_at(X, Y, W, H, st, x, y, p.fac1, p.fac2);
+  /* Hessian determinant on the tile +- 1 (cuda_akaze.cu:673-701) */
+  for (int y = ey0 + warp; y < ey1; y += 8) {
+    const int yl = y < st ? st - y : y - st;
+    const int yh = y >= H - st ? 2 * H - y - st - 2 : y + st;
+    const float *xu = sX + (yl - dy0) * dw - dx0, *xc = sX + (y - dy0) * dw - dx0, *xd = sX + (yh - dy0) * dw - dx0;
+    const float *yu = sY + (yl - dy0) * dw - dx0, *yd = sY + (yh - dy0) * dw - dx0;
+    float *o = sD + (y - ey0) * ew - ex0;
+    for (int x = ex0 + lane; x < ex1; x += 32) {
+      const int xl = x < st ? st - x : x - st;
+      const int xh = x >= W - st ? 2 * W - x - st - 2 : x + st;
+      float ul = xu[xl], ur = xu[xh], ll = xd[xl], lr = xd[xh];
+      const float lxx = fac1 * (ur + lr - ul - ll) + fac2 * (xc[xh] - xc[xl]);
+      const float lyx = fac1 * (lr + ll - ur - ul) + fac2 * (xd[x] - xu[x]);
+      ul = yu[xl];
+      ur = yu[xh];
+      ll = yd[xl];
+      lr = yd[xh];
+      const float lyy = fac1 * (lr + ll - ur - ul) + fac2 * (yd[x] - yu[x]);
+      o[x] = lxx * lyy - lyx * lyx;
+    }
   }
   __syncthreads();
   const float border = L.border;
-  for (int i = tid; i < (ty1 - ty0) * (tx1 - tx0); i += 256) {
-    const int y = ty0 + i / (tx1 - tx0), x = tx0 + i % (tx1 - tx0);
+  for (int y = ty0 + warp; y < ty1; y += 8)
+    for (int x = tx0 + lane; x < tx1; x += 32) {
     const int left_x = (int)((float)x - border + 0.5f) - 1;
     const int right_x = (int)((float)x + border + 0.5f) + 1;
     const int up_y = (int)((float)y - border + 0.5f) - 1;

@@ -482,8 +482,8 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
       const int steps = (nsteps - done + (nch - c) - 1) / (nch - c);
       akz_fed_launch fl;
       memset(&fl, 0, sizeof(fl));
-      fl.tw = steps <= 4 ? 128 : 64;
-      fl.th = 32;
+      fl.tw = 128 - 2 * steps; /* k_fed region is 128 x 40 = tile +- steps */
+      fl.th = 40 - 2 * steps;
       fl.seg_off = (int)b->segs.size();
       for (int i = 0; i < n; i++) {
         if (b->im[i].nlev <= l) continue;

@@ -126,7 +126,7 @@ cudaError_t akz_launch_extract(const akz_extract_params &p, int nrows, cudaStrea
 cudaError_t akz_launch_nms(const akz_nms_params &p, cudaStream_t s);
 cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaStream_t s);
 
-#define AKZ_DETECT_TW 32
+#define AKZ_DETECT_TW 64
 #define AKZ_DETECT_TH 32
 #define AKZ_GAUSS_TW 64
 #define AKZ_GAUSS_TH 32

@@ -51,14 +51,13 @@ __global__ void __launch_bounds__(256) k_contrast(akz_contrast_params p)
 
   if (PASS == 1)
     for (int b = tid; b < p.nbins; b += 256) sHist[b] = 0;
-  for (int i = tid; i < (py1 - py0) * (px1 - px0); i += 256) {
-    const int y = py0 + i / (px1 - px0), x = px0 + i % (px1 - px0);
-    sP[(y - py0) * PW + (x - px0)] = akz_fetch_input(p.t, I, x, y, p.inv255);
-  }
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int y = py0 + warp; y < py1; y += 8)
+    for (int x = px0 + lane; x < px1; x += 32) sP[(y - py0) * PW + (x - px0)] = akz_fetch_input(p.t, I, x, y, p.inv255);
   __syncthreads();
   const float k0 = p.taps[0], k1 = p.taps[1], k2 = p.taps[2];
-  for (int i = tid; i < (py1 - py0) * (gx1 - gx0); i += 256) {
-    const int y = py0 + i / (gx1 - gx0), x = gx0 + i % (gx1 - gx0);
+  for (int y = py0 + warp; y < py1; y += 8)
+    for (int x = gx0 + lane; x < gx1; x += 32) {
     const float *r = sP + (y - py0) * PW - px0;
     float acc = k0 * (r[max(x - 2, 0)] + r[min(x + 2, W - 1)]);
     acc = acc + k1 * (r[max(x - 1, 0)] + r[min(x + 1, W - 1)]);
@@ -66,8 +65,8 @@ __global__ void __launch_bounds__(256) k_contrast(akz_contrast_params p)
     sT[(y - py0) * GW + (x - gx0)] = acc;
   }
   __syncthreads();
-  for (int i = tid; i < (gy1 - gy0) * (gx1 - gx0); i += 256) {
-    const int y = gy0 + i / (gx1 - gx0), x = gx0 + i % (gx1 - gx0);
+  for (int y = gy0 + warp; y < gy1; y += 8)
+    for (int x = gx0 + lane; x < gx1; x += 32) {
     const float *c = sT + (x - gx0) - py0 * GW;
     float acc = k0 * (c[max(y - 2, 0) * GW] + c[min(y + 2, H - 1) * GW]);
     acc = acc + k1 * (c[max(y - 1, 0) * GW] + c[min(y + 1, H - 1) * GW]);
@@ -80,8 +79,8 @@ __global__ void __launch_bounds__(256) k_contrast(akz_contrast_params p)
   float mx = 0.0f, hmax = 0.0f;
   if (PASS == 1) hmax = sqrtf(__uint_as_float(p.t.stats[img].hmax2_bits));
   const float nb = (float)p.nbins;
-  for (int i = tid; i < max(iy1 - iy0, 0) * max(ix1 - ix0, 0); i += 256) {
-    const int y = iy0 + i / (ix1 - ix0), x = ix0 + i % (ix1 - ix0);
+  for (int y = iy0 + warp; y < iy1; y += 8)
+    for (int x = ix0 + lane; x < ix1; x += 32) {
     const float *rm = sG + (y - 1 - gy0) * GW - gx0, *r0 = sG + (y - gy0) * GW - gx0, *rp = sG + (y + 1 - gy0) * GW - gx0;
     const float rxm = rm[x + 1] - rm[x - 1];
     const float rx0 = r0[x + 1] - r0[x - 1];
@@ -170,13 +169,12 @@ __global__ void __launch_bounds__(256) k_gauss0(akz_gauss_params p)
   const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
   const int tx1 = min(tx0 + TW, W), ty1 = min(ty0 + TH, H);
   const int px0 = max(tx0 - R, 0), px1 = min(tx1 + R, W), py0 = max(ty0 - R, 0), py1 = min(ty1 + R, H);
-  for (int i = tid; i < (py1 - py0) * (px1 - px0); i += 256) {
-    const int y = py0 + i / (px1 - px0), x = px0 + i % (px1 - px0);
-    sP[(y - py0) * PW + (x - px0)] = akz_fetch_input(p.t, I, x, y, p.inv255);
-  }
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int y = py0 + warp; y < py1; y += 8)
+    for (int x = px0 + lane; x < px1; x += 32) sP[(y - py0) * PW + (x - px0)] = akz_fetch_input(p.t, I, x, y, p.inv255);
   __syncthreads();
-  for (int i = tid; i < (py1 - py0) * (tx1 - tx0); i += 256) {
-    const int y = py0 + i / (tx1 - tx0), x = tx0 + i % (tx1 - tx0);
+  for (int y = py0 + warp; y < py1; y += 8)
+    for (int x = tx0 + lane; x < tx1; x += 32) {
     const float *r = sP + (y - py0) * PW - px0;
     float acc;
     if (R > 0) {
@@ -190,8 +188,8 @@ __global__ void __launch_bounds__(256) k_gauss0(akz_gauss_params p)
   }
   __syncthreads();
   float *out = p.t.planes + L.lt;
-  for (int i = tid; i < (ty1 - ty0) * (tx1 - tx0); i += 256) {
-    const int y = ty0 + i / (tx1 - tx0), x = tx0 + i % (tx1 - tx0);
+  for (int y = ty0 + warp; y < ty1; y += 8)
+    for (int x = tx0 + lane; x < tx1; x += 32) {
     const float *c = sT + (x - tx0) - py0 * TW;
     float acc;
     if (R > 0) {
@@ -222,81 +220,87 @@ __device__ __forceinline__ float akz_conductance(float lx, float ly, float inv_k
   return (float)(1.0 / (double)den);
 }
 
-/* One explicit FED step over [ax0,ax1)x[ay0,ay1) with replicate borders
- * (the reference's border formulas of nld_step_scalar equal the generic
- * formula with clamped neighbours: a clamped difference is exactly zero). */
-__device__ __forceinline__ void akz_fed_step(const akz_smem_acc &src, float *dst, int dx0, int dy0, int dstride,
-                                             const float *g, int gx0, int gy0, int gstride, int ax0, int ax1, int ay0,
-                                             int ay1, int W, int H, float h)
+/* FED level kernel.
+ *
+ * Every CTA owns a fixed 128 x 40 region R0 = tile +- d (d = FED steps of the
+ * launch, tile (128-2d) x (40-2d)), so one thread geometry serves every
+ * chunk size: 512 threads, 4 column groups of 32 lanes x 4 bands of 10 rows;
+ * each thread keeps the 10 level values of its column in registers together
+ * with the conductance pair sums (c_x + c_x+1), (c_x-1 + c_x), (c_y + c_y+1)
+ * of the reference's flux terms, which do not change across steps.  A step
+ * reads the east/west neighbours (and the band's outer rows) from a
+ * double-buffered shared plane: 3 shared-memory operations and 13 FP32
+ * operations per pixel-step, one barrier per step.  Pixels outside
+ * tile +- (d - s) after step s are not needed and may hold anything; image
+ * borders are replicate (clamped) neighbours, whose flux is exactly zero, as
+ * in the reference's border formulas (nldiffusion_functions.cpp:241-307).
+ */
+#define AKZ_FED_RW 128
+#define AKZ_FED_RH 40
+#define AKZ_FED_RB 10
+#define AKZ_FED_THREADS 512
+
+size_t akz_fed_smem_bytes(int, int, int, int first)
 {
-  for (int y = ay0 + (int)threadIdx.y; y < ay1; y += 8) {
-    const int ym = max(y - 1, 0), yp = min(y + 1, H - 1);
-    const float *gr = g + (y - gy0) * gstride - gx0;
-    const float *gm = g + (ym - gy0) * gstride - gx0;
-    const float *gp = g + (yp - gy0) * gstride - gx0;
-    for (int x = ax0 + (int)threadIdx.x; x < ax1; x += 32) {
-      const int xm = max(x - 1, 0), xp = min(x + 1, W - 1);
-      const float Lc = src(x, y), Le = src(xp, y), Lw = src(xm, y), Ls = src(x, yp), Ln = src(x, ym);
-      const float gc = gr[x];
-      const float xpos = (gc + gr[xp]) * (Le - Lc);
-      const float xneg = (gr[xm] + gc) * (Lc - Lw);
-      const float ypos = (gc + gp[x]) * (Ls - Lc);
-      const float yneg = (gm[x] + gc) * (Lc - Ln);
-      const float step = h * (xpos - xneg + ypos - yneg);
-      dst[(y - dy0) * dstride + (x - dx0)] = Lc + step;
-    }
-  }
+  if (!first) return 2 * AKZ_FED_RW * AKZ_FED_RH * sizeof(float);
+  const size_t P = (size_t)(AKZ_FED_RH + 6) * (AKZ_FED_RW + 6);
+  const size_t T = (size_t)(AKZ_FED_RH + 6) * (AKZ_FED_RW + 2);
+  const size_t S = (size_t)(AKZ_FED_RH + 2) * (AKZ_FED_RW + 2);
+  return (P + T + S) * sizeof(float);
 }
 
-size_t akz_fed_smem_bytes(int tw, int th, int d, int first)
-{
-  const size_t r0 = (size_t)(tw + 2 * d) * (th + 2 * d);
-  if (!first) return 3 * r0 * sizeof(float);
-  const size_t P = (size_t)(tw + 2 * d + 6) * (th + 2 * d + 6);
-  const size_t T = (size_t)(th + 2 * d + 6) * (tw + 2 * d + 2);
-  const size_t S = (size_t)(tw + 2 * d + 2) * (th + 2 * d + 2);
-  return (P + T + S + r0) * sizeof(float);
-}
-
-template <int TW, int TH>
-__global__ void __launch_bounds__(256) k_fed(akz_fed_params p)
+__global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
 {
   extern __shared__ float sm[];
-  const int tid = threadIdx.y * 32 + threadIdx.x;
+  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
+  constexpr int PS = RW + 6, SS = RW + 2; /* strides of the input and smoothing regions */
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
   const akz_tile_seg sg = p.segs[si];
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const akz_image_desc I = p.t.im[L.image];
   const int W = L.width, H = L.height;
+  const int d = p.steps;
+  const int TW = RW - 2 * d, TH = RH - 2 * d;
   const int lt = blockIdx.x - sg.tile_begin;
   const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
   const int tx1 = min(tx0 + TW, W), ty1 = min(ty0 + TH, H);
-  const int d = p.steps;
-  const int srck = p.first ? sg.aux : p.src; /* first chunk: per-image source kind */
-  const int rx0 = max(tx0 - d, 0), rx1 = min(tx1 + d, W), ry0 = max(ty0 - d, 0), ry1 = min(ty1 + d, H);
-  const int rw = rx1 - rx0;
+  const int ox = tx0 - d, oy = ty0 - d; /* R0 origin (may lie outside the image) */
+  const int srck = p.first ? sg.aux : p.src;
   float *planes = p.t.planes;
 
-  float *gbuf, *bufA, *bufB;
-  akz_smem_acc src;
+  /* this thread: column lx of R0, rows ly0 .. ly0+RB-1 */
+  const int lx = (warp & 3) * 32 + lane;
+  const int ly0 = (warp >> 2) * RB;
+  const int x = ox + lx;
+  const bool xin = x >= 0 && x < W;
+  const int ytop = oy + ly0;
+  const int lxe = min(lx + 1, RW - 1), lxw = max(lx - 1, 0);
+
+  /* level values and the conductance pair sums of the reference's flux terms:
+   *   xpos uses (c_x + c_x+1), xneg (c_x-1 + c_x), ypos (c_y + c_y+1), yneg (c_y-1 + c_y).
+   * A pair that crosses the image border is zero: its flux is exactly zero
+   * there (the reference omits the term), whatever the neighbour value is. */
+  float Lr[RB], gE[RB], gW[RB], gS[RB];
+  float gN0;
+  float *cur, *nxt;
+
   if (p.first) {
-    const int sx0 = max(rx0 - 1, 0), sx1 = min(rx1 + 1, W), sy0 = max(ry0 - 1, 0), sy1 = min(ry1 + 1, H);
-    const int px0 = max(sx0 - 2, 0), px1 = min(sx1 + 2, W), py0 = max(sy0 - 2, 0), py1 = min(sy1 + 2, H);
-    const int PWm = TW + 2 * d + 6, PHm = TH + 2 * d + 6, SWm = TW + 2 * d + 2, SHm = TH + 2 * d + 2;
-    float *sP = sm;
-    float *sT = sP + PWm * PHm;
-    float *sS = sT + PHm * SWm;
-    gbuf = sS + SWm * SHm;
-    const int pw = px1 - px0, sw = sx1 - sx0;
-    /* predecessor: same-size copy, exact 2x half-sample, or a prepared plane */
+    float *sP = sm, *sT = sm + (RH + 6) * PS, *sS = sT + (RH + 6) * SS;
+    const int px0 = max(ox - 3, 0), px1 = min(ox + RW + 3, W), py0 = max(oy - 3, 0), py1 = min(oy + RH + 3, H);
+    const int sx0 = max(ox - 1, 0), sx1 = min(ox + RW + 1, W), sy0 = max(oy - 1, 0), sy1 = min(oy + RH + 1, H);
+    /* input region: predecessor copy, its exact 2x half-sample, or a prepared plane */
     if (srck == 1) {
       const akz_level_desc Lp = p.t.lv[sg.level_desc - 1];
       const float *pp = planes + Lp.lt;
-      for (int i = tid; i < (py1 - py0) * pw; i += 256) {
-        const int y = py0 + i / pw, x = px0 + i % pw;
-        const float *q0 = pp + (long long)(2 * y) * Lp.pitch + 2 * x;
+      for (int y = py0 + warp; y < py1; y += 16) {
+        const float *q0 = pp + (long long)(2 * y) * Lp.pitch;
         const float *q1 = q0 + Lp.pitch;
-        sP[(y - py0) * pw + (x - px0)] = 0.25f * (((__ldg(q0) + __ldg(q0 + 1)) + __ldg(q1)) + __ldg(q1 + 1));
+        float *o = sP + (y - oy + 3) * PS - ox + 3;
+        for (int xx = px0 + lane; xx < px1; xx += 32) {
+          const float2 a = __ldg((const float2 *)(q0 + 2 * xx)), b = __ldg((const float2 *)(q1 + 2 * xx));
+          o[xx] = 0.25f * (((a.x + a.y) + b.x) + b.y);
+        }
       }
     } else {
       const float *pp;
@@ -309,85 +313,154 @@ __global__ void __launch_bounds__(256) k_fed(akz_fed_params p)
         pp = planes + I.t2;
         pitch = L.pitch;
       }
-      for (int i = tid; i < (py1 - py0) * pw; i += 256) {
-        const int y = py0 + i / pw, x = px0 + i % pw;
-        sP[(y - py0) * pw + (x - px0)] = __ldg(pp + (long long)y * pitch + x);
+      for (int y = py0 + warp; y < py1; y += 16) {
+        const float *q = pp + (long long)y * pitch;
+        float *o = sP + (y - oy + 3) * PS - ox + 3;
+        for (int xx = px0 + lane; xx < px1; xx += 32) o[xx] = __ldg(q + xx);
       }
     }
     __syncthreads();
+    /* sigma-1 Gaussian, horizontal then vertical, replicate border */
     const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
-    for (int i = tid; i < (py1 - py0) * sw; i += 256) {
-      const int y = py0 + i / sw, x = sx0 + i % sw;
-      const float *r = sP + (y - py0) * pw - px0;
-      float acc = k0 * (r[max(x - 2, 0)] + r[min(x + 2, W - 1)]);
-      acc = acc + k1 * (r[max(x - 1, 0)] + r[min(x + 1, W - 1)]);
-      acc = acc + k2 * r[x];
-      sT[(y - py0) * sw + (x - sx0)] = acc;
+    for (int y = py0 + warp; y < py1; y += 16) {
+      const float *r = sP + (y - oy + 3) * PS - ox + 3;
+      float *o = sT + (y - oy + 3) * SS - ox + 1;
+      for (int xx = sx0 + lane; xx < sx1; xx += 32) {
+        float acc = k0 * (r[max(xx - 2, 0)] + r[min(xx + 2, W - 1)]);
+        acc = acc + k1 * (r[max(xx - 1, 0)] + r[min(xx + 1, W - 1)]);
+        acc = acc + k2 * r[xx];
+        o[xx] = acc;
+      }
     }
     __syncthreads();
     float *lsp = planes + L.ls;
-    for (int i = tid; i < (sy1 - sy0) * sw; i += 256) {
-      const int y = sy0 + i / sw, x = sx0 + i % sw;
-      const float *c = sT + (x - sx0) - py0 * sw;
-      float acc = k0 * (c[max(y - 2, 0) * sw] + c[min(y + 2, H - 1) * sw]);
-      acc = acc + k1 * (c[max(y - 1, 0) * sw] + c[min(y + 1, H - 1) * sw]);
-      acc = acc + k2 * c[y * sw];
-      sS[(y - sy0) * sw + (x - sx0)] = acc;
-      if (x >= tx0 && x < tx1 && y >= ty0 && y < ty1) lsp[(long long)y * L.pitch + x] = acc;
+    for (int y = sy0 + warp; y < sy1; y += 16) {
+      const float *c2m = sT + (max(y - 2, 0) - oy + 3) * SS - ox + 1, *c2p = sT + (min(y + 2, H - 1) - oy + 3) * SS - ox + 1;
+      const float *c1m = sT + (max(y - 1, 0) - oy + 3) * SS - ox + 1, *c1p = sT + (min(y + 1, H - 1) - oy + 3) * SS - ox + 1;
+      const float *c0 = sT + (y - oy + 3) * SS - ox + 1;
+      float *o = sS + (y - oy + 1) * SS - ox + 1;
+      const bool yt = y >= ty0 && y < ty1;
+      float *lo = lsp + (long long)y * L.pitch;
+      for (int xx = sx0 + lane; xx < sx1; xx += 32) {
+        float acc = k0 * (c2m[xx] + c2p[xx]);
+        acc = acc + k1 * (c1m[xx] + c1p[xx]);
+        acc = acc + k2 * c0[xx];
+        o[xx] = acc;
+        if (yt && xx >= tx0 && xx < tx1) lo[xx] = acc;
+      }
     }
     __syncthreads();
+    /* conductance on R0 from the Scharr gradient of Lsmooth (reflect-101) */
+    float *sG = sP; /* the input region is not read any more except for L0 below */
     const float inv_k = p.kc[L.image * 16 + L.octave].y;
     float *gp = planes + I.g;
-    for (int i = tid; i < (ry1 - ry0) * rw; i += 256) {
-      const int y = ry0 + i / rw, x = rx0 + i % rw;
-      const int xm = akz_refl101(x - 1, W), xp = akz_refl101(x + 1, W);
-      const int ym = akz_refl101(y - 1, H), yp = akz_refl101(y + 1, H);
-      const float *rm = sS + (ym - sy0) * sw - sx0, *r0 = sS + (y - sy0) * sw - sx0, *rp = sS + (yp - sy0) * sw - sx0;
-      const float hm = rm[xp] - rm[xm];
-      const float h0 = r0[xp] - r0[xm];
-      const float hp = rp[xp] - rp[xm];
-      const float lx = 3.0f * (hm + hp) + 10.0f * h0;
-      const float syp = 3.0f * (rp[xm] + rp[xp]) + 10.0f * rp[x];
-      const float sym = 3.0f * (rm[xm] + rm[xp]) + 10.0f * rm[x];
-      const float ly = syp - sym;
-      const float gv = akz_conductance(lx, ly, inv_k, p.diffusivity);
-      gbuf[(y - ry0) * rw + (x - rx0)] = gv;
-      if (p.write_g && x >= tx0 && x < tx1 && y >= ty0 && y < ty1) gp[(long long)y * L.pitch + x] = gv;
+    /* L0 of this thread's pixels before sG overwrites the input region */
+    for (int r = 0; r < RB; r++) {
+      const int y = ytop + r;
+      Lr[r] = (xin && y >= 0 && y < H) ? sP[(ly0 + r + 3) * PS + lx + 3] : 0.0f;
     }
     __syncthreads();
-    src = akz_smem_acc{sP, px0, py0, pw};
-    bufA = sT; /* rowtmp region, free now, holds >= R0 */
-    bufB = sS; /* smoothing region, free now */
+    for (int ly = warp; ly < RH; ly += 16) {
+      const int y = oy + ly;
+      const bool yin = y >= 0 && y < H;
+      const int ym = y > 0 ? y - 1 : 1, yp = y < H - 1 ? y + 1 : H - 2;
+      const float *rm = sS + (ym - oy + 1) * SS - ox + 1, *r0 = sS + (y - oy + 1) * SS - ox + 1;
+      const float *rp = sS + (yp - oy + 1) * SS - ox + 1;
+      const bool yt = y >= ty0 && y < ty1 && p.write_g;
+      for (int l = lane; l < RW; l += 32) {
+        const int xx = ox + l;
+        float gv = 0.0f;
+        if (yin && xx >= 0 && xx < W) {
+          const int xm = xx > 0 ? xx - 1 : 1, xp = xx < W - 1 ? xx + 1 : W - 2;
+          const float hm = rm[xp] - rm[xm];
+          const float h0 = r0[xp] - r0[xm];
+          const float hp = rp[xp] - rp[xm];
+          const float gx = 3.0f * (hm + hp) + 10.0f * h0;
+          const float syp = 3.0f * (rp[xm] + rp[xp]) + 10.0f * rp[xx];
+          const float sym = 3.0f * (rm[xm] + rm[xp]) + 10.0f * rm[xx];
+          const float gy = syp - sym;
+          gv = akz_conductance(gx, gy, inv_k, p.diffusivity);
+          if (yt && xx >= tx0 && xx < tx1) gp[(long long)y * L.pitch + xx] = gv;
+        }
+        sG[ly * RW + l] = gv;
+      }
+    }
+    __syncthreads();
+    const bool xe_in = xin && x + 1 < W, xw_in = xin && x >= 1;
+    for (int r = 0; r < RB; r++) {
+      const int ly = ly0 + r, y = ytop + r;
+      const float gc = sG[ly * RW + lx];
+      const bool yin = y >= 0 && y < H;
+      gE[r] = (yin && xe_in) ? gc + sG[ly * RW + lxe] : 0.0f;
+      gW[r] = (yin && xw_in) ? sG[ly * RW + lxw] + gc : 0.0f;
+      gS[r] = (xin && y >= 0 && y + 1 < H) ? gc + sG[min(ly + 1, RH - 1) * RW + lx] : 0.0f;
+    }
+    gN0 = (xin && ytop >= 1 && ytop < H) ? sG[max(ly0 - 1, 0) * RW + lx] + sG[ly0 * RW + lx] : 0.0f;
+    cur = sT; /* the row-pass buffer is free now and larger than R0 */
+    nxt = sS; /* so is the smoothing buffer, once the conductance is done */
+    __syncthreads();
   } else {
-    gbuf = sm;
-    bufA = sm + (TW + 2 * d) * (TH + 2 * d);
-    bufB = bufA + (TW + 2 * d) * (TH + 2 * d);
+    cur = sm;
+    nxt = sm + RW * RH;
     const float *lp = planes + (p.src == 1 ? I.t1 : I.t2);
     const float *gp = planes + I.g;
-    for (int i = tid; i < (ry1 - ry0) * rw; i += 256) {
-      const int y = ry0 + i / rw, x = rx0 + i % rw;
-      bufB[(y - ry0) * rw + (x - rx0)] = __ldg(lp + (long long)y * L.pitch + x);
-      gbuf[(y - ry0) * rw + (x - rx0)] = __ldg(gp + (long long)y * L.pitch + x);
+    const long long pitch = L.pitch;
+    const int xc = min(max(x, 0), W - 1);
+    for (int r = 0; r < RB; r++) {
+      const int y = ytop + r;
+      Lr[r] = 0.0f;
+      gE[r] = gW[r] = gS[r] = 0.0f;
+      if (xin && y >= 0 && y < H) {
+        const float *gr = gp + (long long)y * pitch;
+        const float gc = __ldg(gr + xc);
+        Lr[r] = __ldg(lp + (long long)y * pitch + xc);
+        if (x + 1 < W) gE[r] = gc + __ldg(gr + xc + 1);
+        if (x >= 1) gW[r] = __ldg(gr + xc - 1) + gc;
+        if (y + 1 < H) gS[r] = gc + __ldg(gr + pitch + xc);
+      }
+    }
+    gN0 = (xin && ytop >= 1 && ytop < H) ? __ldg(gp + (long long)(ytop - 1) * pitch + xc) + __ldg(gp + (long long)ytop * pitch + xc) : 0.0f;
+  }
+  for (int r = 0; r < RB; r++) cur[(ly0 + r) * RW + lx] = Lr[r];
+  __syncthreads();
+
+  /* FED steps: xpos - xneg + ypos - yneg, scaled by tau/2, added to L
+   * (nld_step_scalar, nldiffusion_functions.cpp:232-237 and :309-316) */
+  const int lyn = max(ly0 - 1, 0), lys = min(ly0 + RB, RH - 1);
+  for (int s = 0; s < d; s++) {
+    const float h = p.h[s];
+    float prev = cur[lyn * RW + lx];
+    const float below = cur[lys * RW + lx];
+#pragma unroll
+    for (int r = 0; r < RB; r++) {
+      const int ly = ly0 + r;
+      const float Lc = Lr[r];
+      const float Le = cur[ly * RW + lxe];
+      const float Lw = cur[ly * RW + lxw];
+      const float Ls = r < RB - 1 ? Lr[r + 1] : below;
+      const float gn = r == 0 ? gN0 : gS[r - 1];
+      const float xpos = gE[r] * (Le - Lc);
+      const float xneg = gW[r] * (Lc - Lw);
+      const float ypos = gS[r] * (Ls - Lc);
+      const float yneg = gn * (Lc - prev);
+      const float nv = Lc + h * (xpos - xneg + ypos - yneg);
+      nxt[ly * RW + lx] = nv;
+      prev = Lc;
+      Lr[r] = nv;
     }
     __syncthreads();
-    src = akz_smem_acc{bufB, rx0, ry0, rw};
+    float *t = cur;
+    cur = nxt;
+    nxt = t;
   }
-  /* steps: write into bufA, then alternate */
-  float *dstb = bufA, *other = bufB;
-  for (int s = 1; s <= d; s++) {
-    const int ax0 = max(tx0 - (d - s), 0), ax1 = min(tx1 + (d - s), W);
-    const int ay0 = max(ty0 - (d - s), 0), ay1 = min(ty1 + (d - s), H);
-    akz_fed_step(src, dstb, rx0, ry0, rw, gbuf, rx0, ry0, rw, ax0, ax1, ay0, ay1, W, H, p.h[s - 1]);
-    __syncthreads();
-    src = akz_smem_acc{dstb, rx0, ry0, rw};
-    float *t = dstb;
-    dstb = other;
-    other = t;
-  }
+  /* tile interior from registers */
   float *out = planes + (p.dst == 0 ? L.lt : (p.dst == 1 ? I.t1 : I.t2));
-  for (int i = tid; i < (ty1 - ty0) * (tx1 - tx0); i += 256) {
-    const int y = ty0 + i / (tx1 - tx0), x = tx0 + i % (tx1 - tx0);
-    out[(long long)y * L.pitch + x] = src(x, y);
+  if (x >= tx0 && x < tx1) {
+#pragma unroll
+    for (int r = 0; r < RB; r++) {
+      const int y = ytop + r;
+      if (y >= ty0 && y < ty1) out[(long long)y * L.pitch + x] = Lr[r];
+    }
   }
 }
 
@@ -446,23 +519,14 @@ cudaError_t akz_launch_gauss0(const akz_gauss_params &p, int ntiles, cudaStream_
   return cudaGetLastError();
 }
 
-cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int tw, int th, cudaStream_t s)
+cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int, int, cudaStream_t s)
 {
   if (ntiles <= 0) return cudaSuccess;
-  const size_t smem = akz_fed_smem_bytes(tw, th, p.steps, p.first);
-  const dim3 block(32, 8);
-  if (tw == 128 && th == 32) {
-    cudaFuncSetAttribute(k_fed<128, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_fed<128, 32><<<ntiles, block, smem, s>>>(p);
-  } else if (tw == 64 && th == 32) {
-    cudaFuncSetAttribute(k_fed<64, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_fed<64, 32><<<ntiles, block, smem, s>>>(p);
-  } else if (tw == 64 && th == 64) {
-    cudaFuncSetAttribute(k_fed<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_fed<64, 64><<<ntiles, block, smem, s>>>(p);
-  } else {
-    return cudaErrorInvalidValue;
-  }
+  if (p.steps < 1 || p.steps > 8) return cudaErrorInvalidValue;
+  const size_t smem = akz_fed_smem_bytes(0, 0, p.steps, p.first);
+  cudaError_t e = cudaFuncSetAttribute(k_fed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_fed<<<ntiles, AKZ_FED_THREADS, smem, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu: --batch images, one graph-less run of every stage, no timing line")
     return ap.parse_args()
 
 
@@ -227,6 +229,11 @@ def main():
     batch.set_stream(stream.cuda_stream)
     batch.upload(imgs)
     torch.cuda.synchronize()
+    if args.profile_case:
+        ms = batch.profile()
+        print(json.dumps({"profile_case": f"{B} x {W}x{H}", "stage_ms": [float(x) for x in ms],
+                          "keypoints": [int(c) for c in batch.counts()]}))
+        return 0
 
     # device-resident throughput
     for _ in range(max(args.warmup, 3)):
