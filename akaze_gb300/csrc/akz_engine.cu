@@ -49,6 +49,9 @@ static akz_status akz_fail_cuda(cudaError_t e, const char *expr, const char *fil
                   cudaGetErrorString(e), file, line);
 }
 
+/* Records an error for akz_last_error from other translation units. */
+akz_status akz_report(akz_status s, const char *msg) { return akz_fail(s, "%s", msg); }
+
 #define CK(x)                                                                 \
   do {                                                                        \
     cudaError_t e_ = (x);                                                     \

@@ -16,7 +16,12 @@
  */
 #include <cuda_runtime.h>
 
+#include <mutex>
+
+#include "../../include/akaze_gb300.h"
 #include "akz_device.cuh"
+
+akz_status akz_report(akz_status s, const char *msg);
 
 #define AKZ_MQ 256
 #define AKZ_MT 256
@@ -123,3 +128,79 @@ int akz_match_splits(int nq, int nt, int nsm)
 }
 
 size_t akz_match_partial_bytes(int nq, int nsplit) { return (size_t)nq * nsplit * sizeof(akz_top2); }
+
+/* ------------------------------------------------------------------------ */
+/* Allocation-free 2-NN match.
+ *
+ * For callers that cannot call cudaMalloc: a plugin that runs inside a host
+ * application which owns all device memory and hands out fixed buffers (a
+ * video or inference pipeline with a planned memory budget), or code on a
+ * latency-critical path where an allocation would synchronise the device.
+ * The caller passes the query and train rows and the output in device
+ * memory; the per-split top-2 scratch lives in the library's own
+ * statically sized device array below, so the call allocates nothing.
+ *
+ * Limit: nq * splits top-2 records must fit the array, i.e. at most
+ * AKZ_NOALLOC_MAX_RECORDS (131072) query rows per call; larger nq is
+ * rejected with AKZ_ERR_INVALID_ARG.  Every GPU that loads the library holds
+ * the array (2 MiB) until the process exits.  All calls share it: each call
+ * rewrites every record it reads (nothing needs to start at zero), and calls
+ * whose kernels overlap on the GPU (different streams, or another host
+ * thread) race on it and must be serialised by the caller.
+ */
+#define AKZ_NOALLOC_MAX_RECORDS 131072
+#define AKZ_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) akz_top2 g_akz_noalloc_scratch[AKZ_NOALLOC_MAX_RECORDS];
+
+static std::mutex g_noalloc_mutex;
+static void *g_noalloc_addr[AKZ_NOALLOC_MAX_DEVICES];
+static int g_noalloc_sms[AKZ_NOALLOC_MAX_DEVICES];
+
+/* Device address of the scratch array on the current device, resolved once
+ * per device (host code cannot use the symbol itself as a device pointer). */
+static cudaError_t akz_noalloc_setup(int *dev_out, void **addr, int *nsm)
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= AKZ_NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_akz_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    g_noalloc_sms[dev] = sms;
+    g_noalloc_addr[dev] = ptr;
+  }
+  *dev_out = dev;
+  *addr = g_noalloc_addr[dev];
+  *nsm = g_noalloc_sms[dev];
+  return cudaSuccess;
+}
+
+extern "C" AKZ_API akz_status akz_matcher_bfmatch_noalloc(const uint8_t *query64, int nq, const uint8_t *train64, int nt,
+                                                         akz_dmatch *out, void *stream)
+{
+  if (nq < 0 || nt < 0) return akz_report(AKZ_ERR_INVALID_ARG, "akz_matcher_bfmatch_noalloc: negative size");
+  if (nq > AKZ_NOALLOC_MAX_RECORDS)
+    return akz_report(AKZ_ERR_INVALID_ARG,
+                      "akz_matcher_bfmatch_noalloc: more than 131072 query rows (the fixed scratch limit); "
+                      "use akz_matcher_bfmatch_device");
+  if (nq == 0) return AKZ_OK;
+  if (!query64 || !out || (nt > 0 && !train64))
+    return akz_report(AKZ_ERR_INVALID_ARG, "akz_matcher_bfmatch_noalloc: NULL device buffer");
+  int dev = 0, nsm = 0;
+  void *scratch = nullptr;
+  cudaError_t e = akz_noalloc_setup(&dev, &scratch, &nsm);
+  if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
+  int ns = akz_match_splits(nq, nt, nsm);
+  const int fit = AKZ_NOALLOC_MAX_RECORDS / nq;
+  if (ns > fit) ns = fit;
+  e = akz_match_run(query64, nq, train64, nt, out, scratch, ns, (cudaStream_t)stream);
+  if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
+  return AKZ_OK;
+}

@@ -192,6 +192,21 @@ AKZ_API akz_status akz_matcher_bfmatch(akz_matcher *m, const uint8_t *query, int
 AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *query64, int nq, const uint8_t *train64,
                                               int nt, akz_dmatch *out);
 
+/* Allocation-free variant of akz_matcher_bfmatch_device (no counterpart in
+ * the reference).  For callers that cannot allocate device memory, such as a
+ * plugin inside a host that owns the whole device memory budget or a hot
+ * path where cudaMalloc would synchronise: query64 (nq x 64 B), train64
+ * (nt x 64 B) and out (2*nq matches) are caller-provided device buffers; the
+ * scratch is a fixed 2 MiB device array inside the library, held by every
+ * GPU that loads it until exit.  At most 131072 query rows per call (larger
+ * nq returns AKZ_ERR_INVALID_ARG).  The first call on a device resolves the
+ * array's address; make that first call before any stream capture.  Calls
+ * share the array, so calls that overlap on the GPU race: serialise them.
+ * Runs on stream (a cudaStream_t; NULL for the legacy default stream) and
+ * returns without synchronising. */
+AKZ_API akz_status akz_matcher_bfmatch_noalloc(const uint8_t *query64, int nq, const uint8_t *train64, int nt,
+                                              akz_dmatch *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
