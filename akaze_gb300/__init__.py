@@ -46,6 +46,32 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else None
 
 
+def plan(options, width, height):
+    """Level plan of an image (host only, no GPU): list of dicts with size,
+    octave, sublevel, esigma, deriv_step, border and the FED taus."""
+    L = load()
+    n = ctypes.c_int()
+    check(L.akz_plan_info(ctypes.byref(options), width, height, -1, ctypes.byref(n), *([None] * 8), 0, None))
+    out = []
+    for i in range(n.value):
+        lw, lh, o, s, ds, ns = (ctypes.c_int() for _ in range(6))
+        es, bd = ctypes.c_float(), ctypes.c_float()
+        tau = np.zeros(4096, np.float32)
+        check(L.akz_plan_info(ctypes.byref(options), width, height, i, None, ctypes.byref(lw), ctypes.byref(lh),
+                              ctypes.byref(o), ctypes.byref(s), ctypes.byref(es), ctypes.byref(ds), ctypes.byref(bd),
+                              _ptr(tau), 4096, ctypes.byref(ns)))
+        out.append({"width": lw.value, "height": lh.value, "octave": o.value, "sublevel": s.value, "esigma": es.value,
+                    "deriv_step": ds.value, "border": bd.value, "nsteps": ns.value, "tau": tau[: ns.value].copy()})
+    return out
+
+
+def gaussian_taps(sigma):
+    t = np.zeros(64, np.float32)
+    n = ctypes.c_int()
+    check(load().akz_gaussian_taps(float(sigma), _ptr(t), 64, ctypes.byref(n)))
+    return t[: n.value].copy()
+
+
 class AKAZE:
     """libAKAZECU::AKAZE (AKAZE.h:58-143) over the C ABI."""
 

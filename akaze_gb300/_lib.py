@@ -19,7 +19,7 @@ EXTREMUM_DTYPE = np.dtype([("x", "<i4"), ("y", "<i4"), ("level", "<i4"), ("octav
 
 # every symbol include/akaze_gb300.h declares
 EXPORTS = [
-    "akz_version", "akz_last_error", "akz_options_default", "akz_create", "akz_destroy", "akz_set_stream",
+    "akz_version", "akz_last_error", "akz_options_default", "akz_plan_info", "akz_gaussian_taps", "akz_create", "akz_destroy", "akz_set_stream",
     "akz_create_nonlinear_scale_space", "akz_feature_detection", "akz_compute_descriptors", "akz_get_timing",
     "akz_num_levels", "akz_level_info", "akz_get_level_plane", "akz_get_kcontrast", "akz_get_extrema",
     "akz_batch_create", "akz_batch_destroy", "akz_batch_set_stream", "akz_batch_upload", "akz_batch_input",
@@ -72,6 +72,9 @@ def load():
     sig = {
         "akz_version": ([], ctypes.c_char_p), "akz_last_error": ([], ctypes.c_char_p),
         "akz_options_default": ([ctypes.POINTER(AkzOptions)], I),
+        "akz_plan_info": ([ctypes.POINTER(AkzOptions), I, I, I, IP, IP, IP, IP, IP, ctypes.POINTER(ctypes.c_float), IP,
+                           ctypes.POINTER(ctypes.c_float), P, I, IP], I),
+        "akz_gaussian_taps": ([ctypes.c_float, P, I, IP], I),
         "akz_create": ([ctypes.POINTER(AkzOptions), ctypes.POINTER(P)], I),
         "akz_destroy": ([P], I), "akz_set_stream": ([P, P], I),
         "akz_create_nonlinear_scale_space": ([P, P, I, I, S, I, I], I),

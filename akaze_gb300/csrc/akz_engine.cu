@@ -817,6 +817,43 @@ AKZ_API akz_status akz_options_default(akz_options *o)
   return AKZ_OK;
 }
 
+AKZ_API akz_status akz_plan_info(const akz_options *opt, int width, int height, int level, int *nlevels, int *lw, int *lh,
+                                 int *octave, int *sublevel, float *esigma, int *deriv_step, float *border, float *tau,
+                                 int tau_cap, int *nsteps)
+{
+  akz_status st = akz_validate(opt);
+  if (st != AKZ_OK) return st;
+  if (width < 1 || height < 1) return akz_fail(AKZ_ERR_INVALID_ARG, "bad image size");
+  std::vector<akz_geo> L;
+  std::vector<std::vector<float>> tv;
+  akz_plan_levels(*opt, width, height, L, tv);
+  if (nlevels) *nlevels = (int)L.size();
+  if (level < 0) return AKZ_OK;
+  if (level >= (int)L.size()) return akz_fail(AKZ_ERR_INVALID_ARG, "level %d out of range", level);
+  const akz_geo &g = L[level];
+  if (lw) *lw = g.w;
+  if (lh) *lh = g.h;
+  if (octave) *octave = g.octave;
+  if (sublevel) *sublevel = g.sublevel;
+  if (esigma) *esigma = g.esigma;
+  if (deriv_step) *deriv_step = g.deriv_step;
+  if (border) *border = g.border;
+  if (nsteps) *nsteps = g.nsteps;
+  if (tau)
+    for (int k = 0; k < g.nsteps && k < tau_cap; k++) tau[k] = tv[level][k];
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_gaussian_taps(float sigma, float *taps, int cap, int *ntaps)
+{
+  float t[AKZ_MAX_TAPS];
+  const int R = akz_gauss_taps(sigma, t);
+  if (R < 0) return akz_fail(AKZ_ERR_INVALID_ARG, "Gaussian radius out of range");
+  if (ntaps) *ntaps = 2 * R + 1;
+  for (int i = 0; i <= 2 * R && i < cap; i++) taps[i] = t[i];
+  return AKZ_OK;
+}
+
 AKZ_API akz_status akz_create(const akz_options *opt, akz_context **out)
 {
   if (!opt || !out) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_create: NULL argument");

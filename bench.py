@@ -219,10 +219,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import akaze_gb300 as akz
-    from akaze_gb300 import synth
+    from akaze_gb300 import replicas, synth
 
     B, W, H = args.batch, args.width, args.height
-    imgs = [synth.synth_image(10000 * rank + i, W, H) for i in range(B)]
+    imgs = [synth.synth_image(s, W, H) for s in replicas.rank_seeds(rank, B)]
     opt = akz.AKAZEOptions()
     batch = akz.Batch(opt, [(W, H)] * B)
     stream = torch.cuda.Stream()
@@ -254,13 +254,8 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop() if sampler else None
-    ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-    ms_max = float(t.item())
-    value = B * ws * args.steps / (ms_max / 1000.0)
+    ms_max = replicas.max_over_ranks(e0.elapsed_time(e1), dist, device="cuda")
+    value = replicas.job_throughput(B * args.steps, ws, ms_max / 1000.0)
 
     # stage profile (one non-graph run) for the roofline of the level stage
     stage = [float(x) for x in batch.profile()]
@@ -286,11 +281,8 @@ def main():
     e_steps = max(1, min(args.steps, 10))
     for _ in range(e_steps):
         c2 = batch.detect_describe_into(np_in, kps, ds)
-    el = time.perf_counter() - t0
-    te = torch.tensor([el], device="cuda")
-    if dist:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e = B * ws * e_steps / float(te.item())
+    el = replicas.max_over_ranks(time.perf_counter() - t0, dist, device="cuda")
+    e2e = replicas.job_throughput(B * e_steps, ws, el)
     h2d = B * W * H
     d2h = int(sum(c2)) * (28 + 61) + B * 32
 

@@ -109,6 +109,18 @@ AKZ_API const char *akz_last_error(void);
 /* setDefaultAKAZEOptions / AKAZEOptions::AKAZEOptions (AKAZEConfig.h:86-111). */
 AKZ_API akz_status akz_options_default(akz_options *opt);
 
+/* Level plan of an image, computed on the host without touching the GPU
+ * (AKAZE.cpp:146-197, fed.cpp:41-148): level count, and for level >= 0 its
+ * size, octave, sublevel, evolution sigma, detector step, extrema border and
+ * FED step sizes (tau, up to tau_cap) that lead to it.  No counterpart in the
+ * reference, which keeps the plan private. */
+AKZ_API akz_status akz_plan_info(const akz_options *opt, int width, int height, int level, int *nlevels, int *lw,
+                                 int *lh, int *octave, int *sublevel, float *esigma, int *deriv_step, float *border,
+                                 float *tau, int tau_cap, int *nsteps);
+/* Gaussian taps the library uses for sigma (nldiffusion_functions.cpp:33-43
+ * kernel-size rule), for inspection. */
+AKZ_API akz_status akz_gaussian_taps(float sigma, float *taps, int cap, int *ntaps);
+
 /* ---- single image: libAKAZECU::AKAZE (AKAZE.h:58-143) ---------------- */
 
 /* AKAZE::AKAZE(options) + Allocate_Memory_Evolution (AKAZE.cpp:126-208):

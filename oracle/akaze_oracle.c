@@ -936,3 +936,6 @@ float ako_atan2f(float y, float x) { return akz_atan2f(y, x); }
 void ako_sincosf(float x, float *s, float *c) { akz_sincosf(x, s, c); }
 float ako_expf(float x) { return akz_expf(x); }
 float ako_recip1pf(float f) { return akz_recip1pf(f); }
+
+/* The 486 comparison pairs of the M-LDB bits in bit order (test hook). */
+int ako_descriptor_pairs(int *i1, int *i2) { return ako_cmp_pairs(i1, i2); }

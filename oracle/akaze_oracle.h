@@ -138,6 +138,8 @@ float ako_atan2f(float y, float x);
 void ako_sincosf(float x, float *s, float *c);
 float ako_expf(float x);
 float ako_recip1pf(float f);
+/* The 486 M-LDB comparison pairs (value index cell*3+channel), bit order. */
+int ako_descriptor_pairs(int *i1, int *i2);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,77 @@
+"""The C ABI library without a GPU: it builds for sm_103a, loads, exports
+every symbol include/akaze_gb300.h declares, mirrors the reference's option
+defaults and API shape, and reports bad arguments as status codes."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    with open(os.path.join(ROOT, "include", "akaze_gb300.h")) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"AKZ_API\s+[\w\s\*]+?\b(akz_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    L = gpu_lib.load()
+    declared = _declared()
+    assert len(declared) >= 30
+    for name in declared:
+        assert hasattr(L, name), name
+    assert set(declared) == set(gpu_lib._lib.EXPORTS)
+
+
+def test_defaults_mirror_akazeoptions(gpu_lib):
+    # AKAZEConfig.h:86-111
+    o = gpu_lib.AKAZEOptions()
+    assert (o.omax, o.nsublevels, o.descriptor, o.descriptor_size, o.descriptor_channels) == (4, 4, 5, 0, 3)
+    assert (o.descriptor_pattern_size, o.kcontrast_nbins, o.ncudaimages, o.maxkeypoints) == (10, 300, 4, 131072)
+    assert (o.soffset, o.derivative_factor, o.sderivatives) == (pytest.approx(1.6), 1.5, 1.0)
+    assert (o.dthreshold, o.min_dthreshold, o.kcontrast_percentile) == (
+        pytest.approx(0.001), pytest.approx(1e-5), pytest.approx(0.7))
+    assert o.diffusivity == gpu_lib.PM_G2
+    o.setWidth(123)
+    o.setHeight(45)
+    assert (o.img_width, o.img_height) == (123, 45)
+
+
+@pytest.mark.parametrize("field,value,status", [
+    ("descriptor", 1, 6),            # SURF: not implemented (the reference prints the same)
+    ("descriptor_size", 64, 6),      # random bit subsets: not implemented
+    ("omax", 0, 1),
+    ("kcontrast_nbins", 0, 1),
+    ("soffset", 0.1, 1),
+    ("descriptor_pattern_size", 12, 1),
+])
+def test_invalid_options_are_status_codes(gpu_lib, field, value, status):
+    o = gpu_lib.AKAZEOptions()
+    o.setWidth(64)
+    o.setHeight(64)
+    setattr(o, field, value)
+    h = ctypes.c_void_p()
+    st = gpu_lib.load().akz_create(ctypes.byref(o), ctypes.byref(h))
+    assert st == status
+    assert gpu_lib.load().akz_last_error()
+
+
+def test_null_and_size_errors(gpu_lib):
+    L = gpu_lib.load()
+    assert L.akz_options_default(None) == 1
+    assert L.akz_create(None, None) == 1
+    assert L.akz_feature_detection(None, None) == 1
+    o = gpu_lib.AKAZEOptions()
+    h = ctypes.c_void_p()
+    assert L.akz_batch_create(ctypes.byref(o), 0, None, None, ctypes.byref(h)) == 1
+    assert L.akz_matcher_bfmatch(None, None, 1, None, 1, 61, None) == 1
+
+
+def test_python_api_mirrors_reference_binding(gpu_lib):
+    # python/python_bindings.cpp:27-40 and AKAZE.h:58-143
+    for name in ("Create_Nonlinear_Scale_Space", "Feature_Detection", "Compute_Descriptors", "Get_Computation_Times"):
+        assert callable(getattr(gpu_lib.AKAZE, name))
+    assert callable(gpu_lib.Matcher.BFMatch) and callable(gpu_lib.Matcher.bfmatch)
+    assert gpu_lib.KEYPOINT_DTYPE.itemsize == 28 and gpu_lib.DMATCH_DTYPE.itemsize == 16
