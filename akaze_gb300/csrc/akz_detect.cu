@@ -28,6 +28,102 @@
 
 /* ------------------------------------------------------------------------ */
 
+/* k_detect for a tile whose Lsmooth region (tile +- (2*ST+1)) lies inside
+ * the level: no reflection, compile-time region sizes, straight-line loops.
+ * Same arithmetic, in the same order, as the general path. */
+template <int ST>
+__device__ __forceinline__ void akz_detect_interior(const akz_detect_params &p, const akz_level_desc &L, float *sm,
+                                                    int tx0, int ty0)
+{
+  constexpr int TW = AKZ_DETECT_TW, TH = AKZ_DETECT_TH;
+  constexpr int SW = TW + 4 * ST + 2, SH = TH + 4 * ST + 2;
+  constexpr int DW = TW + 2 * ST + 2, DH = TH + 2 * ST + 2;
+  constexpr int EW = TW + 2, EH = TH + 2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float *sS = sm, *sX = sm + SW * SH, *sY = sX + DW * DH, *sD = sY + DW * DH;
+  const float fac1 = p.fac1, fac2 = p.fac2;
+  const float *ls = p.t.planes + L.ls + (long long)(ty0 - 2 * ST - 1) * L.pitch + (tx0 - 2 * ST - 1);
+#pragma unroll 2
+  for (int n = warp; n < SH; n += 8) {
+    const float *q = ls + (long long)n * L.pitch;
+#pragma unroll
+    for (int j = 0; j < (SW + 31) / 32; j++) {
+      const int m = lane + 32 * j;
+      if (m < SW) sS[n * SW + m] = __ldg(q + m);
+    }
+  }
+  __syncthreads();
+  float *lxp = p.t.planes + L.lx + (long long)(ty0 - ST - 1) * L.pitch + (tx0 - ST - 1);
+  float *lyp = p.t.planes + L.ly + (long long)(ty0 - ST - 1) * L.pitch + (tx0 - ST - 1);
+#pragma unroll 2
+  for (int n = warp; n < DH; n += 8) {
+    const float *su = sS + n * SW, *sc = su + ST * SW, *sd = su + 2 * ST * SW;
+    const bool yt = n >= ST + 1 && n < ST + 1 + TH;
+#pragma unroll
+    for (int j = 0; j < (DW + 31) / 32; j++) {
+      const int m = lane + 32 * j;
+      if (m < DW) {
+        const float ul = su[m], ur = su[m + 2 * ST], ll = sd[m], lr = sd[m + 2 * ST];
+        const float cl = sc[m], cr = sc[m + 2 * ST], uc = su[m + ST], lc = sd[m + ST];
+        const float a = fac1 * (ur + lr - ul - ll) + fac2 * (cr - cl);
+        const float b = fac1 * (lr + ll - ur - ul) + fac2 * (lc - uc);
+        sX[n * DW + m] = a;
+        sY[n * DW + m] = b;
+        if (yt && m >= ST + 1 && m < ST + 1 + TW) {
+          lxp[(long long)n * L.pitch + m] = a;
+          lyp[(long long)n * L.pitch + m] = b;
+        }
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll 2
+  for (int n = warp; n < EH; n += 8) {
+    const float *xu = sX + n * DW, *xc = xu + ST * DW, *xd = xu + 2 * ST * DW;
+    const float *yu = sY + n * DW, *yd = yu + 2 * ST * DW;
+#pragma unroll
+    for (int j = 0; j < (EW + 31) / 32; j++) {
+      const int m = lane + 32 * j;
+      if (m < EW) {
+        float ul = xu[m], ur = xu[m + 2 * ST], ll = xd[m], lr = xd[m + 2 * ST];
+        const float lxx = fac1 * (ur + lr - ul - ll) + fac2 * (xc[m + 2 * ST] - xc[m]);
+        const float lyx = fac1 * (lr + ll - ur - ul) + fac2 * (xd[m + ST] - xu[m + ST]);
+        ul = yu[m];
+        ur = yu[m + 2 * ST];
+        ll = yd[m];
+        lr = yd[m + 2 * ST];
+        const float lyy = fac1 * (lr + ll - ur - ul) + fac2 * (yd[m + ST] - yu[m + ST]);
+        sD[n * EW + m] = lxx * lyy - lyx * lyx;
+      }
+    }
+  }
+  __syncthreads();
+  const float border = L.border;
+  const int W = L.width, H = L.height;
+#pragma unroll 2
+  for (int j = warp; j < TH; j += 8) {
+    const int y = ty0 + j;
+    const int up_y = (int)((float)y - border + 0.5f) - 1;
+    const int down_y = (int)((float)y + border + 0.5f) + 1;
+    if (up_y < 0 || down_y >= H) continue;
+#pragma unroll
+    for (int k = 0; k < TW / 32; k++) {
+      const int i = lane + 32 * k;
+      const int x = tx0 + i;
+      const int left_x = (int)((float)x - border + 0.5f) - 1;
+      const int right_x = (int)((float)x + border + 0.5f) + 1;
+      if (left_x < 0 || right_x >= W) continue;
+      const float *c = sD + (j + 1) * EW + (i + 1);
+      const float v = c[0];
+      if (v > p.thr && v > c[-EW - 1] && v > c[EW + 1] && v > c[EW - 1] && v > c[-EW + 1] && v > c[-1] && v > c[1] &&
+          v > c[EW] && v > c[-EW]) {
+        atomicOr(&p.bitmap[L.bitmap + (long long)y * L.bitmap_pitch + (x >> 5)], 1u << (x & 31));
+        atomicAdd(&p.rowcnt[L.rows + y], 1);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_step)
 {
   constexpr int TW = AKZ_DETECT_TW, TH = AKZ_DETECT_TH;
@@ -46,6 +142,17 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   const int dy0 = max(ty0 - st - 1, 0), dy1 = min(ty1 + st + 1, H);
   const int ex0 = max(tx0 - 1, 0), ex1 = min(tx1 + 1, W), ey0 = max(ty0 - 1, 0), ey1 = min(ty1 + 1, H);
   const int sw = sx1 - sx0, dw = dx1 - dx0, ew = ex1 - ex0;
+  const bool interior = tx0 - 2 * st - 1 >= 0 && ty0 - 2 * st - 1 >= 0 && tx0 + TW + 2 * st + 1 <= W &&
+                        ty0 + TH + 2 * st + 1 <= H;
+  if (interior && st >= 2 && st <= 4 && st <= max_step) {
+    if (st == 2)
+      akz_detect_interior<2>(p, L, sm, tx0, ty0);
+    else if (st == 3)
+      akz_detect_interior<3>(p, L, sm, tx0, ty0);
+    else
+      akz_detect_interior<4>(p, L, sm, tx0, ty0);
+    return;
+  }
   const int SM = (TW + 4 * max_step + 2) * (TH + 4 * max_step + 2);
   const int DM = (TW + 2 * max_step + 2) * (TH + 2 * max_step + 2);
   float *sS = sm, *sX = sm + SM, *sY = sX + DM, *sD = sY + DM;

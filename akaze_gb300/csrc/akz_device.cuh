@@ -39,10 +39,11 @@ __device__ __forceinline__ int akz_find_seg(const akz_tile_seg *segs, int nsegs,
   return lo;
 }
 
-/* Input pixel of image img as float in [0,1]: u8 * (float)(1/255) or f32. */
+/* Input pixel of image img as float in [0,1]: u8 * (float)(1/255) or f32.
+ * Both staging arrays use the same element offsets and pitches. */
 __device__ __forceinline__ float akz_fetch_input(const akz_tables &t, const akz_image_desc &I, int x, int y, float inv255)
 {
-  if (t.input_f32) return __ldg(t.f32 + (I.u8_off >> 2) + (long long)y * (I.u8_pitch >> 2) + x);
+  if (t.input_f32) return __ldg(t.f32 + I.u8_off + (long long)y * I.u8_pitch + x);
   return (float)__ldg(t.u8 + I.u8_off + (long long)y * I.u8_pitch + x) * inv255;
 }
 

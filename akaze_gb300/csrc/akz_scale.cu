@@ -249,6 +249,148 @@ size_t akz_fed_smem_bytes(int, int, int, int first)
   return (P + T + S) * sizeof(float);
 }
 
+/* First-chunk prologue of k_fed for a tile whose input region (R0 +- 3)
+ * lies inside the image: every region has its full compile-time size and no
+ * neighbour needs clamping or reflecting, so the loops are straight-line.
+ * Same arithmetic, in the same order, as the general path in k_fed. */
+template <int SRCK>
+__device__ __forceinline__ void akz_fed_prologue_interior(const akz_fed_params &p, const akz_level_desc &L,
+                                                          const akz_image_desc &I, int level_desc, float *sm, int ox,
+                                                          int oy, int tx0, int ty0, int tx1, int ty1, int lx, int ly0,
+                                                          float *Lr, float *gE, float *gW, float *gS, float &gN0)
+{
+  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
+  constexpr int PS = RW + 6, SS = RW + 2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float *sP = sm, *sT = sm + (RH + 6) * PS, *sS = sT + (RH + 6) * SS;
+  const float *planes = p.t.planes;
+  if (SRCK == 1) {
+    const akz_level_desc Lp = p.t.lv[level_desc - 1];
+    const float *pp = planes + Lp.lt + (long long)(2 * (oy - 3)) * Lp.pitch + 2 * (ox - 3);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int ly = warp + 16 * k;
+      if (ly < RH + 6) {
+        const float *q0 = pp + (long long)(2 * ly) * Lp.pitch, *q1 = q0 + Lp.pitch;
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+          const int l = lane + 32 * j;
+          if (l < PS) {
+            const float2 a = __ldg((const float2 *)(q0 + 2 * l)), b = __ldg((const float2 *)(q1 + 2 * l));
+            sP[ly * PS + l] = 0.25f * (((a.x + a.y) + b.x) + b.y);
+          }
+        }
+      }
+    }
+  } else {
+    const float *pp;
+    long long pitch;
+    if (SRCK == 0) {
+      const akz_level_desc Lp = p.t.lv[level_desc - 1];
+      pp = planes + Lp.lt;
+      pitch = Lp.pitch;
+    } else {
+      pp = planes + I.t2;
+      pitch = L.pitch;
+    }
+    pp += (long long)(oy - 3) * pitch + (ox - 3);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int ly = warp + 16 * k;
+      if (ly < RH + 6) {
+        const float *q = pp + (long long)ly * pitch;
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+          const int l = lane + 32 * j;
+          if (l < PS) sP[ly * PS + l] = __ldg(q + l);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int ly = warp + 16 * k;
+    if (ly < RH + 6) {
+      const float *r = sP + ly * PS;
+#pragma unroll
+      for (int j = 0; j < 5; j++) {
+        const int m = lane + 32 * j;
+        if (m < SS) {
+          float acc = k0 * (r[m] + r[m + 4]);
+          acc = acc + k1 * (r[m + 1] + r[m + 3]);
+          acc = acc + k2 * r[m + 2];
+          sT[ly * SS + m] = acc;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  float *lsp = p.t.planes + L.ls + (long long)(oy - 1) * L.pitch + (ox - 1);
+  const int d = tx0 - ox;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int n = warp + 16 * k;
+    if (n < RH + 2) {
+      const float *c = sT + n * SS;
+      const bool yt = n >= d + 1 && n < d + 1 + (ty1 - ty0);
+#pragma unroll
+      for (int j = 0; j < 5; j++) {
+        const int m = lane + 32 * j;
+        if (m < SS) {
+          float acc = k0 * (c[m] + c[m + 4 * SS]);
+          acc = acc + k1 * (c[m + SS] + c[m + 3 * SS]);
+          acc = acc + k2 * c[m + 2 * SS];
+          sS[n * SS + m] = acc;
+          if (yt && m >= d + 1 && m < d + 1 + (tx1 - tx0)) lsp[(long long)n * L.pitch + m] = acc;
+        }
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < RB; r++) Lr[r] = sP[(ly0 + r + 3) * PS + lx + 3];
+  __syncthreads();
+  float *sG = sP;
+  const float inv_k = p.kc[L.image * 16 + L.octave].y;
+  float *gp = p.t.planes + I.g + (long long)oy * L.pitch + ox;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int ly = warp + 16 * k;
+    if (ly < RH) {
+      const float *rm = sS + ly * SS, *r0 = rm + SS, *rp = r0 + SS;
+      const bool yt = p.write_g && ly >= d && ly < d + (ty1 - ty0);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int l = lane + 32 * j;
+        const float hm = rm[l + 2] - rm[l];
+        const float h0 = r0[l + 2] - r0[l];
+        const float hp = rp[l + 2] - rp[l];
+        const float gx = 3.0f * (hm + hp) + 10.0f * h0;
+        const float syp = 3.0f * (rp[l] + rp[l + 2]) + 10.0f * rp[l + 1];
+        const float sym = 3.0f * (rm[l] + rm[l + 2]) + 10.0f * rm[l + 1];
+        const float gy = syp - sym;
+        const float gv = akz_conductance(gx, gy, inv_k, p.diffusivity);
+        sG[ly * RW + l] = gv;
+        if (yt && l >= d && l < d + (tx1 - tx0)) gp[(long long)ly * L.pitch + l] = gv;
+      }
+    }
+  }
+  __syncthreads();
+  const int lxe = min(lx + 1, RW - 1), lxw = max(lx - 1, 0);
+#pragma unroll
+  for (int r = 0; r < RB; r++) {
+    const int ly = ly0 + r;
+    const float gc = sG[ly * RW + lx];
+    gE[r] = gc + sG[ly * RW + lxe];
+    gW[r] = sG[ly * RW + lxw] + gc;
+    gS[r] = gc + sG[min(ly + 1, RH - 1) * RW + lx];
+  }
+  gN0 = sG[max(ly0 - 1, 0) * RW + lx] + sG[ly0 * RW + lx];
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
 {
   extern __shared__ float sm[];
@@ -285,7 +427,17 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   float gN0;
   float *cur, *nxt;
 
-  if (p.first) {
+  const bool interior = ox >= 3 && oy >= 3 && ox + RW + 3 <= W && oy + RH + 3 <= H;
+  if (p.first && interior) {
+    if (srck == 1)
+      akz_fed_prologue_interior<1>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx, ly0, Lr, gE, gW, gS, gN0);
+    else if (srck == 0)
+      akz_fed_prologue_interior<0>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx, ly0, Lr, gE, gW, gS, gN0);
+    else
+      akz_fed_prologue_interior<2>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx, ly0, Lr, gE, gW, gS, gN0);
+    cur = sm + (RH + 6) * PS;                 /* row-pass buffer */
+    nxt = cur + (RH + 6) * SS;                /* smoothing buffer */
+  } else if (p.first) {
     float *sP = sm, *sT = sm + (RH + 6) * PS, *sS = sT + (RH + 6) * SS;
     const int px0 = max(ox - 3, 0), px1 = min(ox + RW + 3, W), py0 = max(oy - 3, 0), py1 = min(oy + RH + 3, H);
     const int sx0 = max(ox - 1, 0), sx1 = min(ox + RW + 1, W), sy0 = max(oy - 1, 0), sy1 = min(oy + RH + 1, H);

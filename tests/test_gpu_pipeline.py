@@ -70,3 +70,36 @@ def test_pair_matches(gpu_lib, oracle):
     m = gpu_lib.Matcher().bfmatch(da, db)
     om = oracle.bfmatch(oda, odb)
     assert _exact(m.reshape(-1), om.reshape(-1))
+
+
+def test_float_input_equals_u8_over_255(gpu_lib, oracle):
+    img = synth.synth_image(31, 320, 240)
+    f = oracle.u8_to_unit(img)  # (float)u * (float)(1/255), as the demos' convertTo
+    res = []
+    for im in (img, f):
+        o = gpu_lib.AKAZEOptions()
+        o.setWidth(320)
+        o.setHeight(240)
+        ak = gpu_lib.AKAZE(o)
+        ak.Create_Nonlinear_Scale_Space(im)
+        ak.Feature_Detection()
+        res.append(ak.Compute_Descriptors())
+    assert np.array_equal(res[0][0], res[1][0])
+    assert np.array_equal(res[0][1].view(np.uint8), res[1][1].view(np.uint8))
+
+
+def test_uneven_batch_equals_single_images(gpu_lib, oracle):
+    sizes = synth.uneven_sizes(5, 6)
+    imgs = [synth.synth_image(700 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    b = gpu_lib.Batch(gpu_lib.AKAZEOptions(), sizes)
+    b.upload(imgs)
+    b.run()
+    counts = b.counts()
+    b.run()  # graph replay gives the same results
+    assert np.array_equal(counts, b.counts())
+    for i, ((w, h), img) in enumerate(zip(sizes, imgs)):
+        kp, d = b.results(i)
+        orc = oracle.Oracle(w, h)
+        okp, od = orc.run(img)
+        assert _exact(kp, okp), (i, w, h)
+        assert np.array_equal(d, od), (i, w, h)
