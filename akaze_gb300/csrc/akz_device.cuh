@@ -89,6 +89,37 @@ __device__ __forceinline__ float akz_det_at(const A &lx, const A &ly, int W, int
   return lxx * lyy - lyx * lyx;
 }
 
+/* Packed FP32x2 additions (sm_100+ add/sub .f32x2): two independent IEEE
+ * float additions per instruction, each rounded exactly like the scalar one.
+ * There is deliberately no packed multiply: the assembler of CUDA 13.0
+ * contracts a packed multiply (mul.rn.f32x2, or fma.rn.f32x2 with a -0
+ * addend) feeding a packed add into a packed fused multiply-add despite the
+ * .rn modifier and -fmad=false (measured on sm_103a: 9-14% of random operands
+ * differ from the scalar result), while scalar products feeding a packed add
+ * are kept as written (0 of 2^20 differ). */
+__device__ __forceinline__ unsigned long long akz_f2u(float2 v)
+{
+  return ((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x);
+}
+__device__ __forceinline__ float2 akz_u2f(unsigned long long u)
+{
+  return make_float2(__uint_as_float((unsigned int)u), __uint_as_float((unsigned int)(u >> 32)));
+}
+__device__ __forceinline__ float2 f2add(float2 a, float2 b)
+{
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(akz_f2u(a)), "l"(akz_f2u(b)));
+  return akz_u2f(r);
+}
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b)
+{
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(akz_f2u(a)), "l"(akz_f2u(b)));
+  return akz_u2f(r);
+}
+__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ void st2(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
+
 struct akz_plane_acc {
   const float *p;
   int pitch;

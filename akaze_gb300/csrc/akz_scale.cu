@@ -206,38 +206,25 @@ __global__ void __launch_bounds__(256) k_gauss0(akz_gauss_params p)
 /* ------------------------------------------------------------------------ */
 /* Level i >= 1: Lsmooth, conductance and a chunk of FED steps per tile.     */
 
-__device__ __forceinline__ float akz_conductance(float lx, float ly, float inv_k, int type)
-{
-  const float m = lx * lx + ly * ly;
-  if (type == 1) return akz_recip1pf(inv_k * m);
-  if (type == 0) return akz_expf(-inv_k * m);
-  if (type == 2) {
-    const float dL = inv_k * m;
-    const float t = (float)(-3.315 / (double)(dL * dL * dL * dL));
-    return (float)(1.0 - (double)akz_expf(t));
-  }
-  const float den = (float)sqrt(1.0 + (double)(inv_k * m));
-  return (float)(1.0 / (double)den);
-}
-
 /* FED level kernel.
  *
  * Every CTA owns a fixed 128 x 40 region R0 = tile +- d (d = FED steps of the
  * launch, tile (128-2d) x (40-2d)), so one thread geometry serves every
- * chunk size: 512 threads, 4 column groups of 32 lanes x 4 bands of 10 rows;
- * each thread keeps the 10 level values of its column in registers together
- * with the conductance pair sums (c_x + c_x+1), (c_x-1 + c_x), (c_y + c_y+1)
- * of the reference's flux terms, which do not change across steps.  A step
- * reads the east/west neighbours (and the band's outer rows) from a
- * double-buffered shared plane: 3 shared-memory operations and 13 FP32
- * operations per pixel-step, one barrier per step.  Pixels outside
+ * chunk size: 512 threads, 2 column groups of 32 lanes x 2 columns, 8 bands
+ * of 5 rows; each thread keeps the level values of its two columns in
+ * registers together with the conductance pair sums (c_x + c_x+1) and
+ * (c_y + c_y+1) of the reference's flux terms, which do not change across
+ * steps.  A step reads the outer east/west neighbours (and the band's outer
+ * rows) from a double-buffered shared plane and writes its two values with
+ * one 64-bit store: 1.5 shared-memory operations, 3 products and 3.5 packed
+ * FP32x2 additions per pixel-step, one barrier per step.  Pixels outside
  * tile +- (d - s) after step s are not needed and may hold anything; image
  * borders are replicate (clamped) neighbours, whose flux is exactly zero, as
  * in the reference's border formulas (nldiffusion_functions.cpp:241-307).
  */
 #define AKZ_FED_RW 128
 #define AKZ_FED_RH 40
-#define AKZ_FED_RB 10
+#define AKZ_FED_RB 5
 #define AKZ_FED_THREADS 512
 
 size_t akz_fed_smem_bytes(int, int, int, int first)
@@ -249,146 +236,236 @@ size_t akz_fed_smem_bytes(int, int, int, int first)
   return (P + T + S) * sizeof(float);
 }
 
-/* First-chunk prologue of k_fed for a tile whose input region (R0 +- 3)
- * lies inside the image: every region has its full compile-time size and no
- * neighbour needs clamping or reflecting, so the loops are straight-line.
- * Same arithmetic, in the same order, as the general path in k_fed. */
-template <int SRCK>
-__device__ __forceinline__ void akz_fed_prologue_interior(const akz_fed_params &p, const akz_level_desc &L,
-                                                          const akz_image_desc &I, int level_desc, float *sm, int ox,
-                                                          int oy, int tx0, int ty0, int tx1, int ty1, int lx, int ly0,
-                                                          float *Lr, float *gE, float *gW, float *gS, float &gN0)
+/* Conductance of |grad|^2 = m (AKAZE.cpp:259-268 with pm_g1, pm_g2,
+ * weickert_diffusivity, charbonnier_diffusivity, nldiffusion_functions.cpp:58-118). */
+__device__ __forceinline__ float akz_conductance_m(float m, float inv_k, int type)
 {
-  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
-  constexpr int PS = RW + 6, SS = RW + 2;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float *sP = sm, *sT = sm + (RH + 6) * PS, *sS = sT + (RH + 6) * SS;
+  if (type == 1) return akz_recip1pf(inv_k * m);
+  if (type == 0) return akz_expf(-inv_k * m);
+  if (type == 2) {
+    const float dL = inv_k * m;
+    const float t = (float)(-3.315 / (double)(dL * dL * dL * dL));
+    return (float)(1.0 - (double)akz_expf(t));
+  }
+  const float den = (float)sqrt(1.0 + (double)(inv_k * m));
+  return (float)(1.0 / (double)den);
+}
+
+/* First-chunk prologue of k_fed: the level's starting image on R0 +- 3, its
+ * sigma-1 smoothing Lsmooth (written to HBM for the tile) and the conductance
+ * on R0 (written to HBM for the tile when more chunks follow).
+ *
+ * Every tile runs the same straight-line code.  The input region is read
+ * with replicate (clamped) coordinates, which makes the Gaussian's replicate
+ * border (gaussian_2D_convolution, nldiffusion_functions.cpp:29-47) exact for
+ * every pixel inside the image; Lsmooth's row and column just outside the
+ * image are then replaced by their reflect-101 mirrors (x = -1 by x = 1,
+ * x = W by x = W - 2), the border of the Scharr gradient
+ * (nldiffusion_functions.cpp:50-53).  Values outside the image are finite
+ * and unused: their conductance pair sums are zero.
+ *
+ * Leaves the level values of R0 in sT (RW x RH) and the conductance in sP
+ * (RW x RH).  Filter passes work on column pairs with packed FP32x2 additions
+ * and scalar products, in the reference's operation order:
+ *   Gaussian  k0*(v[-2] + v[+2]) + k1*(v[-1] + v[+1]) + k2*v[0], rows then columns;
+ *   Scharr    gx = 3*(d[y-1] + d[y+1]) + 10*d[y],  d = v[x+1] - v[x-1],
+ *             gy = s[y+1] - s[y-1],  s = 3*(v[x-1] + v[x+1]) + 10*v[x]. */
+template <int SRCK>
+__device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const akz_level_desc &L,
+                                                 const akz_image_desc &I, int level_desc, float *sm, int ox, int oy,
+                                                 int tx0, int ty0, int tx1, int ty1, int lx0, int ly0)
+{
+  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB, NT = AKZ_FED_THREADS;
+  constexpr int PS = RW + 6, SS = RW + 2, PH = RH + 6, SH = RH + 2;
+  constexpr int NP = SS / 2;          /* column pairs of the smoothing regions */
+  constexpr int VR = 6, VG = SH / VR; /* rows per thread and row groups of the vertical pass */
+  static_assert(SH % VR == 0 && NP * VG <= NT && (RW * RH) % NT == 0, "k_fed prologue geometry");
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int W = L.width, H = L.height;
+  float *sP = sm, *sT = sm + PH * PS, *sS = sT + PH * SS;
   const float *planes = p.t.planes;
-  if (SRCK == 1) {
-    const akz_level_desc Lp = p.t.lv[level_desc - 1];
-    const float *pp = planes + Lp.lt + (long long)(2 * (oy - 3)) * Lp.pitch + 2 * (ox - 3);
+
+  /* 1. starting image on R0 +- 3: predecessor copy, its exact 2x
+   *    half-sample, or the INTER_AREA plane prepared in T2 */
+  {
+    const float *pp;
+    long long pitch;
+    if (SRCK == 2) {
+      pp = planes + I.t2;
+      pitch = L.pitch;
+    } else {
+      const akz_level_desc Lp = p.t.lv[level_desc - 1];
+      pp = planes + Lp.lt;
+      pitch = Lp.pitch;
+    }
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < (PH + 15) / 16; k++) {
       const int ly = warp + 16 * k;
-      if (ly < RH + 6) {
-        const float *q0 = pp + (long long)(2 * ly) * Lp.pitch, *q1 = q0 + Lp.pitch;
+      if (ly < PH) {
+        const int y = akz_clampi(oy - 3 + ly, 0, H - 1);
+        const float *q0 = pp + (long long)(SRCK == 1 ? 2 * y : y) * pitch;
 #pragma unroll
-        for (int j = 0; j < 5; j++) {
+        for (int j = 0; j < (PS + 31) / 32; j++) {
           const int l = lane + 32 * j;
           if (l < PS) {
-            const float2 a = __ldg((const float2 *)(q0 + 2 * l)), b = __ldg((const float2 *)(q1 + 2 * l));
-            sP[ly * PS + l] = 0.25f * (((a.x + a.y) + b.x) + b.y);
+            const int x = akz_clampi(ox - 3 + l, 0, W - 1);
+            float v;
+            if (SRCK == 1) {
+              const float2 a = __ldg((const float2 *)(q0 + 2 * x)), b = __ldg((const float2 *)(q0 + pitch + 2 * x));
+              v = 0.25f * (((a.x + a.y) + b.x) + b.y);
+            } else {
+              v = __ldg(q0 + x);
+            }
+            sP[ly * PS + l] = v;
           }
         }
       }
     }
-  } else {
-    const float *pp;
-    long long pitch;
-    if (SRCK == 0) {
-      const akz_level_desc Lp = p.t.lv[level_desc - 1];
-      pp = planes + Lp.lt;
-      pitch = Lp.pitch;
-    } else {
-      pp = planes + I.t2;
-      pitch = L.pitch;
-    }
-    pp += (long long)(oy - 3) * pitch + (ox - 3);
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      const int ly = warp + 16 * k;
-      if (ly < RH + 6) {
-        const float *q = pp + (long long)ly * pitch;
-#pragma unroll
-        for (int j = 0; j < 5; j++) {
-          const int l = lane + 32 * j;
-          if (l < PS) sP[ly * PS + l] = __ldg(q + l);
-        }
-      }
-    }
   }
   __syncthreads();
+
+  /* 2. rows of the Gaussian on columns R0 +- 1 (sT column c is x = ox - 1 + c) */
   const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
 #pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const int ly = warp + 16 * k;
-    if (ly < RH + 6) {
-      const float *r = sP + ly * PS;
+  for (int k = 0; k < (PH * NP + NT - 1) / NT; k++) {
+    const int i = tid + NT * k;
+    if (i < PH * NP) {
+      const int row = i / NP, c = 2 * (i - row * NP);
+      const float *r = sP + row * PS + c;
+      const float2 A = ld2(r), B = ld2(r + 2), C = ld2(r + 4);
+      const float2 s04 = f2add(A, C);
+      const float2 s13 = f2add(make_float2(A.y, B.x), make_float2(B.y, C.x));
+      float2 acc = make_float2(k0 * s04.x, k0 * s04.y);
+      acc = f2add(acc, make_float2(k1 * s13.x, k1 * s13.y));
+      acc = f2add(acc, make_float2(k2 * B.x, k2 * B.y));
+      st2(sT + row * SS + c, acc);
+    }
+  }
+  __syncthreads();
+
+  /* 3. columns of the Gaussian: Lsmooth on R0 +- 1 (sS row n is y = oy - 1 + n) */
+  if (tid < NP * VG) {
+    const int g = tid / NP, c = 2 * (tid - g * NP);
+    const float *col = sT + (g * VR) * SS + c;
+    float2 v[VR + 4];
 #pragma unroll
-      for (int j = 0; j < 5; j++) {
-        const int m = lane + 32 * j;
-        if (m < SS) {
-          float acc = k0 * (r[m] + r[m + 4]);
-          acc = acc + k1 * (r[m + 1] + r[m + 3]);
-          acc = acc + k2 * r[m + 2];
-          sT[ly * SS + m] = acc;
-        }
+    for (int j = 0; j < VR + 4; j++) v[j] = ld2(col + j * SS);
+    const int x = ox - 1 + c;
+    const bool w0 = x >= tx0 && x < tx1, w1 = x + 1 >= tx0 && x + 1 < tx1;
+    float *lsp = p.t.planes + L.ls + x;
+#pragma unroll
+    for (int j = 0; j < VR; j++) {
+      const float2 s04 = f2add(v[j], v[j + 4]);
+      const float2 s13 = f2add(v[j + 1], v[j + 3]);
+      float2 acc = make_float2(k0 * s04.x, k0 * s04.y);
+      acc = f2add(acc, make_float2(k1 * s13.x, k1 * s13.y));
+      acc = f2add(acc, make_float2(k2 * v[j + 2].x, k2 * v[j + 2].y));
+      const int n = g * VR + j;
+      st2(sS + n * SS + c, acc);
+      const int y = oy - 1 + n;
+      if (y >= ty0 && y < ty1) {
+        float *o = lsp + (long long)y * L.pitch;
+        if (w0) o[0] = acc.x;
+        if (w1) o[1] = acc.y;
       }
     }
   }
   __syncthreads();
-  float *lsp = p.t.planes + L.ls + (long long)(oy - 1) * L.pitch + (ox - 1);
-  const int d = tx0 - ox;
+
+  /* 4. level values of R0 into sT (free now), and the reflect-101 border
+   *    of Lsmooth: columns first, then whole rows (which fixes the corners) */
 #pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const int n = warp + 16 * k;
-    if (n < RH + 2) {
-      const float *c = sT + n * SS;
-      const bool yt = n >= d + 1 && n < d + 1 + (ty1 - ty0);
-#pragma unroll
-      for (int j = 0; j < 5; j++) {
-        const int m = lane + 32 * j;
-        if (m < SS) {
-          float acc = k0 * (c[m] + c[m + 4 * SS]);
-          acc = acc + k1 * (c[m + SS] + c[m + 3 * SS]);
-          acc = acc + k2 * c[m + 2 * SS];
-          sS[n * SS + m] = acc;
-          if (yt && m >= d + 1 && m < d + 1 + (tx1 - tx0)) lsp[(long long)n * L.pitch + m] = acc;
-        }
-      }
+  for (int k = 0; k < RW * RH / NT; k++) {
+    const int i = tid + NT * k;
+    sT[i] = sP[(i / RW + 3) * PS + i % RW + 3];
+  }
+  const int cm = -ox, cp = W - ox + 1; /* sS columns of x = -1 and x = W */
+  const int nm = -oy, np = H - oy + 1; /* sS rows of y = -1 and y = H */
+  if (cm >= 0 || cp < SS) {
+    if (tid < SH) {
+      float *row = sS + tid * SS;
+      if (cm >= 0) row[cm] = row[cm + 2];
+      if (cp < SS) row[cp] = row[cp - 2];
     }
   }
   __syncthreads();
-#pragma unroll
-  for (int r = 0; r < RB; r++) Lr[r] = sP[(ly0 + r + 3) * PS + lx + 3];
-  __syncthreads();
+  if (nm >= 0 || np < SH) {
+    if (tid < SS) {
+      if (nm >= 0) sS[nm * SS + tid] = sS[(nm + 2) * SS + tid];
+      if (np < SH) sS[np * SS + tid] = sS[(np - 2) * SS + tid];
+    }
+    __syncthreads();
+  }
+
+  /* 5. Scharr gradient of Lsmooth and the conductance on R0, in this
+   *    thread's k_fed geometry: columns lx0, lx0+1, rows ly0 .. ly0+RB-1 */
   float *sG = sP;
   const float inv_k = p.kc[L.image * 16 + L.octave].y;
-  float *gp = p.t.planes + I.g + (long long)oy * L.pitch + ox;
+  float2 dh[RB + 2], sh[RB + 2];
 #pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const int ly = warp + 16 * k;
-    if (ly < RH) {
-      const float *rm = sS + ly * SS, *r0 = rm + SS, *rp = r0 + SS;
-      const bool yt = p.write_g && ly >= d && ly < d + (ty1 - ty0);
+  for (int j = 0; j < RB + 2; j++) {
+    const float *row = sS + (ly0 + j) * SS + lx0; /* x0 - 1 .. x0 + 2 */
+    const float2 P = ld2(row), Q = ld2(row + 2);
+    dh[j] = f2sub(Q, P);
+    const float2 t = f2add(P, Q);
+    sh[j] = f2add(make_float2(3.0f * t.x, 3.0f * t.y), make_float2(10.0f * P.y, 10.0f * Q.x));
+  }
+  const int x0 = ox + lx0;
+  const bool w0 = p.write_g && x0 >= tx0 && x0 < tx1, w1 = p.write_g && x0 + 1 >= tx0 && x0 + 1 < tx1;
+  float *gp = p.t.planes + I.g + x0;
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int l = lane + 32 * j;
-        const float hm = rm[l + 2] - rm[l];
-        const float h0 = r0[l + 2] - r0[l];
-        const float hp = rp[l + 2] - rp[l];
-        const float gx = 3.0f * (hm + hp) + 10.0f * h0;
-        const float syp = 3.0f * (rp[l] + rp[l + 2]) + 10.0f * rp[l + 1];
-        const float sym = 3.0f * (rm[l] + rm[l + 2]) + 10.0f * rm[l + 1];
-        const float gy = syp - sym;
-        const float gv = akz_conductance(gx, gy, inv_k, p.diffusivity);
-        sG[ly * RW + l] = gv;
-        if (yt && l >= d && l < d + (tx1 - tx0)) gp[(long long)ly * L.pitch + l] = gv;
-      }
+  for (int r = 0; r < RB; r++) {
+    const float2 u = f2add(dh[r], dh[r + 2]);
+    const float2 gx = f2add(make_float2(3.0f * u.x, 3.0f * u.y), make_float2(10.0f * dh[r + 1].x, 10.0f * dh[r + 1].y));
+    const float2 gy = f2sub(sh[r + 2], sh[r]);
+    const float2 m = f2add(make_float2(gx.x * gx.x, gx.y * gx.y), make_float2(gy.x * gy.x, gy.y * gy.y));
+    const float2 gv = make_float2(akz_conductance_m(m.x, inv_k, p.diffusivity), akz_conductance_m(m.y, inv_k, p.diffusivity));
+    st2(sG + (ly0 + r) * RW + lx0, gv);
+    const int y = oy + ly0 + r;
+    if (y >= ty0 && y < ty1) {
+      float *o = gp + (long long)y * L.pitch;
+      if (w0) o[0] = gv.x;
+      if (w1) o[1] = gv.y;
     }
   }
   __syncthreads();
-  const int lxe = min(lx + 1, RW - 1), lxw = max(lx - 1, 0);
+}
+
+/* Registers of one k_fed thread (columns x0, x0+1 of R0, RB rows) from the
+ * level values and the conductance on R0 in shared memory:
+ *   Lp[r]   the two level values;
+ *   gw[r]   c(x0-1) + c(x0)   the west flux pair of column x0;
+ *   gm[r]   c(x0) + c(x0+1)   the flux pair between the two columns;
+ *   ge[r]   c(x0+1) + c(x0+2) the east flux pair of column x0+1;
+ *   gs[r]   c(x, y) + c(x, y+1) of both columns; gn0 the pair above row 0.
+ * A pair that crosses the image border is zero: the reference omits that
+ * flux term (nldiffusion_functions.cpp:241-307), and zero times any finite
+ * difference adds nothing. */
+__device__ __forceinline__ void akz_fed_gather_smem(const float *sL, const float *sG, int lx0, int ly0, int x0, int ytop,
+                                                    int W, int H, float2 *Lp, float *gw, float *gm, float *ge,
+                                                    float2 *gs, float2 &gn0)
+{
+  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
+  const bool x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
+  const int lxw = max(lx0 - 1, 0), lxe = min(lx0 + 2, RW - 1);
 #pragma unroll
   for (int r = 0; r < RB; r++) {
-    const int ly = ly0 + r;
-    const float gc = sG[ly * RW + lx];
-    gE[r] = gc + sG[ly * RW + lxe];
-    gW[r] = sG[ly * RW + lxw] + gc;
-    gS[r] = gc + sG[min(ly + 1, RH - 1) * RW + lx];
+    const int ly = ly0 + r, y = ytop + r;
+    const bool yin = y >= 0 && y < H;
+    Lp[r] = ld2(sL + ly * RW + lx0);
+    const float2 c = ld2(sG + ly * RW + lx0);
+    const float2 cs = ld2(sG + min(ly + 1, RH - 1) * RW + lx0);
+    const float cw = sG[ly * RW + lxw], ce = sG[ly * RW + lxe];
+    gw[r] = (yin && x0in && x0 >= 1) ? cw + c.x : 0.0f;
+    gm[r] = (yin && x0 >= 0 && x0 + 1 < W) ? c.x + c.y : 0.0f;
+    ge[r] = (yin && x1in && x0 + 2 < W) ? c.y + ce : 0.0f;
+    gs[r].x = (x0in && y >= 0 && y + 1 < H) ? c.x + cs.x : 0.0f;
+    gs[r].y = (x1in && y >= 0 && y + 1 < H) ? c.y + cs.y : 0.0f;
   }
-  gN0 = sG[max(ly0 - 1, 0) * RW + lx] + sG[ly0 * RW + lx];
-  __syncthreads();
+  const float2 cn = ld2(sG + max(ly0 - 1, 0) * RW + lx0), c0 = ld2(sG + ly0 * RW + lx0);
+  const bool nin = ytop >= 1 && ytop < H;
+  gn0.x = (x0in && nin) ? cn.x + c0.x : 0.0f;
+  gn0.y = (x1in && nin) ? cn.y + c0.y : 0.0f;
 }
 
 __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
@@ -411,194 +488,96 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   const int srck = p.first ? sg.aux : p.src;
   float *planes = p.t.planes;
 
-  /* this thread: column lx of R0, rows ly0 .. ly0+RB-1 */
-  const int lx = (warp & 3) * 32 + lane;
-  const int ly0 = (warp >> 2) * RB;
-  const int x = ox + lx;
-  const bool xin = x >= 0 && x < W;
+  /* this thread: columns lx0, lx0+1 of R0, rows ly0 .. ly0+RB-1 */
+  const int lx0 = 2 * ((warp & 1) * 32 + lane);
+  const int ly0 = (warp >> 1) * RB;
+  const int x0 = ox + lx0;
   const int ytop = oy + ly0;
-  const int lxe = min(lx + 1, RW - 1), lxw = max(lx - 1, 0);
 
-  /* level values and the conductance pair sums of the reference's flux terms:
-   *   xpos uses (c_x + c_x+1), xneg (c_x-1 + c_x), ypos (c_y + c_y+1), yneg (c_y-1 + c_y).
-   * A pair that crosses the image border is zero: its flux is exactly zero
-   * there (the reference omits the term), whatever the neighbour value is. */
-  float Lr[RB], gE[RB], gW[RB], gS[RB];
-  float gN0;
+  float2 Lp[RB], gs[RB], gn0;
+  float gw[RB], gm[RB], ge[RB];
   float *cur, *nxt;
 
-  const bool interior = ox >= 3 && oy >= 3 && ox + RW + 3 <= W && oy + RH + 3 <= H;
-  if (p.first && interior) {
-    if (srck == 1)
-      akz_fed_prologue_interior<1>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx, ly0, Lr, gE, gW, gS, gN0);
-    else if (srck == 0)
-      akz_fed_prologue_interior<0>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx, ly0, Lr, gE, gW, gS, gN0);
-    else
-      akz_fed_prologue_interior<2>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx, ly0, Lr, gE, gW, gS, gN0);
-    cur = sm + (RH + 6) * PS;                 /* row-pass buffer */
-    nxt = cur + (RH + 6) * SS;                /* smoothing buffer */
-  } else if (p.first) {
+  if (p.first) {
     float *sP = sm, *sT = sm + (RH + 6) * PS, *sS = sT + (RH + 6) * SS;
-    const int px0 = max(ox - 3, 0), px1 = min(ox + RW + 3, W), py0 = max(oy - 3, 0), py1 = min(oy + RH + 3, H);
-    const int sx0 = max(ox - 1, 0), sx1 = min(ox + RW + 1, W), sy0 = max(oy - 1, 0), sy1 = min(oy + RH + 1, H);
-    /* input region: predecessor copy, its exact 2x half-sample, or a prepared plane */
-    if (srck == 1) {
-      const akz_level_desc Lp = p.t.lv[sg.level_desc - 1];
-      const float *pp = planes + Lp.lt;
-      for (int y = py0 + warp; y < py1; y += 16) {
-        const float *q0 = pp + (long long)(2 * y) * Lp.pitch;
-        const float *q1 = q0 + Lp.pitch;
-        float *o = sP + (y - oy + 3) * PS - ox + 3;
-        for (int xx = px0 + lane; xx < px1; xx += 32) {
-          const float2 a = __ldg((const float2 *)(q0 + 2 * xx)), b = __ldg((const float2 *)(q1 + 2 * xx));
-          o[xx] = 0.25f * (((a.x + a.y) + b.x) + b.y);
-        }
-      }
-    } else {
-      const float *pp;
-      long long pitch;
-      if (srck == 0) {
-        const akz_level_desc Lp = p.t.lv[sg.level_desc - 1];
-        pp = planes + Lp.lt;
-        pitch = Lp.pitch;
-      } else {
-        pp = planes + I.t2;
-        pitch = L.pitch;
-      }
-      for (int y = py0 + warp; y < py1; y += 16) {
-        const float *q = pp + (long long)y * pitch;
-        float *o = sP + (y - oy + 3) * PS - ox + 3;
-        for (int xx = px0 + lane; xx < px1; xx += 32) o[xx] = __ldg(q + xx);
-      }
-    }
-    __syncthreads();
-    /* sigma-1 Gaussian, horizontal then vertical, replicate border */
-    const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
-    for (int y = py0 + warp; y < py1; y += 16) {
-      const float *r = sP + (y - oy + 3) * PS - ox + 3;
-      float *o = sT + (y - oy + 3) * SS - ox + 1;
-      for (int xx = sx0 + lane; xx < sx1; xx += 32) {
-        float acc = k0 * (r[max(xx - 2, 0)] + r[min(xx + 2, W - 1)]);
-        acc = acc + k1 * (r[max(xx - 1, 0)] + r[min(xx + 1, W - 1)]);
-        acc = acc + k2 * r[xx];
-        o[xx] = acc;
-      }
-    }
-    __syncthreads();
-    float *lsp = planes + L.ls;
-    for (int y = sy0 + warp; y < sy1; y += 16) {
-      const float *c2m = sT + (max(y - 2, 0) - oy + 3) * SS - ox + 1, *c2p = sT + (min(y + 2, H - 1) - oy + 3) * SS - ox + 1;
-      const float *c1m = sT + (max(y - 1, 0) - oy + 3) * SS - ox + 1, *c1p = sT + (min(y + 1, H - 1) - oy + 3) * SS - ox + 1;
-      const float *c0 = sT + (y - oy + 3) * SS - ox + 1;
-      float *o = sS + (y - oy + 1) * SS - ox + 1;
-      const bool yt = y >= ty0 && y < ty1;
-      float *lo = lsp + (long long)y * L.pitch;
-      for (int xx = sx0 + lane; xx < sx1; xx += 32) {
-        float acc = k0 * (c2m[xx] + c2p[xx]);
-        acc = acc + k1 * (c1m[xx] + c1p[xx]);
-        acc = acc + k2 * c0[xx];
-        o[xx] = acc;
-        if (yt && xx >= tx0 && xx < tx1) lo[xx] = acc;
-      }
-    }
-    __syncthreads();
-    /* conductance on R0 from the Scharr gradient of Lsmooth (reflect-101) */
-    float *sG = sP; /* the input region is not read any more except for L0 below */
-    const float inv_k = p.kc[L.image * 16 + L.octave].y;
-    float *gp = planes + I.g;
-    /* L0 of this thread's pixels before sG overwrites the input region */
-    for (int r = 0; r < RB; r++) {
-      const int y = ytop + r;
-      Lr[r] = (xin && y >= 0 && y < H) ? sP[(ly0 + r + 3) * PS + lx + 3] : 0.0f;
-    }
-    __syncthreads();
-    for (int ly = warp; ly < RH; ly += 16) {
-      const int y = oy + ly;
-      const bool yin = y >= 0 && y < H;
-      const int ym = y > 0 ? y - 1 : 1, yp = y < H - 1 ? y + 1 : H - 2;
-      const float *rm = sS + (ym - oy + 1) * SS - ox + 1, *r0 = sS + (y - oy + 1) * SS - ox + 1;
-      const float *rp = sS + (yp - oy + 1) * SS - ox + 1;
-      const bool yt = y >= ty0 && y < ty1 && p.write_g;
-      for (int l = lane; l < RW; l += 32) {
-        const int xx = ox + l;
-        float gv = 0.0f;
-        if (yin && xx >= 0 && xx < W) {
-          const int xm = xx > 0 ? xx - 1 : 1, xp = xx < W - 1 ? xx + 1 : W - 2;
-          const float hm = rm[xp] - rm[xm];
-          const float h0 = r0[xp] - r0[xm];
-          const float hp = rp[xp] - rp[xm];
-          const float gx = 3.0f * (hm + hp) + 10.0f * h0;
-          const float syp = 3.0f * (rp[xm] + rp[xp]) + 10.0f * rp[xx];
-          const float sym = 3.0f * (rm[xm] + rm[xp]) + 10.0f * rm[xx];
-          const float gy = syp - sym;
-          gv = akz_conductance(gx, gy, inv_k, p.diffusivity);
-          if (yt && xx >= tx0 && xx < tx1) gp[(long long)y * L.pitch + xx] = gv;
-        }
-        sG[ly * RW + l] = gv;
-      }
-    }
-    __syncthreads();
-    const bool xe_in = xin && x + 1 < W, xw_in = xin && x >= 1;
-    for (int r = 0; r < RB; r++) {
-      const int ly = ly0 + r, y = ytop + r;
-      const float gc = sG[ly * RW + lx];
-      const bool yin = y >= 0 && y < H;
-      gE[r] = (yin && xe_in) ? gc + sG[ly * RW + lxe] : 0.0f;
-      gW[r] = (yin && xw_in) ? sG[ly * RW + lxw] + gc : 0.0f;
-      gS[r] = (xin && y >= 0 && y + 1 < H) ? gc + sG[min(ly + 1, RH - 1) * RW + lx] : 0.0f;
-    }
-    gN0 = (xin && ytop >= 1 && ytop < H) ? sG[max(ly0 - 1, 0) * RW + lx] + sG[ly0 * RW + lx] : 0.0f;
-    cur = sT; /* the row-pass buffer is free now and larger than R0 */
-    nxt = sS; /* so is the smoothing buffer, once the conductance is done */
-    __syncthreads();
+    if (srck == 1)
+      akz_fed_prologue<1>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
+    else if (srck == 0)
+      akz_fed_prologue<0>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
+    else
+      akz_fed_prologue<2>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
+    akz_fed_gather_smem(sT, sP, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
+    cur = sT; /* holds the level values of R0 */
+    nxt = sS; /* free once the conductance is done */
   } else {
     cur = sm;
     nxt = sm + RW * RH;
     const float *lp = planes + (p.src == 1 ? I.t1 : I.t2);
     const float *gp = planes + I.g;
     const long long pitch = L.pitch;
-    const int xc = min(max(x, 0), W - 1);
+    const bool x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
+#pragma unroll
     for (int r = 0; r < RB; r++) {
       const int y = ytop + r;
-      Lr[r] = 0.0f;
-      gE[r] = gW[r] = gS[r] = 0.0f;
-      if (xin && y >= 0 && y < H) {
-        const float *gr = gp + (long long)y * pitch;
-        const float gc = __ldg(gr + xc);
-        Lr[r] = __ldg(lp + (long long)y * pitch + xc);
-        if (x + 1 < W) gE[r] = gc + __ldg(gr + xc + 1);
-        if (x >= 1) gW[r] = __ldg(gr + xc - 1) + gc;
-        if (y + 1 < H) gS[r] = gc + __ldg(gr + pitch + xc);
+      Lp[r] = make_float2(0.0f, 0.0f);
+      gs[r] = make_float2(0.0f, 0.0f);
+      gw[r] = gm[r] = ge[r] = 0.0f;
+      if (y >= 0 && y < H) {
+        const float *gr = gp + (long long)y * pitch, *lr = lp + (long long)y * pitch;
+        const float c0 = x0in ? __ldg(gr + x0) : 0.0f, c1 = x1in ? __ldg(gr + x0 + 1) : 0.0f;
+        if (x0in) Lp[r].x = __ldg(lr + x0);
+        if (x1in) Lp[r].y = __ldg(lr + x0 + 1);
+        if (x0in && x0 >= 1) gw[r] = __ldg(gr + x0 - 1) + c0;
+        if (x0 >= 0 && x0 + 1 < W) gm[r] = c0 + c1;
+        if (x1in && x0 + 2 < W) ge[r] = c1 + __ldg(gr + x0 + 2);
+        if (y + 1 < H) {
+          if (x0in) gs[r].x = c0 + __ldg(gr + pitch + x0);
+          if (x1in) gs[r].y = c1 + __ldg(gr + pitch + x0 + 1);
+        }
       }
     }
-    gN0 = (xin && ytop >= 1 && ytop < H) ? __ldg(gp + (long long)(ytop - 1) * pitch + xc) + __ldg(gp + (long long)ytop * pitch + xc) : 0.0f;
+    gn0 = make_float2(0.0f, 0.0f);
+    if (ytop >= 1 && ytop < H) {
+      const float *ga = gp + (long long)(ytop - 1) * pitch, *gb = gp + (long long)ytop * pitch;
+      if (x0in) gn0.x = __ldg(ga + x0) + __ldg(gb + x0);
+      if (x1in) gn0.y = __ldg(ga + x0 + 1) + __ldg(gb + x0 + 1);
+    }
+#pragma unroll
+    for (int r = 0; r < RB; r++) st2(cur + (ly0 + r) * RW + lx0, Lp[r]);
+    __syncthreads();
   }
-  for (int r = 0; r < RB; r++) cur[(ly0 + r) * RW + lx] = Lr[r];
-  __syncthreads();
 
-  /* FED steps: xpos - xneg + ypos - yneg, scaled by tau/2, added to L
-   * (nld_step_scalar, nldiffusion_functions.cpp:232-237 and :309-316) */
+  /* FED steps (nld_step_scalar, nldiffusion_functions.cpp:232-237, :309-316):
+   *   L += h * (((xpos - xneg) + ypos) - yneg)
+   * Each flux product is formed once and used twice, which is exact: the
+   * reference's xneg at x+1 is (c(x) + c(x+1)) * (L(x+1) - L(x)), the same
+   * operands in the same order as xpos at x, and likewise yneg at y+1 and ypos
+   * at y.  Additions run as packed FP32x2 pairs of the two columns; products
+   * stay scalar. */
   const int lyn = max(ly0 - 1, 0), lys = min(ly0 + RB, RH - 1);
+  const int lxw = max(lx0 - 1, 0), lxe = min(lx0 + 2, RW - 1);
   for (int s = 0; s < d; s++) {
     const float h = p.h[s];
-    float prev = cur[lyn * RW + lx];
-    const float below = cur[lys * RW + lx];
+    const float2 above = ld2(cur + lyn * RW + lx0);
+    const float2 below = ld2(cur + lys * RW + lx0);
+    const float2 dn = f2sub(Lp[0], above);
+    float2 Fn = make_float2(gn0.x * dn.x, gn0.y * dn.y);
 #pragma unroll
     for (int r = 0; r < RB; r++) {
       const int ly = ly0 + r;
-      const float Lc = Lr[r];
-      const float Le = cur[ly * RW + lxe];
-      const float Lw = cur[ly * RW + lxw];
-      const float Ls = r < RB - 1 ? Lr[r + 1] : below;
-      const float gn = r == 0 ? gN0 : gS[r - 1];
-      const float xpos = gE[r] * (Le - Lc);
-      const float xneg = gW[r] * (Lc - Lw);
-      const float ypos = gS[r] * (Ls - Lc);
-      const float yneg = gn * (Lc - prev);
-      const float nv = Lc + h * (xpos - xneg + ypos - yneg);
-      nxt[ly * RW + lx] = nv;
-      prev = Lc;
-      Lr[r] = nv;
+      const float2 Lc = Lp[r];
+      const float Lw = cur[ly * RW + lxw], Le = cur[ly * RW + lxe];
+      const float2 dwm = f2sub(Lc, make_float2(Lw, Lc.x)); /* L(x0)-L(x0-1), L(x0+1)-L(x0) */
+      const float de = Le - Lc.y;                          /* L(x0+2)-L(x0+1) */
+      const float Fw = gw[r] * dwm.x, Fm = gm[r] * dwm.y, Fe = ge[r] * de;
+      const float2 xs = f2sub(make_float2(Fm, Fe), make_float2(Fw, Fm)); /* xpos - xneg */
+      const float2 ds = f2sub(r < RB - 1 ? Lp[r + 1] : below, Lc);
+      const float2 Fs = make_float2(gs[r].x * ds.x, gs[r].y * ds.y); /* ypos */
+      const float2 t = f2sub(f2add(xs, Fs), Fn);
+      const float2 nv = f2add(Lc, make_float2(h * t.x, h * t.y));
+      st2(nxt + ly * RW + lx0, nv);
+      Lp[r] = nv;
+      Fn = Fs;
     }
     __syncthreads();
     float *t = cur;
@@ -607,11 +586,14 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   }
   /* tile interior from registers */
   float *out = planes + (p.dst == 0 ? L.lt : (p.dst == 1 ? I.t1 : I.t2));
-  if (x >= tx0 && x < tx1) {
+  const bool w0 = x0 >= tx0 && x0 < tx1, w1 = x0 + 1 >= tx0 && x0 + 1 < tx1;
 #pragma unroll
-    for (int r = 0; r < RB; r++) {
-      const int y = ytop + r;
-      if (y >= ty0 && y < ty1) out[(long long)y * L.pitch + x] = Lr[r];
+  for (int r = 0; r < RB; r++) {
+    const int y = ytop + r;
+    if (y >= ty0 && y < ty1) {
+      float *o = out + (long long)y * L.pitch + x0;
+      if (w0) o[0] = Lp[r].x;
+      if (w1) o[1] = Lp[r].y;
     }
   }
 }
