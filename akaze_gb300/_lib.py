@@ -26,7 +26,7 @@ EXPORTS = [
     "akz_batch_run", "akz_batch_counts", "akz_batch_results", "akz_batch_device_results",
     "akz_batch_detect_describe", "akz_batch_level_plane", "akz_batch_kernel_count", "akz_batch_profile",
     "akz_matcher_create", "akz_matcher_destroy", "akz_matcher_set_stream", "akz_matcher_bfmatch",
-    "akz_matcher_bfmatch_device", "akz_matcher_bfmatch_noalloc",
+    "akz_matcher_bfmatch_device", "akz_matcher_bfmatch_noalloc", "akz_measure_popc_rate",
 ]
 
 
@@ -102,6 +102,7 @@ def load():
         "akz_matcher_bfmatch": ([P, P, I, P, I, I, P], I),
         "akz_matcher_bfmatch_device": ([P, P, I, P, I, P], I),
         "akz_matcher_bfmatch_noalloc": ([P, I, P, I, P, P], I),
+        "akz_measure_popc_rate": ([I, ctypes.POINTER(ctypes.c_double), P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: --batch images, one graph-less run of every stage, no timing line")
+    ap.add_argument("--workload", default="batch1080p", choices=["batch1080p", "single640", "uneven64", "matcher"],
+                    help="batch1080p: the headline line (default); single640: one 640x480 pair, GPU and CPU; "
+                         "uneven64: 64 images of uneven sizes, images/s and per-image latency; "
+                         "matcher: 2-NN sweep N=M 1024..131072, Gmatch/s against the popc roofline")
     return ap.parse_args()
 
 
@@ -151,12 +155,13 @@ def dist_setup(args):
     return ws, rank, local
 
 
-def cpu_oracle_rate(w, h, seconds, seed=900):
-    """Images/s of the CPU oracle (all host cores) on a bounded sample."""
+def cpu_oracle_rate(w, h, seconds, seed=900, threads=None, max_runs=50):
+    """Images/s of the CPU oracle on a bounded sample (all host cores unless
+    threads is given)."""
     from akaze_gb300 import synth
     from oracle import oracle_ctypes as oc
     oc.build()
-    cores = os.cpu_count() or 1
+    cores = threads or os.cpu_count() or 1
     oc.set_threads(cores)
     img = synth.synth_image(seed, w, h)
     o = oc.Oracle(w, h)
@@ -166,8 +171,9 @@ def cpu_oracle_rate(w, h, seconds, seed=900):
         o.run(img)
         n += 1
         el = time.perf_counter() - t0
-        if el >= seconds or n >= 50:
+        if el >= seconds or n >= max_runs:
             break
+    oc.set_threads(os.cpu_count() or 1)
     return n / el, cores, f"{n} runs of one {w}x{h} synthetic image, {cores} OpenMP threads, {el:.1f} s"
 
 
@@ -207,10 +213,172 @@ def run_reference(args):
     return 0
 
 
+def _torch_stream():
+    import torch
+    torch.cuda.set_device(0)
+    return torch, torch.cuda.Stream()
+
+
+def _event_ms(torch, stream, fn, reps):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def nndr_inliers(kp1, kp2, matches, Hm, ratio=0.8, px=2.5):
+    """NNDR matches and homography inliers (akaze_match.cpp:35-36, utils.cpp:154-243)."""
+    from akaze_gb300 import synth
+    if len(matches) == 0:
+        return 0, 0
+    d1, d2 = matches[:, 0]["distance"], matches[:, 1]["distance"]
+    good = d1 < ratio * d2
+    qi, ti = matches[good, 0]["queryIdx"], matches[good, 0]["trainIdx"]
+    x, y = synth._apply(Hm, kp1["x"][qi].astype(np.float64), kp1["y"][qi].astype(np.float64))
+    err = np.hypot(x - kp2["x"][ti], y - kp2["y"][ti])
+    return int(good.sum()), int((err < px).sum())
+
+
+def workload_single640(args):
+    """One 640x480 pair through the reference's class API on the GPU, next to
+    the CPU oracle on one thread and on all host cores."""
+    torch, stream = _torch_stream()
+    import akaze_gb300 as akz
+    from akaze_gb300 import synth
+    W, H = 640, 480
+    img1, img2, Hm = synth.synth_pair(11, W, H)
+    o = akz.AKAZEOptions()
+    o.setWidth(W)
+    o.setHeight(H)
+    ak = akz.AKAZE(o)
+    ak.set_stream(stream.cuda_stream)
+    res = [ak.detect_and_compute(im) for im in (img1, img2)]
+    reps = max(args.steps, 10)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ak.detect_and_compute(img1)
+    api_ms = 1000 * (time.perf_counter() - t0) / reps
+    b = akz.Batch(akz.AKAZEOptions(), [(W, H)])
+    b.set_stream(stream.cuda_stream)
+    b.upload([img1])
+    for _ in range(max(args.warmup, 3)):
+        b.run()
+    dev_ms = _event_ms(torch, stream, b.run, reps)
+    m = akz.Matcher()
+    (k1, d1), (k2, d2) = res
+    matches = m.bfmatch(d1, d2)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        m.bfmatch(d1, d2)
+    match_ms = 1000 * (time.perf_counter() - t0) / reps
+    nn, inl = nndr_inliers(k1, k2, matches, Hm)
+    cpu_all, cores, _ = cpu_oracle_rate(W, H, 3.0, seed=11)
+    cpu_one, _, _ = cpu_oracle_rate(W, H, 3.0, seed=11, threads=1, max_runs=20)
+    print(json.dumps({
+        "workload": "single640", "config": "640x480 u8 pair, default options, full M-LDB, 2-NN match",
+        "gpu_ms_per_image_device": dev_ms, "gpu_ms_per_image_class_api": api_ms, "match_ms_host_api": match_ms,
+        "keypoints": [int(len(k1)), int(len(k2))], "nndr_matches": nn, "homography_inliers": inl,
+        "cpu_ms_per_image": {"threads_%d" % cores: 1000.0 / cpu_all, "threads_1": 1000.0 / cpu_one},
+        "speedup_device_vs_cpu_all_cores": (1000.0 / cpu_all) / dev_ms,
+    }))
+    return 0
+
+
+def workload_uneven64(args):
+    """64 images of uneven sizes in one graph-replayed batch (images/s), and
+    each image alone (per-image latency, p50/p99)."""
+    torch, stream = _torch_stream()
+    import akaze_gb300 as akz
+    from akaze_gb300 import synth
+    sizes = synth.uneven_sizes(2024, 64)
+    imgs = [synth.synth_image(3000 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    opt = akz.AKAZEOptions()
+    b = akz.Batch(opt, sizes)
+    b.set_stream(stream.cuda_stream)
+    b.upload(imgs)
+    for _ in range(max(args.warmup, 3)):
+        b.run()
+    step_ms = _event_ms(torch, stream, b.run, args.steps)
+    counts = b.counts()
+    singles = []
+    for (w, h), im in zip(sizes, imgs):
+        s1 = akz.Batch(opt, [(w, h)])
+        s1.set_stream(stream.cuda_stream)
+        s1.upload([im])
+        for _ in range(3):
+            s1.run()
+        singles.append(_event_ms(torch, stream, s1.run, 5))
+        s1.close()
+    lat = np.array(singles)
+    mpix = sum(w * h for w, h in sizes) / 1e6
+    print(json.dumps({
+        "workload": "uneven64", "config": "64 synthetic images, W~U[320,1920], H~U[240,1080], multiples of 8",
+        "images_per_s": 64 * 1000.0 / step_ms, "batch_ms": step_ms, "megapixels_per_batch": mpix,
+        "latency_ms_alone": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                             "min": float(lat.min()), "max": float(lat.max())},
+        "latency_ms_in_batch": step_ms, "keypoints_total": int(sum(counts)),
+    }))
+    return 0
+
+
+def workload_matcher(args):
+    """2-NN Hamming sweep N=M in 1024..131072 against the popc roofline; the
+    top-2 of 256 sampled queries per size is checked against numpy."""
+    torch, stream = _torch_stream()
+    import ctypes
+    import akaze_gb300 as akz
+    from akaze_gb300 import synth
+    lib = akz._lib.load()
+    rate = ctypes.c_double(0)
+    akz._lib.check(lib.akz_measure_popc_rate(2000, ctypes.byref(rate), ctypes.c_void_p(stream.cuda_stream)))
+    peak_pairs = rate.value / 16.0
+    m = akz.Matcher()
+    m.set_stream(stream.cuda_stream)
+    rows = []
+    for k in range(8):
+        N = 1024 << k
+        q61, t61 = synth.matcher_rows(5000 + k, N, N)
+        q64 = np.zeros((N, 64), np.uint8)
+        t64 = np.zeros((N, 64), np.uint8)
+        q64[:, :61], t64[:, :61] = q61, t61
+        qd, td = torch.from_numpy(q64).cuda(), torch.from_numpy(t64).cuda()
+        out = torch.empty((N, 2, 4), dtype=torch.int32, device="cuda")
+        fn = lambda: m.bfmatch_device(qd.data_ptr(), N, td.data_ptr(), N, out.data_ptr())
+        for _ in range(2):
+            fn()
+        reps = max(3, min(50, int(2e10 / (N * N))))
+        ms = _event_ms(torch, stream, fn, reps)
+        res = out.cpu().numpy()
+        resf = res.view(np.float32)
+        rng = np.random.default_rng(k)
+        sample = rng.choice(N, min(256, N), replace=False)
+        ok = True
+        for i in sample:
+            d = np.bitwise_count(np.bitwise_xor(t64, q64[i]).view(np.uint64)).sum(axis=1)
+            order = np.lexsort((np.arange(N), d))
+            want = [(int(order[0]), int(d[order[0]])), (int(order[1]), int(d[order[1]]))]
+            got = [(int(res[i, j, 1]), int(resf[i, j, 3])) for j in range(2)]
+            ok &= want == got
+        pairs = N * N / (ms / 1000.0)
+        rows.append({"N": N, "ms": ms, "gmatch_per_s": pairs / 1e9, "frac_popc_roofline": pairs / peak_pairs,
+                     "sample_exact": bool(ok)})
+    print(json.dumps({"workload": "matcher", "config": "N=M rows of 486 Bernoulli(0.5) bits in 64 B, 30% planted "
+                      "copies with 5% bit flips", "popc_triples_per_s": rate.value,
+                      "peak_gmatch_per_s": peak_pairs / 1e9, "sweep": rows}))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "batch1080p":
+        return {"single640": workload_single640, "uneven64": workload_uneven64,
+                "matcher": workload_matcher}[args.workload](args)
     ws, rank, local = dist_setup(args)
     import torch
     torch.cuda.set_device(local)
@@ -291,6 +459,7 @@ def main():
             dist.destroy_process_group()
         return 0
     cpu_v, cores, sample = cpu_oracle_rate(W, H, args.cpu_seconds)
+    cpu_1, _, sample_1 = cpu_oracle_rate(W, H, min(args.cpu_seconds, 6.0), threads=1, max_runs=5)
     nkp = float(np.mean(counts))
     line = {
         "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
@@ -310,7 +479,8 @@ def main():
                               "frac": image_algorithmic_bytes(W, H, nkp) * value / 1e9 / pk["hbm_gbs"],
                               "bytes_per_image": image_algorithmic_bytes(W, H, nkp)},
         "stage_ms": dict(zip(["contrast", "level0", "levels", "detector", "scan_extract", "suppression", "describe"], stage)),
-        "cpu_baseline": {"value": cpu_v, "unit": "images/s", "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": cpu_v, "unit": "images/s", "cores": cores, "kind": "port", "sample": sample,
+                         "single_thread": {"value": cpu_1, "sample": sample_1}},
         "e2e": {"value": e2e, "unit": "images/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": n_launch * args.steps,
         "clocks": clocks,

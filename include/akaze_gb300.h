@@ -219,6 +219,14 @@ AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *que
 AKZ_API akz_status akz_matcher_bfmatch_noalloc(const uint8_t *query64, int nq, const uint8_t *train64, int nt,
                                               akz_dmatch *out, void *stream);
 
+/* Measurement helper for the matcher's roofline (no counterpart in the
+ * reference, whose README.md:22 publishes no matcher figure): the sustained
+ * rate of 32-bit (xor, popc, add) triples on the current GPU, from one timed
+ * launch of iters iterations x 8 chains per thread on every SM.  A pair of
+ * 64-byte rows costs 16 triples, so the matcher's peak in pairs/s is
+ * *triples_per_s / 16.  Synchronises stream; allocates 4 bytes. */
+AKZ_API akz_status akz_measure_popc_rate(int iters, double *triples_per_s, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
