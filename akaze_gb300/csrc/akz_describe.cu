@@ -24,8 +24,10 @@
 
 /* orientation samples in the reference's thread order: tx = 16*(j+6) + (i+6) */
 __constant__ signed char c_oi[109], c_oj[109], c_or2[109];
-/* comparison pairs (cell*3 + channel) in bit order */
-__constant__ unsigned char c_cmp1[486], c_cmp2[486];
+/* comparison pairs (cell*3 + channel) in bit order; read with one coalesced
+ * load per warp and bit word (a __constant__ table would serialise the
+ * lanes' different addresses) */
+__device__ unsigned char g_cmp1[512], g_cmp2[512];
 
 struct akz_warp_smem {
   float s[3][441];
@@ -78,15 +80,28 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
         S.bin[s] = (unsigned char)bin;
       }
       __syncwarp();
-      for (int b = lane; b < 42; b += 32) {
-        float rx = 0.0f, ry = 0.0f;
-        for (int s = 0; s < 109; s++)
-          if (S.bin[s] == b) {
-            rx += S.s[0][s];
-            ry += S.s[1][s];
+      {
+        /* bins lane and lane + 32 in one pass, each summed in sample order */
+        const int b1 = lane + 32;
+        float rx0 = 0.0f, ry0 = 0.0f, rx1 = 0.0f, ry1 = 0.0f;
+        for (int s = 0; s < 109; s++) {
+          const int b = S.bin[s];
+          const float sx = S.s[0][s], sy = S.s[1][s];
+          if (b == lane) {
+            rx0 += sx;
+            ry0 += sy;
           }
-        S.bx[b] = rx;
-        S.by[b] = ry;
+          if (b == b1) {
+            rx1 += sx;
+            ry1 += sy;
+          }
+        }
+        S.bx[lane] = rx0;
+        S.by[lane] = ry0;
+        if (b1 < 42) {
+          S.bx[b1] = rx1;
+          S.by[b1] = ry1;
+        }
       }
       __syncwarp();
       float best = -1.0f;
@@ -165,14 +180,16 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
       S.v[q] = acc;
     }
     __syncwarp();
-    if (lane < 16) {
-      uint32_t word = 0;
-      for (int b = 0; b < 32; b++) {
-        const int bit = lane * 32 + b;
-        if (bit < 486 && S.v[c_cmp1[bit]] > S.v[c_cmp2[bit]]) word |= 1u << b;
-      }
-      p.desc[(long long)(I.kp_base + k) * 16 + lane] = word;
+    /* word w holds bits 32w .. 32w+31, LSB first: one ballot per word */
+    uint32_t myword = 0;
+#pragma unroll 4
+    for (int w = 0; w < 16; w++) {
+      const int bit = w * 32 + lane;
+      const bool v = bit < 486 && S.v[__ldg(&g_cmp1[bit])] > S.v[__ldg(&g_cmp2[bit])];
+      const uint32_t word = __ballot_sync(0xffffffffu, v);
+      if (lane == w) myword = word;
     }
+    if (lane < 16) p.desc[(long long)(I.kp_base + k) * 16 + lane] = myword;
     __syncwarp();
   }
 }
@@ -192,7 +209,7 @@ static cudaError_t akz_init_describe_tables()
       n++;
     }
   }
-  unsigned char c1[486], c2[486];
+  unsigned char c1[512] = {0}, c2[512] = {0};
   int m = 0;
   const int g0[3] = {0, 4, 13}, g1[3] = {4, 13, 29};
   for (int grid = 0; grid < 3; grid++)
@@ -207,8 +224,8 @@ static cudaError_t akz_init_describe_tables()
   if ((e = cudaMemcpyToSymbol(c_oi, oi, sizeof(oi))) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_oj, oj, sizeof(oj))) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_or2, orr, sizeof(orr))) != cudaSuccess) return e;
-  if ((e = cudaMemcpyToSymbol(c_cmp1, c1, sizeof(c1))) != cudaSuccess) return e;
-  return cudaMemcpyToSymbol(c_cmp2, c2, sizeof(c2));
+  if ((e = cudaMemcpyToSymbol(g_cmp1, c1, sizeof(c1))) != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(g_cmp2, c2, sizeof(c2));
 }
 
 cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaStream_t s)

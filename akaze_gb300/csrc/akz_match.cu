@@ -116,12 +116,14 @@ cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *
   return cudaGetLastError();
 }
 
-/* Number of train splits so that the grid covers the GPU. */
+/* Number of train splits so that the grid holds about 4 CTAs per SM, with at
+ * least 64 train rows per split: a small query set is otherwise a handful of
+ * CTAs each walking the whole train set, bound by the latency of one row. */
 int akz_match_splits(int nq, int nt, int nsm)
 {
   const int qb = (nq + AKZ_MQ - 1) / AKZ_MQ;
-  int ns = (2 * nsm + qb - 1) / qb;
-  const int maxs = (nt + 1023) / 1024;
+  int ns = (4 * nsm + qb - 1) / qb;
+  const int maxs = (nt + 63) / 64;
   if (ns > maxs) ns = maxs;
   if (ns < 1) ns = 1;
   return ns;
