@@ -36,14 +36,18 @@ __device__ __forceinline__ void akz_detect_interior(const akz_detect_params &p, 
                                                     int tx0, int ty0)
 {
   constexpr int TW = AKZ_DETECT_TW, TH = AKZ_DETECT_TH;
-  constexpr int SW = TW + 4 * ST + 2, SH = TH + 4 * ST + 2;
-  constexpr int DW = TW + 2 * ST + 2, DH = TH + 2 * ST + 2;
-  constexpr int EW = TW + 2, EH = TH + 2;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float *sS = sm, *sX = sm + SW * SH, *sY = sX + DW * DH, *sD = sY + DW * DH;
+  constexpr int SW = TW + 4 * ST + 2, SH = TH + 4 * ST + 2; /* Lsmooth: tile +- (2ST+1) */
+  constexpr int DW = TW + 2 * ST + 2, DH = TH + 2 * ST + 2; /* Lx, Ly:  tile +- (ST+1)  */
+  constexpr int EW = TW + 2, EH = TH + 2;                   /* Ldet:    tile +- 1       */
+  constexpr int DP = DW / 2, EP = EW / 2;                   /* column pairs */
+  static_assert(SW % 2 == 0 && DW % 2 == 0 && EW % 2 == 0, "pair layout");
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  /* the determinant plane reuses the Lsmooth region, dead after the derivative pass */
+  float *sS = sm, *sX = sm + SW * SH, *sY = sX + DW * DH, *sD = sm;
+  static_assert(EW * EH <= SW * SH, "determinant plane fits the Lsmooth region");
   const float fac1 = p.fac1, fac2 = p.fac2;
   const float *ls = p.t.planes + L.ls + (long long)(ty0 - 2 * ST - 1) * L.pitch + (tx0 - 2 * ST - 1);
-#pragma unroll 2
+#pragma unroll
   for (int n = warp; n < SH; n += 8) {
     const float *q = ls + (long long)n * L.pitch;
 #pragma unroll
@@ -53,49 +57,57 @@ __device__ __forceinline__ void akz_detect_interior(const akz_detect_params &p, 
     }
   }
   __syncthreads();
+  /* Lx, Ly on the tile +- (ST+1), two columns per item: D column d is
+   * Lsmooth column d + ST; its taps sit at d, d + ST and d + 2ST, so the
+   * outer taps are aligned pairs for every ST (cuda_akaze.cu:651-671) */
   float *lxp = p.t.planes + L.lx + (long long)(ty0 - ST - 1) * L.pitch + (tx0 - ST - 1);
   float *lyp = p.t.planes + L.ly + (long long)(ty0 - ST - 1) * L.pitch + (tx0 - ST - 1);
-#pragma unroll 2
-  for (int n = warp; n < DH; n += 8) {
-    const float *su = sS + n * SW, *sc = su + ST * SW, *sd = su + 2 * ST * SW;
-    const bool yt = n >= ST + 1 && n < ST + 1 + TH;
-#pragma unroll
-    for (int j = 0; j < (DW + 31) / 32; j++) {
-      const int m = lane + 32 * j;
-      if (m < DW) {
-        const float ul = su[m], ur = su[m + 2 * ST], ll = sd[m], lr = sd[m + 2 * ST];
-        const float cl = sc[m], cr = sc[m + 2 * ST], uc = su[m + ST], lc = sd[m + ST];
-        const float a = fac1 * (ur + lr - ul - ll) + fac2 * (cr - cl);
-        const float b = fac1 * (lr + ll - ur - ul) + fac2 * (lc - uc);
-        sX[n * DW + m] = a;
-        sY[n * DW + m] = b;
-        if (yt && m >= ST + 1 && m < ST + 1 + TW) {
-          lxp[(long long)n * L.pitch + m] = a;
-          lyp[(long long)n * L.pitch + m] = b;
-        }
+  for (int i = tid; i < DH * DP; i += 256) {
+    const int n = i / DP, d = 2 * (i - n * DP);
+    const float *su = sS + n * SW + d, *sc = su + ST * SW, *sd = su + 2 * ST * SW;
+    const float2 ul = ld2(su), ur = ld2(su + 2 * ST), ll = ld2(sd), lr = ld2(sd + 2 * ST);
+    const float2 cl = ld2(sc), cr = ld2(sc + 2 * ST);
+    const float2 uc = (ST & 1) ? make_float2(su[ST], su[ST + 1]) : ld2(su + ST);
+    const float2 lc = (ST & 1) ? make_float2(sd[ST], sd[ST + 1]) : ld2(sd + ST);
+    const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
+    const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(lc, uc);
+    const float2 a = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
+    const float2 b = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+    st2(sX + n * DW + d, a);
+    st2(sY + n * DW + d, b);
+    if (n >= ST + 1 && n < ST + 1 + TH) {
+      float *ox = lxp + (long long)n * L.pitch + d, *oy = lyp + (long long)n * L.pitch + d;
+      if (d >= ST + 1 && d < ST + 1 + TW) {
+        ox[0] = a.x;
+        oy[0] = b.x;
+      }
+      if (d + 1 >= ST + 1 && d + 1 < ST + 1 + TW) {
+        ox[1] = a.y;
+        oy[1] = b.y;
       }
     }
   }
   __syncthreads();
-#pragma unroll 2
-  for (int n = warp; n < EH; n += 8) {
-    const float *xu = sX + n * DW, *xc = xu + ST * DW, *xd = xu + 2 * ST * DW;
-    const float *yu = sY + n * DW, *yd = yu + 2 * ST * DW;
-#pragma unroll
-    for (int j = 0; j < (EW + 31) / 32; j++) {
-      const int m = lane + 32 * j;
-      if (m < EW) {
-        float ul = xu[m], ur = xu[m + 2 * ST], ll = xd[m], lr = xd[m + 2 * ST];
-        const float lxx = fac1 * (ur + lr - ul - ll) + fac2 * (xc[m + 2 * ST] - xc[m]);
-        const float lyx = fac1 * (lr + ll - ur - ul) + fac2 * (xd[m + ST] - xu[m + ST]);
-        ul = yu[m];
-        ur = yu[m + 2 * ST];
-        ll = yd[m];
-        lr = yd[m + 2 * ST];
-        const float lyy = fac1 * (lr + ll - ur - ul) + fac2 * (yd[m + ST] - yu[m + ST]);
-        sD[n * EW + m] = lxx * lyy - lyx * lyx;
-      }
-    }
+  /* Hessian determinant on the tile +- 1 (cuda_akaze.cu:673-701): E column e
+   * is D column e + ST */
+  for (int i = tid; i < EH * EP; i += 256) {
+    const int n = i / EP, e = 2 * (i - n * EP);
+    const float *xu = sX + n * DW + e, *xc = xu + ST * DW, *xd = xu + 2 * ST * DW;
+    const float *yu = sY + n * DW + e, *yd = yu + 2 * ST * DW;
+    const float2 ul = ld2(xu), ur = ld2(xu + 2 * ST), ll = ld2(xd), lr = ld2(xd + 2 * ST);
+    const float2 cl = ld2(xc), cr = ld2(xc + 2 * ST);
+    const float2 xuc = (ST & 1) ? make_float2(xu[ST], xu[ST + 1]) : ld2(xu + ST);
+    const float2 xdc = (ST & 1) ? make_float2(xd[ST], xd[ST + 1]) : ld2(xd + ST);
+    const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
+    const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(xdc, xuc);
+    const float2 lxx = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
+    const float2 lyx = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+    const float2 vul = ld2(yu), vur = ld2(yu + 2 * ST), vll = ld2(yd), vlr = ld2(yd + 2 * ST);
+    const float2 yuc = (ST & 1) ? make_float2(yu[ST], yu[ST + 1]) : ld2(yu + ST);
+    const float2 ydc = (ST & 1) ? make_float2(yd[ST], yd[ST + 1]) : ld2(yd + ST);
+    const float2 cy = f2sub(f2sub(f2add(vlr, vll), vur), vul), dy = f2sub(ydc, yuc);
+    const float2 lyy = f2add(make_float2(fac1 * cy.x, fac1 * cy.y), make_float2(fac2 * dy.x, fac2 * dy.y));
+    st2(sD + n * EW + e, f2sub(make_float2(lxx.x * lyy.x, lxx.y * lyy.y), make_float2(lyx.x * lyx.x, lyx.y * lyx.y)));
   }
   __syncthreads();
   const float border = L.border;
@@ -155,7 +167,7 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   }
   const int SM = (TW + 4 * max_step + 2) * (TH + 4 * max_step + 2);
   const int DM = (TW + 2 * max_step + 2) * (TH + 2 * max_step + 2);
-  float *sS = sm, *sX = sm + SM, *sY = sX + DM, *sD = sY + DM;
+  float *sS = sm, *sX = sm + SM, *sY = sX + DM, *sD = sm; /* determinant plane over the dead Lsmooth region */
 
   const int lane = tid & 31, warp = tid >> 5;
   const float *ls = p.t.planes + L.ls;
@@ -546,8 +558,7 @@ cudaError_t akz_launch_detect(const akz_detect_params &p, int ntiles, int max_st
   if (ntiles <= 0) return cudaSuccess;
   const size_t SM = (size_t)(AKZ_DETECT_TW + 4 * max_step + 2) * (AKZ_DETECT_TH + 4 * max_step + 2);
   const size_t DM = (size_t)(AKZ_DETECT_TW + 2 * max_step + 2) * (AKZ_DETECT_TH + 2 * max_step + 2);
-  const size_t EM = (size_t)(AKZ_DETECT_TW + 2) * (AKZ_DETECT_TH + 2);
-  const size_t smem = (SM + 2 * DM + EM) * sizeof(float);
+  const size_t smem = (SM + 2 * DM) * sizeof(float); /* the determinant plane reuses the Lsmooth region */
   cudaError_t e = cudaFuncSetAttribute(k_detect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k_detect<<<ntiles, 256, smem, s>>>(p, max_step);
