@@ -28,43 +28,70 @@
 
 /* ------------------------------------------------------------------------ */
 
-/* k_detect for a tile whose Lsmooth region (tile +- (2*ST+1)) lies inside
- * the level: no reflection, compile-time region sizes, straight-line loops.
- * Same arithmetic, in the same order, as the general path. */
-template <int ST>
-__device__ __forceinline__ void akz_detect_interior(const akz_detect_params &p, const akz_level_desc &L, float *sm,
-                                                    int tx0, int ty0)
+/* k_detect for every tile of a level with derivative step ST (2..4, the steps
+ * of the default options): compile-time region sizes, straight-line loops,
+ * column pairs with packed FP32x2 additions (products scalar), in the
+ * reference's operation order.
+ *
+ * Borders: the Lsmooth region is staged with reflect-101 coordinates, which
+ * makes Lx and Ly exact at every pixel inside the image (their taps at +-ST
+ * are the reference's reflect-101 indices, cuda_akaze.cu:657-660).  The
+ * determinant reads Lx and Ly at reflect-101 indices too, i.e. the mirrored
+ * in-image value, not a derivative of the mirrored image, so after the
+ * derivative pass the entries just outside the image (within ST) are
+ * replaced by their in-image mirrors.
+ *
+ * Layout: tile 64 x 32, 64-bit pair accesses in row-major flat order. */
+template <int ST, bool BORDER>
+__device__ __forceinline__ void akz_detect_tile(const akz_detect_params &p, const akz_level_desc &L, float *sm, int tx0,
+                                                int ty0)
 {
   constexpr int TW = AKZ_DETECT_TW, TH = AKZ_DETECT_TH;
-  constexpr int SW = TW + 4 * ST + 2, SH = TH + 4 * ST + 2; /* Lsmooth: tile +- (2ST+1) */
   constexpr int DW = TW + 2 * ST + 2, DH = TH + 2 * ST + 2; /* Lx, Ly:  tile +- (ST+1)  */
+  constexpr int SW = TW + 4 * ST + 2, SH = TH + 4 * ST + 2; /* Lsmooth: tile +- (2ST+1) */
+  constexpr int SWS = SW;                                   /* Lsmooth row stride */
   constexpr int EW = TW + 2, EH = TH + 2;                   /* Ldet:    tile +- 1       */
   constexpr int DP = DW / 2, EP = EW / 2;                   /* column pairs */
-  static_assert(SW % 2 == 0 && DW % 2 == 0 && EW % 2 == 0, "pair layout");
+  static_assert(DW % 2 == 0 && EW % 2 == 0 && SW % 2 == 0, "pair layout");
+  static_assert(EW * EH <= SWS * SH, "determinant plane fits the Lsmooth region");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int W = L.width, H = L.height;
   /* the determinant plane reuses the Lsmooth region, dead after the derivative pass */
-  float *sS = sm, *sX = sm + SW * SH, *sY = sX + DW * DH, *sD = sm;
-  static_assert(EW * EH <= SW * SH, "determinant plane fits the Lsmooth region");
+  float *sS = sm, *sX = sm + SWS * SH, *sY = sX + DW * DH, *sD = sm;
   const float fac1 = p.fac1, fac2 = p.fac2;
-  const float *ls = p.t.planes + L.ls + (long long)(ty0 - 2 * ST - 1) * L.pitch + (tx0 - 2 * ST - 1);
+  const float *ls = p.t.planes + L.ls;
+  if (BORDER) {
 #pragma unroll
-  for (int n = warp; n < SH; n += 8) {
-    const float *q = ls + (long long)n * L.pitch;
+    for (int n = warp; n < SH; n += 8) {
+      const int y = akz_refl101(min(ty0 - 2 * ST - 1 + n, H + 2 * ST), H);
+      const float *q = ls + (long long)y * L.pitch;
 #pragma unroll
-    for (int j = 0; j < (SW + 31) / 32; j++) {
-      const int m = lane + 32 * j;
-      if (m < SW) sS[n * SW + m] = __ldg(q + m);
+      for (int j = 0; j < (SW + 31) / 32; j++) {
+        const int m = lane + 32 * j;
+        if (m < SW) sS[n * SWS + m] = __ldg(q + akz_refl101(min(tx0 - 2 * ST - 1 + m, W + 2 * ST), W));
+      }
+    }
+  } else {
+    const float *q0 = ls + (long long)(ty0 - 2 * ST - 1) * L.pitch + (tx0 - 2 * ST - 1);
+#pragma unroll
+    for (int n = warp; n < SH; n += 8) {
+      const float *q = q0 + (long long)n * L.pitch;
+#pragma unroll
+      for (int j = 0; j < (SW + 31) / 32; j++) {
+        const int m = lane + 32 * j;
+        if (m < SW) sS[n * SWS + m] = __ldg(q + m);
+      }
     }
   }
   __syncthreads();
   /* Lx, Ly on the tile +- (ST+1), two columns per item: D column d is
    * Lsmooth column d + ST; its taps sit at d, d + ST and d + 2ST, so the
    * outer taps are aligned pairs for every ST (cuda_akaze.cu:651-671) */
-  float *lxp = p.t.planes + L.lx + (long long)(ty0 - ST - 1) * L.pitch + (tx0 - ST - 1);
-  float *lyp = p.t.planes + L.ly + (long long)(ty0 - ST - 1) * L.pitch + (tx0 - ST - 1);
+  const int dx0 = tx0 - ST - 1, dy0 = ty0 - ST - 1; /* image coordinates of D (0, 0) */
+  float *lxp = p.t.planes + L.lx, *lyp = p.t.planes + L.ly;
   for (int i = tid; i < DH * DP; i += 256) {
     const int n = i / DP, d = 2 * (i - n * DP);
-    const float *su = sS + n * SW + d, *sc = su + ST * SW, *sd = su + 2 * ST * SW;
+    const float *su = sS + n * SWS + d, *sc = su + ST * SWS, *sd = su + 2 * ST * SWS;
     const float2 ul = ld2(su), ur = ld2(su + 2 * ST), ll = ld2(sd), lr = ld2(sd + 2 * ST);
     const float2 cl = ld2(sc), cr = ld2(sc + 2 * ST);
     const float2 uc = (ST & 1) ? make_float2(su[ST], su[ST + 1]) : ld2(su + ST);
@@ -75,19 +102,45 @@ __device__ __forceinline__ void akz_detect_interior(const akz_detect_params &p, 
     const float2 b = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
     st2(sX + n * DW + d, a);
     st2(sY + n * DW + d, b);
-    if (n >= ST + 1 && n < ST + 1 + TH) {
-      float *ox = lxp + (long long)n * L.pitch + d, *oy = lyp + (long long)n * L.pitch + d;
-      if (d >= ST + 1 && d < ST + 1 + TW) {
+    const int y = dy0 + n, x = dx0 + d;
+    if (n >= ST + 1 && n < ST + 1 + TH && (!BORDER || y < H)) {
+      float *ox = lxp + (long long)y * L.pitch + x, *oy = lyp + (long long)y * L.pitch + x;
+      if (d >= ST + 1 && d < ST + 1 + TW && (!BORDER || x < W)) {
         ox[0] = a.x;
         oy[0] = b.x;
       }
-      if (d + 1 >= ST + 1 && d + 1 < ST + 1 + TW) {
+      if (d + 1 >= ST + 1 && d + 1 < ST + 1 + TW && (!BORDER || x + 1 < W)) {
         ox[1] = a.y;
         oy[1] = b.y;
       }
     }
   }
   __syncthreads();
+  /* reflect-101 mirrors of Lx, Ly within ST outside the image: columns
+   * first, then whole rows (which covers the corners); the sources are
+   * in-image entries, which these passes do not write */
+  if (BORDER && (dx0 < 0 || dx0 + DW > W)) {
+    for (int i = tid; i < DH * DW; i += 256) {
+      const int n = i / DW, c = i - n * DW, x = dx0 + c;
+      const int xm = x < 0 ? -x : (x >= W && x <= W - 1 + ST ? 2 * W - 2 - x : -1);
+      if (xm >= 0) {
+        sX[n * DW + c] = sX[n * DW + xm - dx0];
+        sY[n * DW + c] = sY[n * DW + xm - dx0];
+      }
+    }
+    __syncthreads();
+  }
+  if (BORDER && (dy0 < 0 || dy0 + DH > H)) {
+    for (int i = tid; i < DH * DW; i += 256) {
+      const int n = i / DW, c = i - n * DW, y = dy0 + n;
+      const int ym = y < 0 ? -y : (y >= H && y <= H - 1 + ST ? 2 * H - 2 - y : -1);
+      if (ym >= 0) {
+        sX[n * DW + c] = sX[(ym - dy0) * DW + c];
+        sY[n * DW + c] = sY[(ym - dy0) * DW + c];
+      }
+    }
+    __syncthreads();
+  }
   /* Hessian determinant on the tile +- 1 (cuda_akaze.cu:673-701): E column e
    * is D column e + ST */
   for (int i = tid; i < EH * EP; i += 256) {
@@ -110,21 +163,21 @@ __device__ __forceinline__ void akz_detect_interior(const akz_detect_params &p, 
     st2(sD + n * EW + e, f2sub(make_float2(lxx.x * lyy.x, lxx.y * lyy.y), make_float2(lyx.x * lyx.x, lyx.y * lyx.y)));
   }
   __syncthreads();
+  /* strict 3x3 maxima above the threshold inside the border (cuda_akaze.cu:727-743);
+   * the border test also rejects tile pixels outside the image */
   const float border = L.border;
-  const int W = L.width, H = L.height;
-#pragma unroll 2
   for (int j = warp; j < TH; j += 8) {
     const int y = ty0 + j;
     const int up_y = (int)((float)y - border + 0.5f) - 1;
     const int down_y = (int)((float)y + border + 0.5f) + 1;
     if (up_y < 0 || down_y >= H) continue;
 #pragma unroll
-    for (int k = 0; k < TW / 32; k++) {
+    for (int k = 0; k < (TW + 31) / 32; k++) {
       const int i = lane + 32 * k;
       const int x = tx0 + i;
       const int left_x = (int)((float)x - border + 0.5f) - 1;
       const int right_x = (int)((float)x + border + 0.5f) + 1;
-      if (left_x < 0 || right_x >= W) continue;
+      if (i >= TW || left_x < 0 || right_x >= W) continue;
       const float *c = sD + (j + 1) * EW + (i + 1);
       const float v = c[0];
       if (v > p.thr && v > c[-EW - 1] && v > c[EW + 1] && v > c[EW - 1] && v > c[-EW + 1] && v > c[-1] && v > c[1] &&
@@ -154,15 +207,24 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   const int dy0 = max(ty0 - st - 1, 0), dy1 = min(ty1 + st + 1, H);
   const int ex0 = max(tx0 - 1, 0), ex1 = min(tx1 + 1, W), ey0 = max(ty0 - 1, 0), ey1 = min(ty1 + 1, H);
   const int sw = sx1 - sx0, dw = dx1 - dx0, ew = ex1 - ex0;
-  const bool interior = tx0 - 2 * st - 1 >= 0 && ty0 - 2 * st - 1 >= 0 && tx0 + TW + 2 * st + 1 <= W &&
-                        ty0 + TH + 2 * st + 1 <= H;
-  if (interior && st >= 2 && st <= 4 && st <= max_step) {
-    if (st == 2)
-      akz_detect_interior<2>(p, L, sm, tx0, ty0);
-    else if (st == 3)
-      akz_detect_interior<3>(p, L, sm, tx0, ty0);
-    else
-      akz_detect_interior<4>(p, L, sm, tx0, ty0);
+  if (st >= 2 && st <= 4 && st <= max_step) {
+    const bool border = tx0 - 2 * st - 1 < 0 || ty0 - 2 * st - 1 < 0 || tx0 + TW + 2 * st + 1 > W ||
+                        ty0 + TH + 2 * st + 1 > H;
+    if (border) {
+      if (st == 2)
+        akz_detect_tile<2, true>(p, L, sm, tx0, ty0);
+      else if (st == 3)
+        akz_detect_tile<3, true>(p, L, sm, tx0, ty0);
+      else
+        akz_detect_tile<4, true>(p, L, sm, tx0, ty0);
+    } else {
+      if (st == 2)
+        akz_detect_tile<2, false>(p, L, sm, tx0, ty0);
+      else if (st == 3)
+        akz_detect_tile<3, false>(p, L, sm, tx0, ty0);
+      else
+        akz_detect_tile<4, false>(p, L, sm, tx0, ty0);
+    }
     return;
   }
   const int SM = (TW + 4 * max_step + 2) * (TH + 4 * max_step + 2);
@@ -556,9 +618,11 @@ __global__ void __launch_bounds__(AKZ_NMS_THREADS) k_nms(akz_nms_params p)
 cudaError_t akz_launch_detect(const akz_detect_params &p, int ntiles, int max_step, cudaStream_t s)
 {
   if (ntiles <= 0) return cudaSuccess;
+  /* Lsmooth region + Lx, Ly regions; the determinant plane reuses the
+   * Lsmooth region */
   const size_t SM = (size_t)(AKZ_DETECT_TW + 4 * max_step + 2) * (AKZ_DETECT_TH + 4 * max_step + 2);
   const size_t DM = (size_t)(AKZ_DETECT_TW + 2 * max_step + 2) * (AKZ_DETECT_TH + 2 * max_step + 2);
-  const size_t smem = (SM + 2 * DM) * sizeof(float); /* the determinant plane reuses the Lsmooth region */
+  const size_t smem = (SM + 2 * DM) * sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(k_detect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k_detect<<<ntiles, 256, smem, s>>>(p, max_step);
