@@ -28,6 +28,25 @@
 
 /* ------------------------------------------------------------------------ */
 
+/* The reference's border test for an extremum at coordinate v of a level of
+ * size n (cuda_akaze.cu:734-740):
+ *   (int)((float)v - border + 0.5f) - 1 >= 0  and  (int)((float)v + border + 0.5f) + 1 < n.
+ * Both sides are monotone in v, so the accepted coordinates form one range;
+ * these return its ends, found with the same float expressions. */
+__device__ __forceinline__ int akz_border_lo(float border)
+{
+  int v = max((int)border - 2, 0);
+  while ((int)((float)v - border + 0.5f) - 1 < 0) v++;
+  return v;
+}
+
+__device__ __forceinline__ int akz_border_hi(float border, int n)
+{
+  int v = min(n - 1 - (int)border + 2, n - 1);
+  while (v >= 0 && (int)((float)v + border + 0.5f) + 1 >= n) v--;
+  return v;
+}
+
 /* k_detect for every tile of a level with derivative step ST (2..4, the steps
  * of the default options): compile-time region sizes, straight-line loops,
  * column pairs with packed FP32x2 additions (products scalar), in the
@@ -164,26 +183,25 @@ __device__ __forceinline__ void akz_detect_tile(const akz_detect_params &p, cons
   }
   __syncthreads();
   /* strict 3x3 maxima above the threshold inside the border (cuda_akaze.cu:727-743);
-   * the border test also rejects tile pixels outside the image */
-  const float border = L.border;
+   * the border range also rejects tile pixels outside the image */
+  const int xlo = akz_border_lo(L.border), xhi = akz_border_hi(L.border, W);
+  const int ylo = akz_border_lo(L.border), yhi = akz_border_hi(L.border, H);
   for (int j = warp; j < TH; j += 8) {
     const int y = ty0 + j;
-    const int up_y = (int)((float)y - border + 0.5f) - 1;
-    const int down_y = (int)((float)y + border + 0.5f) + 1;
-    if (up_y < 0 || down_y >= H) continue;
+    if (y < ylo || y > yhi) continue;
 #pragma unroll
     for (int k = 0; k < (TW + 31) / 32; k++) {
       const int i = lane + 32 * k;
       const int x = tx0 + i;
-      const int left_x = (int)((float)x - border + 0.5f) - 1;
-      const int right_x = (int)((float)x + border + 0.5f) + 1;
-      if (i >= TW || left_x < 0 || right_x >= W) continue;
+      if (i >= TW || x < xlo || x > xhi) continue;
       const float *c = sD + (j + 1) * EW + (i + 1);
       const float v = c[0];
-      if (v > p.thr && v > c[-EW - 1] && v > c[EW + 1] && v > c[EW - 1] && v > c[-EW + 1] && v > c[-1] && v > c[1] &&
-          v > c[EW] && v > c[-EW]) {
-        atomicOr(&p.bitmap[L.bitmap + (long long)y * L.bitmap_pitch + (x >> 5)], 1u << (x & 31));
-        atomicAdd(&p.rowcnt[L.rows + y], 1);
+      if (v > p.thr) {
+        if (v > c[-EW - 1] && v > c[EW + 1] && v > c[EW - 1] && v > c[-EW + 1] && v > c[-1] && v > c[1] &&
+            v > c[EW] && v > c[-EW]) {
+          atomicOr(&p.bitmap[L.bitmap + (long long)y * L.bitmap_pitch + (x >> 5)], 1u << (x & 31));
+          atomicAdd(&p.rowcnt[L.rows + y], 1);
+        }
       }
     }
   }
