@@ -27,6 +27,8 @@ EXPORTS = [
     "akz_batch_detect_describe", "akz_batch_level_plane", "akz_batch_kernel_count", "akz_batch_profile",
     "akz_matcher_create", "akz_matcher_destroy", "akz_matcher_set_stream", "akz_matcher_bfmatch",
     "akz_matcher_bfmatch_device", "akz_matcher_bfmatch_noalloc", "akz_measure_popc_rate",
+    "akz_sg_conv_forward", "akz_sg_conv_backward_data", "akz_sg_conv_backward_weights", "akz_sg_adam",
+    "akz_sg_weight_elems", "akz_sg_infer_level", "akz_sg_mse_grad",
 ]
 
 
@@ -103,6 +105,13 @@ def load():
         "akz_matcher_bfmatch_device": ([P, P, I, P, I, P], I),
         "akz_matcher_bfmatch_noalloc": ([P, I, P, I, P, P], I),
         "akz_measure_popc_rate": ([I, ctypes.POINTER(ctypes.c_double), P], I),
+        "akz_sg_conv_forward": ([P, P, P, P, I, I, I, I, I, I, P], I),
+        "akz_sg_conv_backward_data": ([P, P, P, P, I, I, I, I, I, P], I),
+        "akz_sg_conv_backward_weights": ([P, P, P, P, I, I, I, I, I, P], I),
+        "akz_sg_adam": ([P, P, P, P, I, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, I, P], I),
+        "akz_sg_weight_elems": ([], ctypes.c_size_t),
+        "akz_sg_mse_grad": ([P, P, P, I, ctypes.c_float, P, I, P], I),
+        "akz_sg_infer_level": ([P, P, ctypes.c_size_t, I, I, ctypes.c_float, ctypes.c_float, P, P, P, P, P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -1,0 +1,221 @@
+/*
+ * akz_surrogate_infer.cu - inference of the FED surrogate on a whole level,
+ * BF16 tensor-core implicit GEMM with FP32 accumulation.
+ *
+ * Per level:   im2col  (L_start, g, dt feature) -> A1 [pixel][32] bf16
+ *              (k = tap*3 + channel, 27 used), replicate border;
+ *              conv 1  1x1 GEMM  32 -> 32, ReLU;
+ *              conv 2-4 3x3 implicit GEMM 32 -> 32, ReLU (k = tap*32 + ci);
+ *              conv 5  3x3 32 -> 1 (padded to 8 outputs), then
+ *              L_end = L_start + s_out * (net output).
+ * Every 3x3 layer extends its input by replicate padding at the image border.
+ *
+ * GEMM kernel: a CTA computes a 32 x 4 pixel block (4 warps, one pixel row
+ * each, two m16 tiles per warp) for all outputs.  Its input region (with a
+ * one-pixel halo for 3x3) is staged in shared memory as 64-byte pixel rows
+ * whose four 16-byte channel chunks are XOR-swizzled by (pixel >> 1) & 3, so
+ * the eight rows of an ldmatrix 8x8 read land on distinct banks.  Weights
+ * are staged as [n][k] rows padded by 16 bytes (also conflict-free).
+ * mma.sync m16n8k16 bf16 -> f32.
+ */
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/akaze_gb300.h"
+
+akz_status akz_report(akz_status s, const char *msg);
+
+struct akz_sg_level {
+  const float *l0, *g;
+  long long pitch;
+  int W, H;
+  float dtf, s_out;
+  float *out;
+};
+
+__device__ __forceinline__ int sg_clamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__global__ void k_sg_im2col(akz_sg_level lv, __nv_bfloat16 *act)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= lv.W) return;
+  __align__(16) __nv_bfloat16 v[32];
+#pragma unroll
+  for (int t = 0; t < 9; t++) {
+    const int yy = sg_clamp(y + t / 3 - 1, 0, lv.H - 1), xx = sg_clamp(x + t % 3 - 1, 0, lv.W - 1);
+    const long long o = (long long)yy * lv.pitch + xx;
+    v[3 * t] = __float2bfloat16_rn(lv.l0[o]);
+    v[3 * t + 1] = __float2bfloat16_rn(lv.g[o]);
+    v[3 * t + 2] = __float2bfloat16_rn(lv.dtf);
+  }
+#pragma unroll
+  for (int k = 27; k < 32; k++) v[k] = __float2bfloat16_rn(0.0f);
+  uint4 *dst = (uint4 *)(act + ((long long)y * lv.W + x) * 32);
+  const uint4 *src = (const uint4 *)v;
+#pragma unroll
+  for (int c = 0; c < 4; c++) dst[c] = src[c];
+}
+
+__device__ __forceinline__ void sg_ldsm_x4(unsigned int (&r)[4], const void *p)
+{
+  const unsigned int a = (unsigned int)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
+__device__ __forceinline__ void sg_ldsm_x2(unsigned int (&r)[2], const void *p)
+{
+  const unsigned int a = (unsigned int)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0, %1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(a));
+}
+
+__device__ __forceinline__ void sg_mma(float (&d)[4], const unsigned int (&a)[4], unsigned int b0, unsigned int b1)
+{
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+               "{%0, %1, %2, %3};"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+#define SG_BX 32
+#define SG_BY 4
+
+/* NTAPS 1 (1x1) or 9 (3x3); NT n8 output tiles (4 -> 32 outputs, 1 -> 8);
+ * FINAL: write L_start + s_out * output channel 0 to the level plane,
+ * otherwise bias + ReLU -> bf16 NHWC. */
+template <int NTAPS, int NT, bool FINAL>
+__global__ void __launch_bounds__(128) k_sg_conv_mma(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ wt,
+                                                     const float *__restrict__ bias, __nv_bfloat16 *__restrict__ out,
+                                                     akz_sg_level lv)
+{
+  constexpr int K = NTAPS * 32, KS = K + 8; /* weight row stride (bf16): 16-byte pad */
+  constexpr int HALO = NTAPS == 9 ? 1 : 0;
+  constexpr int RX = SG_BX + 2 * HALO, RY = SG_BY + 2 * HALO;
+  __shared__ __align__(16) __nv_bfloat16 sW[NT * 8 * KS];
+  __shared__ __align__(16) unsigned char sA[RX * RY * 64];
+  __shared__ float sBias[NT * 8];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int W = lv.W, H = lv.H;
+  const int x0 = blockIdx.x * SG_BX, y0 = blockIdx.y * SG_BY;
+  for (int i = tid; i < NT * 8 * (K / 8); i += 128) {
+    const int n = i / (K / 8), c = i - n * (K / 8);
+    *(uint4 *)(sW + n * KS + c * 8) = *(const uint4 *)(wt + n * K + c * 8);
+  }
+  if (tid < NT * 8) sBias[tid] = bias[tid];
+  for (int i = tid; i < RX * RY * 4; i += 128) {
+    const int q = i >> 2, c = i & 3;
+    const int ry = q / RX, rx = q - ry * RX;
+    const int yy = sg_clamp(y0 - HALO + ry, 0, H - 1), xx = sg_clamp(x0 - HALO + rx, 0, W - 1);
+    const uint4 v = *(const uint4 *)(in + ((long long)yy * W + xx) * 32 + c * 8);
+    *(uint4 *)(sA + q * 64 + ((c ^ ((q >> 1) & 3)) << 4)) = v;
+  }
+  __syncthreads();
+
+  float acc[2][NT][4];
+#pragma unroll
+  for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+    for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[mt][nt][j] = 0.0f;
+
+#pragma unroll 1
+  for (int t = 0; t < NTAPS; t++) {
+    const int dy = NTAPS == 9 ? t / 3 : 0, dx = NTAPS == 9 ? t % 3 : 0;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      unsigned int a[2][4];
+#pragma unroll
+      for (int mt = 0; mt < 2; mt++) {
+        const int q = (warp + dy) * RX + mt * 16 + (lane & 15) + dx;
+        const int c = h * 2 + (lane >> 4);
+        sg_ldsm_x4(a[mt], sA + q * 64 + ((c ^ ((q >> 1) & 3)) << 4));
+      }
+      const int kb = t * 32 + h * 16;
+      if (NT >= 2) {
+#pragma unroll
+        for (int np = 0; np < NT / 2; np++) {
+          unsigned int b[4];
+          const int n = np * 16 + ((lane >> 4) & 1) * 8 + (lane & 7);
+          sg_ldsm_x4(b, sW + n * KS + kb + ((lane >> 3) & 1) * 8);
+#pragma unroll
+          for (int mt = 0; mt < 2; mt++) {
+            sg_mma(acc[mt][2 * np], a[mt], b[0], b[1]);
+            sg_mma(acc[mt][2 * np + 1], a[mt], b[2], b[3]);
+          }
+        }
+      } else {
+        unsigned int b[2];
+        const int n = lane & 7;
+        sg_ldsm_x2(b, sW + n * KS + kb + ((lane >> 3) & 1) * 8);
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) sg_mma(acc[mt][0], a[mt], b[0], b[1]);
+      }
+    }
+  }
+
+  const int y = y0 + warp;
+  if (y >= H) return;
+#pragma unroll
+  for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+      const int x = x0 + mt * 16 + (lane >> 2) + half * 8;
+      if (x >= W) continue;
+      if (FINAL) {
+        if ((lane & 3) == 0) {
+          const long long o = (long long)y * lv.pitch + x;
+          lv.out[o] = lv.l0[o] + lv.s_out * (acc[mt][0][half * 2] + sBias[0]);
+        }
+      } else {
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++) {
+          const int ch = nt * 8 + (lane & 3) * 2;
+          const float v0 = fmaxf(acc[mt][nt][half * 2] + sBias[ch], 0.0f);
+          const float v1 = fmaxf(acc[mt][nt][half * 2 + 1] + sBias[ch + 1], 0.0f);
+          *(__nv_bfloat162 *)(out + ((long long)y * W + x) * 32 + ch) = __floats2bfloat162_rn(v0, v1);
+        }
+      }
+    }
+}
+
+/* Packed weights (bf16): layer 1 [32][32], layers 2-4 [32][288], layer 5
+ * [8][288] (rows 1-7 zero); biases (f32): 4 x 32 + 8. */
+#define SG_W1 (32 * 32)
+#define SG_W3 (32 * 288)
+#define SG_W5 (8 * 288)
+
+extern "C" AKZ_API size_t akz_sg_weight_elems(void) { return SG_W1 + 3 * SG_W3 + SG_W5; }
+
+extern "C" AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pitch, int width, int height,
+                                                 float dt_feature, float s_out, const void *weights_bf16,
+                                                 const float *biases, void *scratch, float *out, void *stream)
+{
+  if (!l0 || !g || !weights_bf16 || !biases || !scratch || !out || width < 1 || height < 1 || pitch < (size_t)width)
+    return akz_report(AKZ_ERR_INVALID_ARG, "akz_sg_infer_level: bad arguments");
+  if (((uintptr_t)weights_bf16 & 15) || ((uintptr_t)scratch & 15))
+    return akz_report(AKZ_ERR_INVALID_ARG, "akz_sg_infer_level: weights and scratch must be 16-byte aligned");
+  cudaStream_t s = (cudaStream_t)stream;
+  akz_sg_level lv;
+  lv.l0 = l0;
+  lv.g = g;
+  lv.pitch = (long long)pitch;
+  lv.W = width;
+  lv.H = height;
+  lv.dtf = dt_feature;
+  lv.s_out = s_out;
+  lv.out = out;
+  const __nv_bfloat16 *w = (const __nv_bfloat16 *)weights_bf16;
+  __nv_bfloat16 *a0 = (__nv_bfloat16 *)scratch, *a1 = a0 + (size_t)width * height * 32;
+  k_sg_im2col<<<dim3((width + 127) / 128, height), 128, 0, s>>>(lv, a0);
+  const dim3 grid((width + SG_BX - 1) / SG_BX, (height + SG_BY - 1) / SG_BY);
+  k_sg_conv_mma<1, 4, false><<<grid, 128, 0, s>>>(a0, w, biases, a1, lv);
+  k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a1, w + SG_W1, biases + 32, a0, lv);
+  k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a0, w + SG_W1 + SG_W3, biases + 64, a1, lv);
+  k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a1, w + SG_W1 + 2 * SG_W3, biases + 96, a0, lv);
+  k_sg_conv_mma<9, 1, true><<<grid, 128, 0, s>>>(a0, w + SG_W1 + 3 * SG_W3, biases + 128, nullptr, lv);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
+  return AKZ_OK;
+}

@@ -227,6 +227,43 @@ AKZ_API akz_status akz_matcher_bfmatch_noalloc(const uint8_t *query64, int nq, c
  * *triples_per_s / 16.  Synchronises stream; allocates 4 bytes. */
 AKZ_API akz_status akz_measure_popc_rate(int iters, double *triples_per_s, void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* Learned FED surrogate (no counterpart in the reference; it replaces the
+ * FED cycle of AKAZE.cpp:244-270 for octaves >= 1 when enabled).  A 5-layer
+ * 3x3 convolutional net 3 -> 32 -> 32 -> 32 -> 32 -> 1 with ReLU maps a
+ * level's starting image, its conductance and a feature of the level's FED
+ * time span to the residual L_end - L_start, scaled by s_out.
+ *
+ * Training kernels, FP32 NCHW tensors on the device, valid convolutions,
+ * weights [cout][cin][3][3], 1 <= cin, cout <= 32: */
+AKZ_API akz_status akz_sg_conv_forward(const float *in, const float *w, const float *bias, float *out, int nb, int cin,
+                                      int cout, int hi, int wi, int relu, void *stream);
+/* din = (mask > 0) * dL/d(in); mask NULL for no ReLU factor */
+AKZ_API akz_status akz_sg_conv_backward_data(const float *dout, const float *w, const float *mask, float *din, int nb,
+                                            int cin, int cout, int hi, int wi, void *stream);
+/* dw, db overwritten with the gradients summed over the batch */
+AKZ_API akz_status akz_sg_conv_backward_weights(const float *in, const float *dout, float *dw, float *db, int nb, int cin,
+                                               int cout, int hi, int wi, void *stream);
+AKZ_API akz_status akz_sg_adam(float *param, const float *grad, float *m, float *v, int n, float lr, float beta1,
+                              float beta2, float eps, int step, void *stream);
+/* dout = scale * (out - target); loss_parts[0 .. nparts-1] receive partial
+ * sums of (out - target)^2 */
+AKZ_API akz_status akz_sg_mse_grad(const float *out, const float *target, float *dout, int n, float scale,
+                                  float *loss_parts, int nparts, void *stream);
+
+/* Inference on one level plane (BF16 tensor cores, FP32 accumulation),
+ * replicate border: out = l0 + s_out * net(l0, g, dt_feature).  l0, g, out
+ * are float planes with row pitch `pitch` elements; weights_bf16 holds
+ * akz_sg_weight_elems() bf16 values (layer 1 [32][32] over the im2col index
+ * tap*3 + channel, layers 2-4 [32][288] over tap*32 + ci, layer 5 [8][288]
+ * with rows 1-7 zero), biases 4 x 32 + 8 floats; scratch holds
+ * 2 * width * height * 64 bytes.  Weights and scratch 16-byte aligned.
+ * Asynchronous on stream. */
+AKZ_API size_t akz_sg_weight_elems(void);
+AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pitch, int width, int height,
+                                     float dt_feature, float s_out, const void *weights_bf16, const float *biases,
+                                     void *scratch, float *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
