@@ -288,6 +288,27 @@ class Batch:
         check(self._lib.akz_batch_kernel_count(self._h, ctypes.byref(n)))
         return n.value
 
+    def set_surrogate(self, params=None, first_octave=1, check_tol=0.0, s_out=None):
+        """Use the learned FED surrogate (FP32 params of akaze_gb300.surrogate,
+        or None to switch it off) for the levels of octave >= first_octave."""
+        if params is None:
+            check(self._lib.akz_batch_set_surrogate(self._h, None, None, ctypes.c_float(0), 1, ctypes.c_float(0)))
+            return
+        from . import surrogate
+        blob, biases = surrogate.pack_inference(params)
+        blob = np.ascontiguousarray(blob, np.uint16)
+        biases = np.ascontiguousarray(biases, np.float32)
+        check(self._lib.akz_batch_set_surrogate(self._h, _ptr(blob), _ptr(biases),
+                                                ctypes.c_float(surrogate.S_OUT if s_out is None else s_out),
+                                                int(first_octave), ctypes.c_float(check_tol)))
+
+    def surrogate_errors(self):
+        n = ctypes.c_int()
+        check(self._lib.akz_batch_surrogate_errors(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, np.float32)
+        check(self._lib.akz_batch_surrogate_errors(self._h, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
     def profile(self):
         """Per-stage device ms of one run (contrast, level 0, levels, detector,
         scan+extract, suppression, orientation+M-LDB)."""

@@ -28,7 +28,8 @@ EXPORTS = [
     "akz_matcher_create", "akz_matcher_destroy", "akz_matcher_set_stream", "akz_matcher_bfmatch",
     "akz_matcher_bfmatch_device", "akz_matcher_bfmatch_noalloc", "akz_measure_popc_rate",
     "akz_sg_conv_forward", "akz_sg_conv_backward_data", "akz_sg_conv_backward_weights", "akz_sg_adam",
-    "akz_sg_weight_elems", "akz_sg_infer_level", "akz_sg_mse_grad",
+    "akz_sg_weight_elems", "akz_sg_infer_level", "akz_sg_mse_grad", "akz_batch_set_surrogate",
+    "akz_batch_surrogate_errors",
 ]
 
 
@@ -111,6 +112,8 @@ def load():
         "akz_sg_adam": ([P, P, P, P, I, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, I, P], I),
         "akz_sg_weight_elems": ([], ctypes.c_size_t),
         "akz_sg_mse_grad": ([P, P, P, I, ctypes.c_float, P, I, P], I),
+        "akz_batch_set_surrogate": ([P, P, P, ctypes.c_float, I, ctypes.c_float], I),
+        "akz_batch_surrogate_errors": ([P, P, I, IP], I),
         "akz_sg_infer_level": ([P, P, ctypes.c_size_t, I, I, ctypes.c_float, ctypes.c_float, P, P, P, P, P], I),
     }
     for name, (args, res) in sig.items():

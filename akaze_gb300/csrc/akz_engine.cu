@@ -24,6 +24,11 @@
 #include "akz_kernels.h"
 
 cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit, cudaStream_t s);
+cudaError_t akz_sg_maxdiff(const float *a, const float *b, int pitch, int width, int height, float *slot, cudaStream_t s);
+extern "C" akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pitch, int width, int height,
+                                         float dt_feature, float s_out, const void *weights_bf16, const float *biases,
+                                         void *scratch, float *out, void *stream);
+extern "C" size_t akz_sg_weight_elems(void);
 int akz_match_splits(int nq, int nt, int nsm);
 size_t akz_match_partial_bytes(int nq, int nsplit);
 
@@ -248,6 +253,16 @@ struct akz_batch {
   int detect_off = 0, detect_n = 0, detect_tiles = 0;
   int extract_off = 0, extract_n = 0, extract_rows = 0;
   std::vector<std::vector<akz_fed_launch>> fed;  /* per level index */
+  /* learned surrogate (akz_batch_set_surrogate): per level, the zero-step
+   * launch that forms Lsmooth, the conductance and the start image, and the
+   * plain chunks of image 0 into the check plane */
+  std::vector<akz_fed_launch> sg_prep;
+  std::vector<std::vector<akz_fed_launch>> sg_check;
+  int sg_on = 0, sg_first_octave = 1;
+  float sg_s_out = 0.0f, sg_tol = 0.0f;
+  std::vector<float> sg_dtf;
+  void *d_sg_w = nullptr, *d_sg_scratch = nullptr;
+  float *d_sg_b = nullptr, *d_sg_chk = nullptr, *d_sg_err = nullptr;
   std::vector<akz_area_launch> area;              /* per level index (nsegs 0 when none) */
   std::vector<akz_area_seg> area_segs;
   std::vector<int> area_start, area_si;
@@ -309,6 +324,8 @@ static void akz_batch_free(akz_batch *b)
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->arena) cudaFree(b->arena);
+  for (void *q : {(void *)b->d_sg_w, b->d_sg_scratch, (void *)b->d_sg_b, (void *)b->d_sg_chk, (void *)b->d_sg_err})
+    if (q) cudaFree(q);
   if (b->f32) cudaFree(b->f32);
   if (b->h_stats) cudaFreeHost(b->h_stats);
   for (auto &e : b->ev)
@@ -457,6 +474,8 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
 
   b->fed.resize(b->maxlev);
   b->area.resize(b->maxlev);
+  b->sg_prep.resize(b->maxlev);
+  b->sg_check.resize(b->maxlev);
   for (int l = 1; l < b->maxlev; l++) {
     const int nsteps = (int)b->tau[l].size();
     const int nch = std::max(1, (nsteps + 7) / 8);
@@ -506,7 +525,42 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
       for (int k = 0; k < steps; k++) fl.p.h[k] = 0.5f * b->tau[l][done + k];
       done += steps;
       b->fed[l].push_back(fl);
+      /* the same chunk for image 0 alone, the last one into the check plane */
+      akz_fed_launch cl = fl;
+      cl.seg_off = (int)b->segs.size();
+      cl.ntiles = 0;
+      if (b->im[0].nlev > l) {
+        const akz_geo &g = b->geo[0][l], &gp = b->geo[0][l - 1];
+        int src = 0;
+        if (g.octave > gp.octave) src = (gp.w == 2 * g.w && gp.h == 2 * g.h) ? 1 : 2;
+        add_tiles(b->im[0].first_level + l, g.w, g.h, cl.tw, cl.th, src, cl.ntiles);
+      }
+      cl.nsegs = (int)b->segs.size() - cl.seg_off;
+      if (c == nch - 1) cl.p.dst = 3;
+      b->sg_check[l].push_back(cl);
     }
+    /* zero FED steps over 128 x 40 tiles: Lsmooth, the conductance (kept)
+     * and the start image in Lt */
+    akz_fed_launch pl;
+    memset(&pl, 0, sizeof(pl));
+    pl.tw = 128;
+    pl.th = 40;
+    pl.seg_off = (int)b->segs.size();
+    for (int i = 0; i < n; i++) {
+      if (b->im[i].nlev <= l) continue;
+      const akz_geo &g = b->geo[i][l], &gp = b->geo[i][l - 1];
+      int src = 0;
+      if (g.octave > gp.octave) src = (gp.w == 2 * g.w && gp.h == 2 * g.h) ? 1 : 2;
+      add_tiles(b->im[i].first_level + l, g.w, g.h, pl.tw, pl.th, src, pl.ntiles);
+    }
+    pl.nsegs = (int)b->segs.size() - pl.seg_off;
+    pl.p.steps = 0;
+    pl.p.first = 1;
+    pl.p.dst = 0;
+    pl.p.write_g = 1;
+    pl.p.diffusivity = opt->diffusivity;
+    for (int k = 0; k < 5; k++) pl.p.taps1[k] = b->taps1[k];
+    b->sg_prep[l] = pl;
   }
   b->detect_off = (int)b->segs.size();
   for (int i = 0; i < n; i++)
@@ -604,6 +658,7 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
 static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe = nullptr)
 {
   const akz_tables t = akz_make_tables(b);
+  if (b->sg_on) CK(cudaMemsetAsync(b->d_sg_err, 0, (size_t)b->maxlev * sizeof(float), s));
   CK(cudaMemsetAsync(b->d_stats, 0, (size_t)b->nimg * sizeof(akz_image_stats), s));
   CK(cudaMemsetAsync(b->d_hist, 0, (size_t)b->nimg * b->opt.kcontrast_nbins * sizeof(unsigned int), s));
   akz_contrast_params cp;
@@ -638,13 +693,40 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe 
       ap.alpha = b->d_area_alpha;
       CK(akz_launch_area(ap, b->area[l].maxw, b->area[l].maxh, s));
     }
-    for (auto &fl : b->fed[l]) {
+    auto run_fed = [&](const akz_fed_launch &fl, const float *gate) -> cudaError_t {
+      if (fl.ntiles <= 0) return cudaSuccess;
       akz_fed_params p = fl.p;
       p.t = t;
       p.segs = b->d_segs + fl.seg_off;
       p.nsegs = fl.nsegs;
       p.kc = b->d_kc;
-      CK(akz_launch_fed(p, fl.ntiles, fl.tw, fl.th, s));
+      p.chk = b->d_sg_chk;
+      p.gate = gate;
+      p.gate_tol = b->sg_tol;
+      return akz_launch_fed(p, fl.ntiles, fl.tw, fl.th, s);
+    };
+    if (!b->sg_on || l / b->opt.nsublevels < b->sg_first_octave) {
+      for (auto &fl : b->fed[l]) CK(run_fed(fl, nullptr));
+      continue;
+    }
+    /* learned surrogate: start image, Lsmooth and conductance, then the net
+     * in place on every image; with a tolerance, image 0 is also run through
+     * the plain chunks into the check plane, compared, and the plain launches
+     * of the level follow behind a device-side gate on that comparison */
+    CK(run_fed(b->sg_prep[l], nullptr));
+    for (int i = 0; i < b->nimg; i++) {
+      if (b->im[i].nlev <= l) continue;
+      const akz_level_desc &L = b->lv[b->im[i].first_level + l];
+      float *lt = b->planes + L.lt;
+      const akz_status st = akz_sg_infer_level(lt, b->planes + b->im[i].g, (size_t)L.pitch, L.width, L.height,
+                                               b->sg_dtf[l], b->sg_s_out, b->d_sg_w, b->d_sg_b, b->d_sg_scratch, lt, s);
+      if (st != AKZ_OK) return st;
+    }
+    if (b->sg_tol > 0.0f && b->im[0].nlev > l) {
+      for (auto &cl : b->sg_check[l]) CK(run_fed(cl, nullptr));
+      const akz_level_desc &L0 = b->lv[b->im[0].first_level + l];
+      CK(akz_sg_maxdiff(b->d_sg_chk, b->planes + L0.lt, L0.pitch, L0.width, L0.height, b->d_sg_err + l, s));
+      for (auto &fl : b->fed[l]) CK(run_fed(fl, b->d_sg_err + l));
     }
   }
   return AKZ_OK;
@@ -1281,6 +1363,73 @@ AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *q64
   if (nq == 0) return AKZ_OK;
   if (!q64 || !out || (nt > 0 && !t64)) return akz_fail(AKZ_ERR_INVALID_ARG, "NULL matcher buffer");
   return akz_match_device(m, q64, nq, t64, nt, out);
+}
+
+/* Learned FED surrogate for the levels of octave >= first_octave
+ * (weights_bf16 NULL turns it off). */
+AKZ_API akz_status akz_batch_set_surrogate(akz_batch *b, const uint16_t *weights_bf16, const float *biases, float s_out,
+                                           int first_octave, float check_tol)
+{
+  AKZ_GUARD(b);
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  if (!weights_bf16) {
+    b->sg_on = 0;
+    return AKZ_OK;
+  }
+  if (!biases || first_octave < 1 || !(s_out == s_out) || !(check_tol >= 0.0f))
+    return akz_fail(AKZ_ERR_INVALID_ARG, "akz_batch_set_surrogate: bad arguments");
+  size_t scratch = 16, chk = 1;
+  for (int i = 0; i < b->nimg; i++)
+    for (int l = 0; l < b->im[i].nlev; l++) {
+      if (l / b->opt.nsublevels < first_octave) continue;
+      const akz_level_desc &L = b->lv[b->im[i].first_level + l];
+      scratch = std::max(scratch, (size_t)2 * L.width * L.height * 64);
+      if (i == 0) chk = std::max(chk, (size_t)L.pitch * L.height);
+    }
+  const size_t nw = akz_sg_weight_elems();
+  if (!b->d_sg_w) {
+    CK(cudaMalloc(&b->d_sg_w, nw * 2));
+    CK(cudaMalloc((void **)&b->d_sg_b, 136 * sizeof(float)));
+    CK(cudaMalloc((void **)&b->d_sg_err, (size_t)b->maxlev * sizeof(float)));
+    CK(cudaMalloc(&b->d_sg_scratch, scratch));
+    CK(cudaMalloc((void **)&b->d_sg_chk, chk * sizeof(float)));
+  }
+  CK(cudaMemcpy(b->d_sg_w, weights_bf16, nw * 2, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_sg_b, biases, 136 * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemset(b->d_sg_err, 0, (size_t)b->maxlev * sizeof(float)));
+  b->sg_dtf.assign(b->maxlev, 0.0f);
+  for (int l = 1; l < b->maxlev; l++) {
+    int i = 0;
+    while (i < b->nimg && b->im[i].nlev <= l) i++;
+    if (i == b->nimg) continue;
+    const double e1 = b->geo[i][l].esigma, e0 = b->geo[i][l - 1].esigma;
+    b->sg_dtf[l] = (float)(0.25 * std::log2(std::max(0.5 * (e1 * e1 - e0 * e0), 1e-12)));
+  }
+  b->sg_on = 1;
+  b->sg_first_octave = first_octave;
+  b->sg_s_out = s_out;
+  b->sg_tol = check_tol;
+  return AKZ_OK;
+}
+
+/* Per level, the max |surrogate - plain FED| of image 0 in the last run
+ * (0 for levels without a check); a level above the tolerance fell back to
+ * plain FED for every image. */
+AKZ_API akz_status akz_batch_surrogate_errors(akz_batch *b, float *err, int cap, int *nlevels)
+{
+  AKZ_GUARD(b);
+  if (nlevels) *nlevels = b->maxlev;
+  if (!err || cap <= 0) return AKZ_OK;
+  if (!b->sg_on || !b->d_sg_err) {
+    for (int l = 0; l < cap; l++) err[l] = 0.0f;
+    return AKZ_OK;
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  CK(cudaMemcpy(err, b->d_sg_err, (size_t)std::min(cap, b->maxlev) * sizeof(float), cudaMemcpyDeviceToHost));
+  return AKZ_OK;
 }
 
 } /* extern "C" */

@@ -51,11 +51,14 @@ struct akz_fed_params {
   int steps;          /* FED steps in this launch */
   int first;          /* 1: start from the predecessor (copy / 2x half-sample / prepared T2) */
   int src;            /* first: 0 predecessor Lt, 1 2x half-sample of it, 2 prepared T2; else 1 T1, 2 T2 */
-  int dst;            /* 0 Lt of the level, 1 T1, 2 T2 */
+  int dst;            /* 0 Lt of the level, 1 T1, 2 T2, 3 chk */
   int write_g;        /* store the conductance for later launches */
   int diffusivity;
   float taps1[5];
   float h[AKZ_MAX_CHUNK]; /* 0.5 * tau per step */
+  float *chk;         /* dst 3: a plane with the level's pitch */
+  const float *gate;  /* non-NULL: the launch runs only if !(*gate <= gate_tol) */
+  float gate_tol;
 };
 
 /* INTER_AREA tables of one octave start: start[] indices are absolute into

@@ -473,6 +473,7 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   extern __shared__ float sm[];
   constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
   constexpr int PS = RW + 6, SS = RW + 2; /* strides of the input and smoothing regions */
+  if (p.gate && *p.gate <= p.gate_tol) return; /* a gated fallback that is not needed */
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
   const akz_tile_seg sg = p.segs[si];
@@ -585,7 +586,7 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
     nxt = t;
   }
   /* tile interior from registers */
-  float *out = planes + (p.dst == 0 ? L.lt : (p.dst == 1 ? I.t1 : I.t2));
+  float *out = p.dst == 3 ? p.chk : planes + (p.dst == 0 ? L.lt : (p.dst == 1 ? I.t1 : I.t2));
   const bool w0 = x0 >= tx0 && x0 < tx1, w1 = x0 + 1 >= tx0 && x0 + 1 < tx1;
 #pragma unroll
   for (int r = 0; r < RB; r++) {
@@ -656,7 +657,7 @@ cudaError_t akz_launch_gauss0(const akz_gauss_params &p, int ntiles, cudaStream_
 cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int, int, cudaStream_t s)
 {
   if (ntiles <= 0) return cudaSuccess;
-  if (p.steps < 1 || p.steps > 8) return cudaErrorInvalidValue;
+  if (p.steps < 0 || p.steps > 8) return cudaErrorInvalidValue; /* 0: Lsmooth, conductance and the start image only */
   const size_t smem = akz_fed_smem_bytes(0, 0, p.steps, p.first);
   cudaError_t e = cudaFuncSetAttribute(k_fed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

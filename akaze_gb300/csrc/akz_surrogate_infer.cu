@@ -21,6 +21,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "../../include/akaze_gb300.h"
 
 akz_status akz_report(akz_status s, const char *msg);
@@ -218,4 +220,27 @@ extern "C" AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
   return AKZ_OK;
+}
+
+/* max |a - b| over a level plane into *slot (non-negative float bits, so an
+ * integer atomicMax orders them); NaN or infinity counts as infinity */
+__global__ void k_sg_maxdiff(const float *a, const float *b, int pitch, int W, int H, float *slot)
+{
+  float m = 0.0f;
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < (long long)W * H; i += (long long)gridDim.x * 256) {
+    const long long o = (i / W) * pitch + i % W;
+    float d = fabsf(a[o] - b[o]);
+    if (!(d <= 3.0e38f)) d = __int_as_float(0x7f800000);
+    m = fmaxf(m, d);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax((int *)slot, __float_as_int(m));
+}
+
+cudaError_t akz_sg_maxdiff(const float *a, const float *b, int pitch, int width, int height, float *slot, cudaStream_t s)
+{
+  const long long n = (long long)width * height;
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 1024);
+  k_sg_maxdiff<<<blocks, 256, 0, s>>>(a, b, pitch, width, height, slot);
+  return cudaGetLastError();
 }

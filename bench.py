@@ -49,10 +49,16 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: --batch images, one graph-less run of every stage, no timing line")
-    ap.add_argument("--workload", default="batch1080p", choices=["batch1080p", "single640", "uneven64", "matcher"],
+    ap.add_argument("--weights", default=os.path.join(ROOT, "akaze_gb300", "surrogate_weights.npz"),
+                    help="surrogate4k: trained surrogate weights (python -m akaze_gb300.surrogate train)")
+    ap.add_argument("--check-tol", type=float, default=2e-3,
+                    help="surrogate4k: per-level tolerance of the surrogate against plain FED before it falls back")
+    ap.add_argument("--workload", default="batch1080p",
+                    choices=["batch1080p", "single640", "uneven64", "matcher", "surrogate4k"],
                     help="batch1080p: the headline line (default); single640: one 640x480 pair, GPU and CPU; "
                          "uneven64: 64 images of uneven sizes, images/s and per-image latency; "
-                         "matcher: 2-NN sweep N=M 1024..131072, Gmatch/s against the popc roofline")
+                         "matcher: 2-NN sweep N=M 1024..131072, Gmatch/s against the popc roofline; "
+                         "surrogate4k: 3840x2160, 6x4 levels, plain FED vs the learned surrogate")
     return ap.parse_args()
 
 
@@ -372,13 +378,99 @@ def workload_matcher(args):
     return 0
 
 
+def repeatability(kp_ref, d_ref, kp, d, px=0.5):
+    """Fraction of reference keypoints with a keypoint at the same level
+    (class_id) within px, and the Hamming distances of those pairs'
+    descriptors."""
+    hits, ham = 0, []
+    for c in np.unique(kp_ref["class_id"]):
+        ri = np.nonzero(kp_ref["class_id"] == c)[0]
+        si = np.nonzero(kp["class_id"] == c)[0]
+        if len(si) == 0:
+            continue
+        order = si[np.argsort(kp["x"][si])]
+        xs = kp["x"][order]
+        for r in ri:
+            lo, hi = np.searchsorted(xs, kp_ref["x"][r] - px), np.searchsorted(xs, kp_ref["x"][r] + px, side="right")
+            cand = order[lo:hi]
+            if len(cand) == 0:
+                continue
+            dd = np.hypot(kp["x"][cand] - kp_ref["x"][r], kp["y"][cand] - kp_ref["y"][r])
+            j = int(np.argmin(dd))
+            if dd[j] <= px:
+                hits += 1
+                ham.append(int(np.unpackbits(d_ref[r] ^ d[cand[j]]).sum()))
+    n = len(kp_ref)
+    ham = np.array(ham) if ham else np.zeros(0)
+    return {"repeatability": hits / n if n else 1.0, "matched": hits, "reference": n,
+            "hamming_mean": float(ham.mean()) if ham.size else 0.0,
+            "hamming_le2": float((ham <= 2).mean()) if ham.size else 1.0}
+
+
+def workload_surrogate4k(args):
+    """3840x2160 with 6 octaves x 4 sublevels: plain FED, the learned
+    surrogate for octaves >= 1 alone, and with its per-level check against
+    plain FED on image 0 and fallback."""
+    torch, stream = _torch_stream()
+    import akaze_gb300 as akz
+    from akaze_gb300 import surrogate as sg
+    from akaze_gb300 import synth
+    if not os.path.exists(args.weights):
+        print(json.dumps({"workload": "surrogate4k", "unavailable": f"no trained weights at {args.weights}"}))
+        return 0
+    params = sg.load_params(args.weights)
+    W, H, B = 3840, 2160, min(args.batch, 8)
+    imgs = [synth.synth_image(9000 + i, W, H) for i in range(B)]
+    opt = akz.AKAZEOptions(omax=6)
+    res = {}
+    for mode, tol in (("plain", None), ("surrogate", 0.0), ("surrogate_checked", args.check_tol)):
+        b = akz.Batch(opt, [(W, H)] * B)
+        b.set_stream(stream.cuda_stream)
+        b.upload(imgs)
+        if tol is not None:
+            b.set_surrogate(params, first_octave=1, check_tol=tol)
+        for _ in range(max(args.warmup, 3)):
+            b.run()
+        ms = _event_ms(torch, stream, b.run, max(3, min(args.steps, 10)))
+        out = {"ms_per_batch": ms, "images_per_s": B * 1000.0 / ms, "stage_ms": [float(x) for x in b.profile()],
+               "results": [b.results(i) for i in range(B)]}
+        if tol is None:
+            sizes = [(int(W / 2 ** o), int(H / 2 ** o)) for o in range(6) for _ in range(4)]
+            out["level_max_abs_image0"] = [float(np.abs(b.plane(0, l, shape=(h, w))).max()) for l, (w, h) in enumerate(sizes)]
+        if tol:
+            e = b.surrogate_errors()
+            out["level_max_err_image0"] = [float(x) for x in e]
+            out["levels_fallen_back"] = int(np.sum(~(e <= tol)))
+        res[mode] = out
+        b.close()
+    line = {"workload": "surrogate4k", "config": f"{B} synthetic 3840x2160 u8, 6 octaves x 4 sublevels, surrogate on "
+            "octaves >= 1 (BF16 tensor-core net, 5 layers x 32 channels)", "check_tol": args.check_tol}
+    for mode, out in res.items():
+        r = {k: v for k, v in out.items() if k != "results"}
+        if mode != "plain":
+            for tag, lim in (("", 24), ("_octaves0to4", 20)):
+                reps = []
+                for i in range(B):
+                    (kr, dr), (k, d) = res["plain"]["results"][i], out["results"][i]
+                    mr, m = kr["class_id"] < lim, k["class_id"] < lim
+                    reps.append(repeatability(kr[mr], dr[mr], k[m], d[m]))
+                r["repeatability" + tag] = float(np.mean([x["repeatability"] for x in reps]))
+                r["hamming_mean" + tag] = float(np.mean([x["hamming_mean"] for x in reps]))
+                r["hamming_le2" + tag] = float(np.mean([x["hamming_le2"] for x in reps]))
+            r["speedup_vs_plain"] = res["plain"]["ms_per_batch"] / out["ms_per_batch"]
+        r["keypoints"] = [int(len(k)) for k, _ in out["results"]]
+        line[mode] = r
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "batch1080p":
-        return {"single640": workload_single640, "uneven64": workload_uneven64,
-                "matcher": workload_matcher}[args.workload](args)
+        return {"single640": workload_single640, "uneven64": workload_uneven64, "matcher": workload_matcher,
+                "surrogate4k": workload_surrogate4k}[args.workload](args)
     ws, rank, local = dist_setup(args)
     import torch
     torch.cuda.set_device(local)

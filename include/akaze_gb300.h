@@ -260,6 +260,20 @@ AKZ_API akz_status akz_sg_mse_grad(const float *out, const float *target, float 
  * 2 * width * height * 64 bytes.  Weights and scratch 16-byte aligned.
  * Asynchronous on stream. */
 AKZ_API size_t akz_sg_weight_elems(void);
+
+/* Use the surrogate for every level of octave >= first_octave of a batch
+ * (weights_bf16 NULL: plain FED again).  weights_bf16 / biases are host
+ * arrays in the layout of akz_sg_infer_level.  Per such level and image:
+ * a zero-step FED launch forms Lsmooth, the conductance and the start image,
+ * then the net writes the level.  With check_tol > 0, image 0's level is also
+ * computed by plain FED and compared; if the max difference exceeds
+ * check_tol (or is not finite), the level falls back to plain FED for every
+ * image, decided on the device.  Rebuilds the batch's graph on the next run. */
+AKZ_API akz_status akz_batch_set_surrogate(akz_batch *b, const uint16_t *weights_bf16, const float *biases, float s_out,
+                                           int first_octave, float check_tol);
+/* After a run: per level, image 0's max |surrogate - plain FED| (0 where no
+ * check ran); *nlevels receives the level count. */
+AKZ_API akz_status akz_batch_surrogate_errors(akz_batch *b, float *err, int cap, int *nlevels);
 AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pitch, int width, int height,
                                      float dt_feature, float s_out, const void *weights_bf16, const float *biases,
                                      void *scratch, float *out, void *stream);

@@ -89,3 +89,40 @@ def test_training_lowers_the_loss(gpu_lib):
     curve = meta["loss_curve"]
     assert curve[-1][1] < curve[0][1]
     assert meta["val_mse"] < meta["val_mse_zero_residual"]
+
+
+def test_surrogate_in_the_pipeline_and_exact_fallback(gpu_lib):
+    pytest.importorskip("torch")
+    from akaze_gb300 import synth
+    W, H = 640, 480
+    sizes = [(W, H)] * 2
+    imgs = [synth.synth_image(800 + i, W, H) for i in range(2)]
+    rng = np.random.default_rng(6)
+    params = [(0.5 * rng.normal(0, np.sqrt(2.0 / (ci * 9)), (co, ci, 3, 3)).astype(np.float32), np.zeros(co, np.float32))
+              for ci, co in sg.LAYERS]
+    plain = gpu_lib.Batch(gpu_lib.AKAZEOptions(), sizes)
+    plain.upload(imgs)
+    plain.run()
+    ref = [plain.results(i) for i in range(2)]
+    b = gpu_lib.Batch(gpu_lib.AKAZEOptions(), sizes)
+    b.upload(imgs)
+    # a tolerance nothing meets: every surrogate level falls back to plain FED,
+    # so the whole result equals the plain pipeline bit for bit
+    b.set_surrogate(params, first_octave=1, check_tol=1e-12)
+    b.run()
+    errs = b.surrogate_errors()
+    assert errs.size == 16 and np.all(errs[4:] > 1e-12) and np.all(errs[:4] == 0)
+    for i in range(2):
+        kp, d = b.results(i)
+        assert kp.tobytes() == ref[i][0].tobytes() and np.array_equal(d, ref[i][1])
+    # a tolerance everything meets: the net's levels stand
+    b.set_surrogate(params, first_octave=1, check_tol=1e9)
+    b.run()
+    assert np.all(np.isfinite(b.surrogate_errors()))
+    assert not np.array_equal(b.plane(0, 5, shape=(240, 320)), plain.plane(0, 5, shape=(240, 320)))
+    assert np.array_equal(b.plane(0, 3, shape=(480, 640)), plain.plane(0, 3, shape=(480, 640)))
+    # switched off again: plain results
+    b.set_surrogate(None)
+    b.run()
+    kp, d = b.results(1)
+    assert kp.tobytes() == ref[1][0].tobytes() and np.array_equal(d, ref[1][1])
