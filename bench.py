@@ -558,7 +558,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"plain A-KAZE detect+MLDB, {W}x{H} u8, 4 octaves x 4 sublevels, default options",
-                   "fed": "plain (the learned surrogate path is not built)",
+                   "fed": "plain (the learned surrogate is built but 2.6x slower at 4K on this GPU: --workload surrogate4k)",
                    "images_per_step_per_gpu": B, "parallelism": f"replicas x{ws}",
                    "l2": "inputs and working set larger than L2 (~%.1f GB per step)" % (B * image_algorithmic_bytes(W, H, 0) / 1e9),
                    "keypoints_per_image": nkp},
