@@ -34,6 +34,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "1080p images/s detect+MLDB, surrogate vs plain FED at fixed repeatability"
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the 27 k_fed
+# launches of one 1920x1080 image, from an ncu capture of an 8-image batch
+# (618.3 MB / 8); the level stage's traffic per step is this times the batch.
+FED_TRAFFIC_PER_1080P_IMAGE = 77.29e6
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
 
@@ -564,7 +568,9 @@ def main():
                    "keypoints_per_image": nkp},
         "roofline": {"bound": "hbm", "kernel": "k_fed (level stage: 15 levels, 166 FED steps)",
                      "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                     "frac": achieved / pk["hbm_gbs"],
+                     "traffic": FED_TRAFFIC_PER_1080P_IMAGE * B if (W, H) == (1920, 1080) else None,
+                     "traffic_note": "ncu DRAM bytes of the level stage, 8-image capture scaled to the batch",
                      "algorithmic_bytes_per_image": fed_algorithmic_bytes(W, H), "launch_ms": fed_ms,
                      "peak_kind": f"{pk_kind} hbm_gbs"},
         "pipeline_roofline": {"achieved": image_algorithmic_bytes(W, H, nkp) * value / 1e9,
