@@ -341,3 +341,12 @@ class Batch:
         out = np.empty(shape, np.float32)
         check(self._lib.akz_batch_level_plane(self._h, i, level, _PLANES[name], _ptr(out)))
         return out
+
+
+def save_keypoints(path, kpts, desc=None):
+    """save_keypoints (utils.cpp:97-152): Mikolajczyk text format."""
+    kp = np.ascontiguousarray(kpts, KEYPOINT_DTYPE)
+    d = None if desc is None else np.ascontiguousarray(desc, np.uint8)
+    check(load().akz_save_keypoints(str(path).encode(), _ptr(kp) if kp.size else None, len(kp),
+                                    _ptr(d) if d is not None and d.size else None,
+                                    0 if d is None else d.shape[1], int(d is not None)))

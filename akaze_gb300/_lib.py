@@ -29,7 +29,7 @@ EXPORTS = [
     "akz_matcher_bfmatch_device", "akz_matcher_bfmatch_noalloc", "akz_measure_popc_rate",
     "akz_sg_conv_forward", "akz_sg_conv_backward_data", "akz_sg_conv_backward_weights", "akz_sg_adam",
     "akz_sg_weight_elems", "akz_sg_infer_level", "akz_sg_mse_grad", "akz_batch_set_surrogate",
-    "akz_batch_surrogate_errors",
+    "akz_batch_surrogate_errors", "akz_nndr_homography_inliers", "akz_save_keypoints",
 ]
 
 
@@ -114,6 +114,8 @@ def load():
         "akz_sg_mse_grad": ([P, P, P, I, ctypes.c_float, P, I, P], I),
         "akz_batch_set_surrogate": ([P, P, P, ctypes.c_float, I, ctypes.c_float], I),
         "akz_batch_surrogate_errors": ([P, P, I, IP], I),
+        "akz_nndr_homography_inliers": ([P, I, P, P, P, ctypes.c_float, ctypes.c_float, P, P, P], I),
+        "akz_save_keypoints": ([ctypes.c_char_p, P, I, P, I, I], I),
         "akz_sg_infer_level": ([P, P, ctypes.c_size_t, I, I, ctypes.c_float, ctypes.c_float, P, P, P, P, P], I),
     }
     for name, (args, res) in sig.items():

@@ -278,6 +278,29 @@ AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pi
                                      float dt_feature, float s_out, const void *weights_bf16, const float *biases,
                                      void *scratch, float *out, void *stream);
 
+/* ---- evaluation and output ---------------------------------------------- */
+
+/* NNDR matches and homography inliers of a 2-NN result, on the device:
+ * matches2points_nndr + compute_inliers_homography (utils.cpp:154-243) as
+ * akaze_match.cpp:161-168 uses them (nndr 0.8, min_error 2.5 there).
+ * matches: 2*nq records as akz_matcher_bfmatch_device writes them (query i's
+ * best, then second best); kp_query / kp_train: the keypoints of the query
+ * and train images; H: 3x3 row-major homography (host) mapping query points
+ * to train points.  status[i] = 0 (no NNDR match), 1 (match) or 2 (match and
+ * inlier); counts[0] = matches, counts[1] = inliers.  The arithmetic is the
+ * reference's: float NNDR and projection, the distance in double.  Device
+ * pointers except H; asynchronous on stream. */
+AKZ_API akz_status akz_nndr_homography_inliers(const akz_dmatch *matches, int nq, const akz_keypoint *kp_query,
+                                               const akz_keypoint *kp_train, const float *H, float nndr,
+                                               float min_error, int8_t *status, int *counts, void *stream);
+
+/* save_keypoints (utils.cpp:97-152): the Krystian Mikolajczyk text format,
+ * "x y 1/r^2 0 1/r^2 [descriptor bytes]" per keypoint with r = size, after a
+ * header of the descriptor length (1 without descriptors) and the count.
+ * Host memory. */
+AKZ_API akz_status akz_save_keypoints(const char *path, const akz_keypoint *kpts, int n, const uint8_t *desc,
+                                      int desc_bytes, int save_desc);
+
 #ifdef __cplusplus
 }
 #endif
