@@ -452,18 +452,23 @@ struct akz_nms_ctx {
 /* Decision of unsettled point i: 0 wait (an earlier neighbour is unsettled),
  * 1 take its own slot, 2 challenge *target (the settled neighbour with the
  * smallest slot value). Neighbours: FindNeighbors, cuda_akaze.cu:1005-1070. */
-__device__ int akz_nms_decide(const akz_nms_ctx &c, int i, int *target)
+/* Visits the neighbours of raw extremum i in the reference's sense
+ * (cuda_akaze.cu:1005-1070): earlier points of the same level and points of
+ * the previous level whose squared distance is below (size/2)^2; weak points
+ * (negative size) have none.  f(j) returns false to stop; visit returns
+ * false when stopped. */
+template <class F>
+__device__ __forceinline__ bool akz_nms_visit(const akz_nms_ctx &c, int i, F f)
 {
   const akz_raw e = c.R[i];
   const float size = e.size;
-  if (!(size >= 0.0f)) return 1; /* weak points have no neighbours */
+  if (!(size >= 0.0f)) return true;
   const float hs = size * .5f;
   const float lim = size * size * 0.25f;
   const akz_level_desc L = c.lv[c.first_level + e.level];
   const int r = 1 << e.octave;
   const float px = (float)(r * e.x), py = (float)(r * e.y);
   const long long rowb = L.rows - c.rows_base;
-  int best = -1, bestv = INT_MAX;
   /* same level: earlier points whose rows are within hs */
   for (int yy = e.y; yy >= 0; yy--) {
     const float pyj = (float)(r * yy);
@@ -472,15 +477,7 @@ __device__ int akz_nms_decide(const akz_nms_ctx &c, int i, int *target)
     const int j1 = yy == e.y ? i : c.rs[rowb + yy + 1];
     for (int j = j0; j < j1; j++) {
       const float ddx = px - (float)(r * c.R[j].x), ddy = py - pyj;
-      const float dist = ddx * ddx + ddy * ddy;
-      if (dist < lim) {
-        const int s = c.state[j];
-        if (s == -1) return 0;
-        if (s >= 0 && s < bestv) {
-          bestv = s;
-          best = j;
-        }
-      }
+      if (ddx * ddx + ddy * ddy < lim && !f(j)) return false;
     }
   }
   /* previous level: points whose rows are within hs either way */
@@ -497,20 +494,42 @@ __device__ int akz_nms_decide(const akz_nms_ctx &c, int i, int *target)
       const int j0 = c.rs[rowp + yy], j1 = c.rs[rowp + yy + 1];
       for (int j = j0; j < j1; j++) {
         const float ddx = px - (float)(rp * c.R[j].x), ddy = py - pyj;
-        const float dist = ddx * ddx + ddy * ddy;
-        if (dist < lim) {
-          const int s = c.state[j];
-          if (s == -1) return 0;
-          if (s >= 0 && s < bestv) {
-            bestv = s;
-            best = j;
-          }
-        }
+        if (ddx * ddx + ddy * ddy < lim && !f(j)) return false;
       }
     }
   }
-  if (best < 0) return 1;
-  *target = best;
+  return true;
+}
+
+/* One point's decision in a round: 0 wait (an unsettled neighbour), 1 take
+ * its own slot (no settled neighbour), 2 challenge *target, the settled
+ * neighbour with the smallest slot value. */
+struct akz_nms_pick {
+  const int *state;
+  int best, bestv;
+  bool wait;
+  __device__ __forceinline__ bool operator()(int j)
+  {
+    const int sj = state[j];
+    if (sj == -1) {
+      wait = true;
+      return false;
+    }
+    if (sj >= 0 && sj < bestv) {
+      bestv = sj;
+      best = j;
+    }
+    return true;
+  }
+};
+
+__device__ __forceinline__ int akz_nms_decide(const akz_nms_ctx &c, int i, int *target)
+{
+  akz_nms_pick pk{c.state, -1, INT_MAX, false};
+  akz_nms_visit(c, i, [&](int j) { return pk(j); });
+  if (pk.wait) return 0;
+  if (pk.best < 0) return 1;
+  *target = pk.best;
   return 2;
 }
 
@@ -554,14 +573,39 @@ __global__ void __launch_bounds__(AKZ_NMS_THREADS) k_nms(akz_nms_params p)
   }
   __syncthreads();
   const akz_nms_ctx c{R, state, p.rowscan + I.rows_base, p.t.lv, I.first_level, I.rows_base};
+  /* neighbour sets, found once (the rounds then cost O(neighbours) each);
+   * a point with more than AKZ_NMS_NB neighbours is decided by scanning */
+  int *nbr = p.nbr + (long long)I.raw_base * AKZ_NMS_NB;
+  unsigned char *nbc = p.nbc + I.raw_base;
+  for (int i = tid; i < n; i += AKZ_NMS_THREADS) {
+    int cnt = 0;
+    int *li = nbr + (long long)i * AKZ_NMS_NB;
+    const bool all = akz_nms_visit(c, i, [&](int j) {
+      if (cnt == AKZ_NMS_NB) return false;
+      li[cnt++] = j;
+      return true;
+    });
+    nbc[i] = (unsigned char)(all ? cnt : AKZ_NMS_NB + 1);
+  }
+  __syncthreads();
   int rounds = 0;
   for (;;) {
     int any = 0;
     for (int i = tid; i < n; i += AKZ_NMS_THREADS) {
       if (state[i] != -1) continue;
       any = 1;
-      int target = -1;
-      const int d = akz_nms_decide(c, i, &target);
+      int target = -1, d;
+      const int cnt = nbc[i];
+      if (cnt <= AKZ_NMS_NB) {
+        akz_nms_pick pk{state, -1, INT_MAX, false};
+        const int *li = nbr + (long long)i * AKZ_NMS_NB;
+        for (int k = 0; k < cnt && pk(li[k]); k++) {
+        }
+        d = pk.wait ? 0 : (pk.best < 0 ? 1 : 2);
+        target = pk.best;
+      } else {
+        d = akz_nms_decide(c, i, &target);
+      }
       dec[i] = (signed char)d;
       if (d == 2) atomicMin(&minc[target], i);
     }

@@ -292,6 +292,8 @@ struct akz_batch {
   signed char *d_dec = nullptr;
   akz_kp *d_kp = nullptr;
   uint32_t *d_desc = nullptr;
+  int *d_nbr = nullptr;
+  unsigned char *d_nbc = nullptr;
   size_t raw_all = 0;
   int input_f32 = 0;
   cudaStream_t stream = nullptr, own_stream = nullptr;
@@ -602,6 +604,8 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
   const size_t o_dec = take(raw);
   const size_t o_kp = take(raw * sizeof(akz_kp));
   const size_t o_desc = take(raw * 64);
+  const size_t o_nbr = take(raw * AKZ_NMS_NB * sizeof(int));
+  const size_t o_nbc = take(raw);
   b->arena_bytes = off;
   cudaError_t e = cudaMalloc(&b->arena, b->arena_bytes);
   if (e != cudaSuccess) {
@@ -630,6 +634,8 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
   b->d_dec = (signed char *)(a + o_dec);
   b->d_kp = (akz_kp *)(a + o_kp);
   b->d_desc = (uint32_t *)(a + o_desc);
+  b->d_nbr = (int *)(a + o_nbr);
+  b->d_nbc = (unsigned char *)(a + o_nbc);
   e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost(&b->h_stats, (size_t)n * sizeof(akz_image_stats));
   for (auto &ev : b->ev)
@@ -772,6 +778,8 @@ static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s, cudaEvent_t *pe
   np.decision = b->d_dec;
   np.kp = b->d_kp;
   np.max_rounds = 1 << 20;
+  np.nbr = b->d_nbr;
+  np.nbc = b->d_nbc;
   CK(akz_launch_nms(np, s));
   return AKZ_OK;
 }

@@ -22,6 +22,7 @@
 #define AKZ_MAX_LEVELS 64
 #define AKZ_MAX_NBINS 4096
 #define AKZ_NMS_THREADS 1024
+#define AKZ_NMS_NB 8 /* neighbour list capacity per raw extremum */
 
 /* One (image, level). */
 struct akz_level_desc {

@@ -106,6 +106,8 @@ struct akz_nms_params {
   signed char *decision;
   akz_kp *kp;
   int max_rounds;
+  int *nbr;           /* AKZ_NMS_NB neighbours per raw extremum */
+  unsigned char *nbc; /* their count; AKZ_NMS_NB + 1: more, decided by scanning */
 };
 
 struct akz_describe_params {
