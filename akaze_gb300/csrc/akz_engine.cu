@@ -250,6 +250,7 @@ struct akz_batch {
   std::vector<akz_tile_seg> segs;
   int contrast_off = 0, contrast_n = 0, contrast_tiles = 0;
   int gauss_off = 0, gauss_n = 0, gauss_tiles = 0;
+  int l0_off = 0, l0_n = 0, l0_tiles = 0; /* k_level0 tiles */
   int detect_off = 0, detect_n = 0, detect_tiles = 0;
   int extract_off = 0, extract_n = 0, extract_rows = 0;
   std::vector<std::vector<akz_fed_launch>> fed;  /* per level index */
@@ -473,6 +474,9 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
   b->gauss_off = (int)b->segs.size();
   for (int i = 0; i < n; i++) add_tiles(b->im[i].first_level, Ws[i], Hs[i], AKZ_GAUSS_TW, AKZ_GAUSS_TH, 0, b->gauss_tiles);
   b->gauss_n = (int)b->segs.size() - b->gauss_off;
+  b->l0_off = (int)b->segs.size();
+  for (int i = 0; i < n; i++) add_tiles(b->im[i].first_level, Ws[i], Hs[i], AKZ_L0_TW, AKZ_L0_TH, 0, b->l0_tiles);
+  b->l0_n = (int)b->segs.size() - b->l0_off;
 
   b->fed.resize(b->maxlev);
   b->area.resize(b->maxlev);
@@ -667,27 +671,47 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe 
   if (b->sg_on) CK(cudaMemsetAsync(b->d_sg_err, 0, (size_t)b->maxlev * sizeof(float), s));
   CK(cudaMemsetAsync(b->d_stats, 0, (size_t)b->nimg * sizeof(akz_image_stats), s));
   CK(cudaMemsetAsync(b->d_hist, 0, (size_t)b->nimg * b->opt.kcontrast_nbins * sizeof(unsigned int), s));
-  akz_contrast_params cp;
-  cp.t = t;
-  cp.segs = b->d_segs + b->contrast_off;
-  cp.nsegs = b->contrast_n;
-  cp.nbins = (int)b->opt.kcontrast_nbins;
-  cp.hist = b->d_hist;
-  cp.inv255 = (float)(1.0 / 255.0);
-  for (int k = 0; k < 5; k++) cp.taps[k] = b->taps1[k];
-  CK(akz_launch_contrast(cp, b->contrast_tiles, 0, s));
-  CK(akz_launch_contrast(cp, b->contrast_tiles, 1, s));
-  CK(akz_launch_contrast_final(t, b->d_hist, cp.nbins, b->opt.kcontrast_percentile, b->d_kc, s));
-  if (pe) CK(cudaEventRecord(pe[1], s));
-  akz_gauss_params gp;
-  gp.t = t;
-  gp.segs = b->d_segs + b->gauss_off;
-  gp.nsegs = b->gauss_n;
-  gp.inv255 = cp.inv255;
-  gp.R = b->R0;
-  for (int k = 0; k <= 2 * b->R0; k++) gp.taps[k] = b->taps0[k];
-  CK(akz_launch_gauss0(gp, b->gauss_tiles, s));
-  if (pe) CK(cudaEventRecord(pe[2], s));
+  const float inv255 = (float)(1.0 / 255.0);
+  if (b->R0 <= 4) {
+    /* level 0 and the contrast gradient from one staging of the input */
+    akz_level0_params lp;
+    lp.t = t;
+    lp.segs = b->d_segs + b->l0_off;
+    lp.nsegs = b->l0_n;
+    lp.inv255 = inv255;
+    for (int k = 0; k < 5; k++) lp.taps0[k] = k < 4 - b->R0 ? 0.0f : b->taps0[k - (4 - b->R0)];
+    for (int k = 0; k < 3; k++) lp.taps1[k] = b->taps1[k];
+    lp.nbins = (int)b->opt.kcontrast_nbins;
+    lp.hist = b->d_hist;
+    CK(akz_launch_level0(lp, b->l0_tiles, s));
+    CK(akz_launch_contrast_final(t, b->d_hist, lp.nbins, b->opt.kcontrast_percentile, b->d_kc, s));
+    if (pe) {
+      CK(cudaEventRecord(pe[1], s));
+      CK(cudaEventRecord(pe[2], s));
+    }
+  } else {
+    akz_contrast_params cp;
+    cp.t = t;
+    cp.segs = b->d_segs + b->contrast_off;
+    cp.nsegs = b->contrast_n;
+    cp.nbins = (int)b->opt.kcontrast_nbins;
+    cp.hist = b->d_hist;
+    cp.inv255 = inv255;
+    for (int k = 0; k < 5; k++) cp.taps[k] = b->taps1[k];
+    CK(akz_launch_contrast(cp, b->contrast_tiles, 0, s));
+    CK(akz_launch_contrast(cp, b->contrast_tiles, 1, s));
+    CK(akz_launch_contrast_final(t, b->d_hist, cp.nbins, b->opt.kcontrast_percentile, b->d_kc, s));
+    if (pe) CK(cudaEventRecord(pe[1], s));
+    akz_gauss_params gp;
+    gp.t = t;
+    gp.segs = b->d_segs + b->gauss_off;
+    gp.nsegs = b->gauss_n;
+    gp.inv255 = inv255;
+    gp.R = b->R0;
+    for (int k = 0; k <= 2 * b->R0; k++) gp.taps[k] = b->taps0[k];
+    CK(akz_launch_gauss0(gp, b->gauss_tiles, s));
+    if (pe) CK(cudaEventRecord(pe[2], s));
+  }
   for (int l = 1; l < b->maxlev; l++) {
     if (b->area[l].nsegs > 0) {
       akz_area_params ap;

@@ -34,6 +34,21 @@ struct akz_contrast_params {
   float taps[5];      /* sigma 1, radius 2 */
 };
 
+/* Level 0 and the contrast gradient in one pass (akz_scale.cu k_level0):
+ * tiles of AKZ_L0_TW x AKZ_L0_TH over level 0 of every image. */
+#define AKZ_L0_TW 128
+#define AKZ_L0_TH 32
+struct akz_level0_params {
+  akz_tables t;
+  const akz_tile_seg *segs;
+  int nsegs;
+  float inv255;
+  float taps0[5]; /* soffset Gaussian, outermost tap first, zero-padded to radius 4 */
+  float taps1[3]; /* sigma 1 */
+  int nbins;
+  unsigned int *hist;
+};
+
 struct akz_gauss_params {
   akz_tables t;
   const akz_tile_seg *segs;
@@ -122,6 +137,7 @@ struct akz_describe_params {
 cudaError_t akz_launch_contrast(const akz_contrast_params &p, int ntiles, int pass, cudaStream_t s);
 cudaError_t akz_launch_contrast_final(const akz_tables &t, const unsigned int *hist, int nbins, float perc, float2 *kc, cudaStream_t s);
 cudaError_t akz_launch_gauss0(const akz_gauss_params &p, int ntiles, cudaStream_t s);
+cudaError_t akz_launch_level0(const akz_level0_params &p, int ntiles, cudaStream_t s);
 cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int tw, int th, cudaStream_t s);
 size_t akz_fed_smem_bytes(int tw, int th, int steps, int first);
 cudaError_t akz_launch_area(const akz_area_params &p, int maxw, int maxh, cudaStream_t s);

@@ -149,6 +149,200 @@ __global__ void k_contrast_final(akz_tables t, const unsigned int *hist, int nbi
 }
 
 /* ------------------------------------------------------------------------ */
+/* Level 0 and the contrast gradient from one staging of the input.
+ *
+ * k_level0: per 128 x 32 tile, the input region tile +- 4 is staged once
+ * with replicate (clamped) coordinates; from it
+ *   Lt0 = the soffset Gaussian (AKAZE.cpp:234, radius <= 4; a smaller kernel
+ *         is zero-padded at its outer end, which adds exact zeros first), and
+ *   m   = Lx^2 + Ly^2 of the Scharr gradient of the sigma-1 Gaussian
+ *         (compute_k_percentile, nldiffusion_functions.cpp:121-170) at every
+ *         interior pixel, written to the image's T1 plane, with the image's
+ *         maximum of m.
+ * k_contrast_hist then bins sqrt(m) / max (nldiffusion_functions.cpp:
+ * 172-197).  Column pairs with packed FP32x2 additions, scalar products, in
+ * the reference's operation order, so every value equals the per-pixel
+ * kernels k_gauss0 / k_contrast. */
+
+__global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
+{
+  constexpr int TW = AKZ_L0_TW, TH = AKZ_L0_TH;
+  constexpr int PW = TW + 8, PH = TH + 8;  /* input: tile +- 4 */
+  constexpr int BW = TW + 2, BH = TH + 6;  /* sigma-1 rows pass: cols tile +- 1, rows tile +- 3 */
+  constexpr int CH = TH + 2;               /* sigma-1 columns pass: rows tile +- 1 */
+  extern __shared__ __align__(16) float l0sm[];
+  float *sP = l0sm, *sA = sP + PH * PW, *sB = sA + PH * TW;
+  float *sC = sP; /* the input region is dead after both rows passes */
+  __shared__ float sRed[8];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
+  const akz_tile_seg sg = p.segs[si];
+  const akz_level_desc L = p.t.lv[sg.level_desc];
+  const akz_image_desc I = p.t.im[L.image];
+  const int W = L.width, H = L.height;
+  const int lt = blockIdx.x - sg.tile_begin;
+  const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
+
+  for (int i = tid; i < PH * PW; i += 256) {
+    const int r = i / PW, c = i - r * PW;
+    const int y = akz_clampi(ty0 - 4 + r, 0, H - 1), x = akz_clampi(tx0 - 4 + c, 0, W - 1);
+    sP[i] = akz_fetch_input(p.t, I, x, y, p.inv255);
+  }
+  __syncthreads();
+  /* rows passes: soffset Gaussian on tile columns (all PH rows), sigma-1 on
+   * columns tile +- 1, rows tile +- 3 */
+  const float t0 = p.taps0[0], t1 = p.taps0[1], t2 = p.taps0[2], t3 = p.taps0[3], t4 = p.taps0[4];
+  const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
+  for (int i = tid; i < PH * (TW / 2); i += 256) {
+    const int r = i / (TW / 2), c = 2 * (i - r * (TW / 2));
+    const float *q = sP + r * PW + c; /* sP column c + 4 is tile column c */
+    const float2 A0 = ld2(q), A1 = ld2(q + 2), A2 = ld2(q + 4), A3 = ld2(q + 6), A4 = ld2(q + 8);
+    const float2 s08 = f2add(A0, A4);
+    const float2 s17 = f2add(make_float2(A0.y, A1.x), make_float2(A3.y, A4.x));
+    const float2 s26 = f2add(A1, A3);
+    const float2 s35 = f2add(make_float2(A1.y, A2.x), make_float2(A2.y, A3.x));
+    float2 acc = make_float2(t0 * s08.x, t0 * s08.y);
+    acc = f2add(acc, make_float2(t1 * s17.x, t1 * s17.y));
+    acc = f2add(acc, make_float2(t2 * s26.x, t2 * s26.y));
+    acc = f2add(acc, make_float2(t3 * s35.x, t3 * s35.y));
+    acc = f2add(acc, make_float2(t4 * A2.x, t4 * A2.y));
+    st2(sA + r * TW + c, acc);
+  }
+  for (int i = tid; i < BH * (BW / 2); i += 256) {
+    const int r = i / (BW / 2), d = 2 * (i - r * (BW / 2));
+    const float *q = sP + (r + 1) * PW + d; /* sB column d is x = tx0 - 1 + d, sP column d + 3 */
+    const float2 B0 = ld2(q), B1 = ld2(q + 2), B2 = ld2(q + 4), B3 = ld2(q + 6);
+    const float2 s15 = f2add(make_float2(B0.y, B1.x), make_float2(B2.y, B3.x));
+    const float2 s24 = f2add(B1, B2);
+    float2 acc = make_float2(k0 * s15.x, k0 * s15.y);
+    acc = f2add(acc, make_float2(k1 * s24.x, k1 * s24.y));
+    acc = f2add(acc, make_float2(k2 * B1.y, k2 * B2.x));
+    st2(sB + r * BW + d, acc);
+  }
+  __syncthreads();
+  /* columns passes: Lt0 for the tile (to HBM), sigma-1 rows tile +- 1 */
+  {
+    const int c = 2 * (tid & 63), g = tid >> 6; /* 64 column pairs x 4 groups of 8 rows */
+    const int x = tx0 + c;
+    float *out = p.t.planes + L.lt;
+    float2 v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = ld2(sA + (g * 8 + j) * TW + c);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const float2 s08 = f2add(v[j], v[j + 8]), s17 = f2add(v[j + 1], v[j + 7]);
+      const float2 s26 = f2add(v[j + 2], v[j + 6]), s35 = f2add(v[j + 3], v[j + 5]);
+      float2 acc = make_float2(t0 * s08.x, t0 * s08.y);
+      acc = f2add(acc, make_float2(t1 * s17.x, t1 * s17.y));
+      acc = f2add(acc, make_float2(t2 * s26.x, t2 * s26.y));
+      acc = f2add(acc, make_float2(t3 * s35.x, t3 * s35.y));
+      acc = f2add(acc, make_float2(t4 * v[j + 4].x, t4 * v[j + 4].y));
+      const int y = ty0 + g * 8 + j;
+      if (y < H) {
+        float *o = out + (long long)y * L.pitch + x;
+        if (x + 1 < W)
+          st2(o, acc);
+        else if (x < W)
+          o[0] = acc.x;
+      }
+    }
+  }
+  for (int i = tid; i < CH * (BW / 2); i += 256) {
+    const int r = i / (BW / 2), d = 2 * (i - r * (BW / 2));
+    const float *q = sB + r * BW + d; /* sC row r is y = ty0 - 1 + r, sB rows r .. r + 4 */
+    const float2 a = ld2(q), b = ld2(q + BW), c = ld2(q + 2 * BW), e = ld2(q + 3 * BW), f = ld2(q + 4 * BW);
+    const float2 s04 = f2add(a, f), s13 = f2add(b, e);
+    float2 acc = make_float2(k0 * s04.x, k0 * s04.y);
+    acc = f2add(acc, make_float2(k1 * s13.x, k1 * s13.y));
+    acc = f2add(acc, make_float2(k2 * c.x, k2 * c.y));
+    st2(sC + r * BW + d, acc);
+  }
+  __syncthreads();
+  /* Scharr gradient magnitude^2 at interior pixels of the tile */
+  float mx = 0.0f;
+  float *mp = p.t.planes + I.t1;
+  for (int i = tid; i < TH * (TW / 2); i += 256) {
+    const int r = i / (TW / 2), c = 2 * (i - r * (TW / 2));
+    const float *rm = sC + r * BW + c, *r0 = rm + BW, *rp = r0 + BW; /* sC columns c .. c + 3 are x - 1 .. x + 2 */
+    const float2 m0 = ld2(rm), m1 = ld2(rm + 2), c0 = ld2(r0), c1 = ld2(r0 + 2), p0 = ld2(rp), p1 = ld2(rp + 2);
+    const float2 hm = f2sub(m1, m0), h0 = f2sub(c1, c0), hp = f2sub(p1, p0); /* v[x+1] - v[x-1] */
+    const float2 u = f2add(hm, hp);
+    const float2 lx = f2add(make_float2(3.0f * u.x, 3.0f * u.y), make_float2(10.0f * h0.x, 10.0f * h0.y));
+    const float2 sp = f2add(p0, p1), sm = f2add(m0, m1); /* (v[x-1] + v[x+1]) */
+    const float2 syp = f2add(make_float2(3.0f * sp.x, 3.0f * sp.y), make_float2(10.0f * p0.y, 10.0f * p1.x));
+    const float2 sym = f2add(make_float2(3.0f * sm.x, 3.0f * sm.y), make_float2(10.0f * m0.y, 10.0f * m1.x));
+    const float2 ly = f2sub(syp, sym);
+    const float2 m = f2add(make_float2(lx.x * lx.x, lx.y * lx.y), make_float2(ly.x * ly.x, ly.y * ly.y));
+    const int y = ty0 + r, x = tx0 + c;
+    if (y < 1 || y >= H - 1) continue;
+    float *o = mp + (long long)y * L.pitch + x;
+    if (x >= 1 && x < W - 1) {
+      o[0] = m.x;
+      mx = fmaxf(mx, m.x);
+    }
+    if (x + 1 >= 1 && x + 1 < W - 1) {
+      o[1] = m.y;
+      mx = fmaxf(mx, m.y);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) sRed[warp] = mx;
+  __syncthreads();
+  if (tid == 0) {
+    float m = sRed[0];
+    for (int w = 1; w < 8; w++) m = fmaxf(m, sRed[w]);
+    atomicMax(&p.t.stats[L.image].hmax2_bits, __float_as_uint(m));
+  }
+}
+
+__global__ void __launch_bounds__(256) k_contrast_hist(akz_level0_params p)
+{
+  constexpr int TW = AKZ_L0_TW, TH = AKZ_L0_TH;
+  __shared__ unsigned int sHist[AKZ_MAX_NBINS];
+  const int tid = threadIdx.x;
+  const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
+  const akz_tile_seg sg = p.segs[si];
+  const akz_level_desc L = p.t.lv[sg.level_desc];
+  const akz_image_desc I = p.t.im[L.image];
+  const int W = L.width, H = L.height;
+  const int lt = blockIdx.x - sg.tile_begin;
+  const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
+  for (int b = tid; b < p.nbins; b += 256) sHist[b] = 0;
+  __syncthreads();
+  const float hmax = sqrtf(__uint_as_float(p.t.stats[L.image].hmax2_bits));
+  const float nb = (float)p.nbins;
+  const float *mp = p.t.planes + I.t1;
+  const int x0 = max(tx0, 1), x1 = min(tx0 + TW, W - 1), y0 = max(ty0, 1), y1 = min(ty0 + TH, H - 1);
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int y = y0 + warp; y < y1; y += 8)
+    for (int x = x0 + lane; x < x1; x += 32) {
+      const float modg = sqrtf(__ldg(mp + (long long)y * L.pitch + x));
+      if (modg != 0.0f) {
+        int nbin = (int)floorf(nb * (modg / hmax));
+        if (nbin == p.nbins) nbin--;
+        atomicAdd(&sHist[nbin], 1u);
+      }
+    }
+  __syncthreads();
+  for (int b = tid; b < p.nbins; b += 256)
+    if (sHist[b]) atomicAdd(&p.hist[(long long)L.image * p.nbins + b], sHist[b]);
+}
+
+cudaError_t akz_launch_level0(const akz_level0_params &p, int ntiles, cudaStream_t s)
+{
+  if (ntiles <= 0) return cudaSuccess;
+  constexpr int smem = ((AKZ_L0_TH + 8) * (AKZ_L0_TW + 8) + (AKZ_L0_TH + 8) * AKZ_L0_TW + (AKZ_L0_TH + 6) * (AKZ_L0_TW + 2)) *
+                       (int)sizeof(float);
+  cudaError_t e0 = cudaFuncSetAttribute(k_level0, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e0 != cudaSuccess) return e0;
+  k_level0<<<ntiles, 256, smem, s>>>(p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_contrast_hist<<<ntiles, 256, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------ */
 /* Level 0: soffset Gaussian of the input (replicate border).               */
 
 __global__ void __launch_bounds__(256) k_gauss0(akz_gauss_params p)
