@@ -337,6 +337,18 @@ class Batch:
         check(self._lib.akz_batch_detect_describe(self._h, ptrs, strides, kp_p, d_p, _ptr(caps), _ptr(counts)))
         return counts
 
+    def detect_describe_packed(self, imgs, kp_out, d_out):
+        """Whole job with packed output: kp_out (capacity records) and d_out
+        (capacity x 61) receive all images' results back to back; returns
+        the per-image counts."""
+        ptrs = (ctypes.c_void_p * self.n)(*[im.ctypes.data for im in imgs])
+        strides = (ctypes.c_size_t * self.n)(*[im.strides[0] for im in imgs])
+        counts = np.zeros(self.n, np.int32)
+        total = ctypes.c_int()
+        check(self._lib.akz_batch_detect_describe_packed(self._h, ptrs, strides, _ptr(kp_out), _ptr(d_out), len(kp_out),
+                                                         _ptr(counts), ctypes.byref(total)))
+        return counts
+
     def plane(self, i, level, name="Lt", shape=None):
         out = np.empty(shape, np.float32)
         check(self._lib.akz_batch_level_plane(self._h, i, level, _PLANES[name], _ptr(out)))

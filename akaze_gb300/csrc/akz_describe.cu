@@ -241,3 +241,33 @@ cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaS
   k_describe<<<nblocks, 32 * AKZ_DESC_WARPS, 0, s>>>(p);
   return cudaGetLastError();
 }
+
+/* Packs every image's keypoints and 61-byte descriptor rows contiguously
+ * (image i at offset sum_{j<i} nkp_j): blockIdx.x is the image, blockIdx.y
+ * a slice of its rows; a thread copies whole rows. */
+__global__ void k_pack_results(akz_tables t, const akz_kp *kp, const uint32_t *desc, akz_kp *kp_out, uint8_t *desc_out)
+{
+  const int img = blockIdx.x;
+  int off = 0;
+  for (int j = 0; j < img; j++) off += t.stats[j].nkp;
+  const int n = t.stats[img].nkp;
+  const akz_image_desc I = t.im[img];
+  for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < n; k += gridDim.y * blockDim.x) {
+    kp_out[off + k] = kp[I.kp_base + k];
+    const uint4 *src = (const uint4 *)(desc + (long long)(I.kp_base + k) * 16);
+    __align__(16) uint8_t row[64];
+    uint4 *rw = (uint4 *)row;
+#pragma unroll
+    for (int c = 0; c < 4; c++) rw[c] = src[c];
+    uint8_t *dst = desc_out + (long long)(off + k) * 61;
+#pragma unroll
+    for (int c = 0; c < 61; c++) dst[c] = row[c];
+  }
+}
+
+cudaError_t akz_launch_pack_results(const akz_tables &t, const akz_kp *kp, const uint32_t *desc, akz_kp *kp_out,
+                                    uint8_t *desc_out, cudaStream_t s)
+{
+  k_pack_results<<<dim3(t.nimg, 8), 256, 0, s>>>(t, kp, desc, kp_out, desc_out);
+  return cudaGetLastError();
+}

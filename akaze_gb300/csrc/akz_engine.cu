@@ -25,6 +25,8 @@
 
 cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit, cudaStream_t s);
 cudaError_t akz_sg_maxdiff(const float *a, const float *b, int pitch, int width, int height, float *slot, cudaStream_t s);
+cudaError_t akz_launch_pack_results(const akz_tables &t, const akz_kp *kp, const uint32_t *desc, akz_kp *kp_out,
+                                    uint8_t *desc_out, cudaStream_t s);
 extern "C" akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pitch, int width, int height,
                                          float dt_feature, float s_out, const void *weights_bf16, const float *biases,
                                          void *scratch, float *out, void *stream);
@@ -295,6 +297,8 @@ struct akz_batch {
   uint32_t *d_desc = nullptr;
   int *d_nbr = nullptr;
   unsigned char *d_nbc = nullptr;
+  void *d_pack = nullptr; /* packed results of akz_batch_detect_describe_packed, grown on demand */
+  size_t cap_pack = 0;    /* rows */
   size_t raw_all = 0;
   int input_f32 = 0;
   cudaStream_t stream = nullptr, own_stream = nullptr;
@@ -327,7 +331,7 @@ static void akz_batch_free(akz_batch *b)
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->arena) cudaFree(b->arena);
-  for (void *q : {(void *)b->d_sg_w, b->d_sg_scratch, (void *)b->d_sg_b, (void *)b->d_sg_chk, (void *)b->d_sg_err})
+  for (void *q : {(void *)b->d_sg_w, b->d_sg_scratch, (void *)b->d_sg_b, (void *)b->d_sg_chk, (void *)b->d_sg_err, b->d_pack})
     if (q) cudaFree(q);
   if (b->f32) cudaFree(b->f32);
   if (b->h_stats) cudaFreeHost(b->h_stats);
@@ -1252,6 +1256,42 @@ AKZ_API akz_status akz_batch_detect_describe(akz_batch *b, const uint8_t *const 
   return AKZ_OK;
 }
 
+AKZ_API akz_status akz_batch_detect_describe_packed(akz_batch *b, const uint8_t *const *images, const size_t *strides,
+                                                    akz_keypoint *kpts, uint8_t *desc, int capacity, int *counts,
+                                                    int *total)
+{
+  AKZ_GUARD(b);
+  if (!counts || !total || capacity < 0) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_batch_detect_describe_packed: bad arguments");
+  akz_status st = akz_batch_upload(b, images, strides, 0);
+  if (st == AKZ_OK) st = akz_batch_launch(b);
+  if (st == AKZ_OK) st = akz_batch_sync_stats(b);
+  if (st != AKZ_OK) return st;
+  long long n = 0;
+  for (int i = 0; i < b->nimg; i++) {
+    counts[i] = b->h_stats[i].nkp;
+    n += counts[i];
+  }
+  *total = (int)n;
+  if (n > capacity)
+    return akz_fail(AKZ_ERR_OVERFLOW, "akz_batch_detect_describe_packed: %lld keypoints exceed the capacity %d", n, capacity);
+  if (n == 0) return AKZ_OK;
+  if ((size_t)n > b->cap_pack) {
+    if (b->d_pack) cudaFree(b->d_pack);
+    b->d_pack = nullptr;
+    b->cap_pack = 0;
+    const size_t rows = (size_t)n + (size_t)n / 4;
+    CK(cudaMalloc(&b->d_pack, rows * (sizeof(akz_kp) + 64)));
+    b->cap_pack = rows;
+  }
+  akz_kp *pk = (akz_kp *)b->d_pack;
+  uint8_t *pd = (uint8_t *)(pk + b->cap_pack);
+  CK(akz_launch_pack_results(akz_make_tables(b), b->d_kp, b->d_desc, pk, pd, b->stream));
+  if (kpts) CK(cudaMemcpyAsync(kpts, pk, (size_t)n * sizeof(akz_kp), cudaMemcpyDeviceToHost, b->stream));
+  if (desc) CK(cudaMemcpyAsync(desc, pd, (size_t)n * 61, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return AKZ_OK;
+}
+
 AKZ_API akz_status akz_batch_level_plane(akz_batch *b, int i, int level, int plane, float *out)
 {
   AKZ_GUARD(b);
@@ -1261,8 +1301,19 @@ AKZ_API akz_status akz_batch_level_plane(akz_batch *b, int i, int level, int pla
 /* Number of kernels one akz_batch_run launches. */
 static int akz_batch_nkernels(const akz_batch *b)
 {
-  int n = 3 + 1 + 1 + 1 + 1 + 1 + 1; /* contrast x3, level 0, detect, scan, extract, nms, describe */
-  for (int l = 1; l < b->maxlev; l++) n += (int)b->fed[l].size() + (b->area[l].nsegs > 0 ? 1 : 0);
+  /* level 0 + contrast: k_level0, k_contrast_hist, k_contrast_final (radius <= 4),
+   * else k_contrast x2, k_contrast_final, k_gauss0; then detect, scan,
+   * extract, nms, describe */
+  int n = (b->R0 <= 4 ? 3 : 4) + 5;
+  for (int l = 1; l < b->maxlev; l++) {
+    n += b->area[l].nsegs > 0 ? 1 : 0;
+    if (b->sg_on && l / b->opt.nsublevels >= b->sg_first_octave) {
+      n += 1 + 6 * b->nimg; /* zero-step prologue, per image im2col + 5 GEMMs */
+      if (b->sg_tol > 0.0f) n += (int)b->sg_check[l].size() + 1 + (int)b->fed[l].size();
+    } else {
+      n += (int)b->fed[l].size();
+    }
+  }
   return n;
 }
 

@@ -9,8 +9,9 @@ their 166 FED steps, Hessian detector, extrema, suppression, orientation,
 descriptors.  One graph replay per step.
 
   value   images/s with the input already in HBM (all ranks; replicas only)
-  e2e     images/s through akz_batch_detect_describe: pinned host u8 in,
-          host keypoints + 61-byte descriptors out, copies inside the timing
+  e2e     images/s through akz_batch_detect_describe_packed: pinned host u8
+          in, host keypoints + 61-byte descriptors out (packed), copies inside
+          the timing
   roofline  HBM roofline of the level (FED) stage, the dominant stage
   cpu_baseline  the CPU oracle on this host's cores (OpenMP), bounded sample
 
@@ -533,18 +534,18 @@ def main():
     pin_in = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(B)]
     for p, im in zip(pin_in, imgs):
         p.numpy()[:] = im
-    cap = int(max(counts)) + 64
-    kps = [torch.empty(cap * 28, dtype=torch.uint8).pin_memory().numpy().view(akz.KEYPOINT_DTYPE) for _ in range(B)]
-    ds = [torch.empty(cap * 61, dtype=torch.uint8).pin_memory().numpy().reshape(cap, 61) for _ in range(B)]
+    cap = int(sum(counts)) + 1024
+    kp_out = torch.empty(cap * 28, dtype=torch.uint8).pin_memory().numpy().view(akz.KEYPOINT_DTYPE)
+    d_out = torch.empty(cap * 61, dtype=torch.uint8).pin_memory().numpy().reshape(cap, 61)
     np_in = [p.numpy() for p in pin_in]
     for _ in range(2):
-        c2 = batch.detect_describe_into(np_in, kps, ds)
+        c2 = batch.detect_describe_packed(np_in, kp_out, d_out)
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     e_steps = max(1, min(args.steps, 10))
     for _ in range(e_steps):
-        c2 = batch.detect_describe_into(np_in, kps, ds)
+        c2 = batch.detect_describe_packed(np_in, kp_out, d_out)
     el = replicas.max_over_ranks(time.perf_counter() - t0, dist, device="cuda")
     e2e = replicas.job_throughput(B * e_steps, ws, el)
     h2d = B * W * H

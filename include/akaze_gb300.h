@@ -278,6 +278,16 @@ AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pi
                                      float dt_feature, float s_out, const void *weights_bf16, const float *biases,
                                      void *scratch, float *out, void *stream);
 
+/* akz_batch_detect_describe with packed host output: kpts (capacity
+ * records) and desc (capacity x 61 bytes) receive every image's keypoints
+ * and descriptors back to back, image i starting at row sum_{j<i} counts[j];
+ * counts[i] receives image i's count and *total their sum.  If the sum
+ * exceeds capacity nothing is copied and AKZ_ERR_OVERFLOW is returned (call
+ * again with *total rows).  Two device-to-host copies per call. */
+AKZ_API akz_status akz_batch_detect_describe_packed(akz_batch *b, const uint8_t *const *images, const size_t *strides,
+                                                    akz_keypoint *kpts, uint8_t *desc, int capacity, int *counts,
+                                                    int *total);
+
 /* ---- evaluation and output ---------------------------------------------- */
 
 /* NNDR matches and homography inliers of a 2-NN result, on the device:

@@ -103,3 +103,24 @@ def test_uneven_batch_equals_single_images(gpu_lib, oracle):
         okp, od = orc.run(img)
         assert _exact(kp, okp), (i, w, h)
         assert np.array_equal(d, od), (i, w, h)
+
+
+def test_packed_output_equals_per_image_results(gpu_lib):
+    sizes = synth.uneven_sizes(9, 5)
+    imgs = [synth.synth_image(900 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    b = gpu_lib.Batch(gpu_lib.AKAZEOptions(), sizes)
+    b.upload(imgs)
+    b.run()
+    per = [b.results(i) for i in range(len(sizes))]
+    total = sum(len(k) for k, _ in per)
+    kp = np.zeros(total, gpu_lib.KEYPOINT_DTYPE)
+    d = np.zeros((total, 61), np.uint8)
+    counts = b.detect_describe_packed(imgs, kp, d)
+    assert list(counts) == [len(k) for k, _ in per]
+    off = 0
+    for k, dd in per:
+        assert kp[off:off + len(k)].tobytes() == k.tobytes()
+        assert np.array_equal(d[off:off + len(k)], dd)
+        off += len(k)
+    with pytest.raises(gpu_lib.AkazeError):
+        b.detect_describe_packed(imgs, kp[: total - 1], d[: total - 1])
