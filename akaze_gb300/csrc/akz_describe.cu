@@ -20,6 +20,7 @@
 #include "akz_fmath.h"
 
 #define AKZ_DESC_WARPS 4
+#define AKZ_DESC_MAXIMG 1024 /* images whose keypoint offsets a CTA keeps in shared memory */
 #define AKZ_CV_PI 3.1415926535897932384626433832795
 
 /* orientation samples in the reference's thread order: tx = 16*(j+6) + (i+6) */
@@ -43,16 +44,46 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   akz_warp_smem &S = sm_all[wib];
   const int nwarps = gridDim.x * AKZ_DESC_WARPS;
+  /* keypoint offsets of the images, once per CTA: sOff[i] = sum_{j<i} nkp_j */
+  __shared__ int sOff[AKZ_DESC_MAXIMG + 1];
+  const bool table = p.t.nimg <= AKZ_DESC_MAXIMG;
+  if (table) {
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      for (int b = 0; b < p.t.nimg; b++) {
+        sOff[b] = acc;
+        acc += p.t.stats[b].nkp;
+      }
+      sOff[p.t.nimg] = acc;
+    }
+    __syncthreads();
+  }
   int total = 0;
-  for (int b = 0; b < p.t.nimg; b++) total += p.t.stats[b].nkp;
+  if (table)
+    total = sOff[p.t.nimg];
+  else
+    for (int b = 0; b < p.t.nimg; b++) total += p.t.stats[b].nkp;
   const int ps = p.pattern_size;
   const int size2 = ps, size3 = (int)ceilf(2.0f * (float)ps / 3.0f), size4 = (int)ceilf(0.5f * (float)ps);
   const int win = max(3 * size3, 4 * size4);
   for (int g = blockIdx.x * AKZ_DESC_WARPS + wib; g < total; g += nwarps) {
     int img = 0, k = g;
-    while (k >= p.t.stats[img].nkp) {
-      k -= p.t.stats[img].nkp;
-      img++;
+    if (table) {
+      int lo = 0, hi = p.t.nimg - 1; /* last image with sOff <= g */
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sOff[mid] <= g)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      img = lo;
+      k = g - sOff[lo];
+    } else {
+      while (k >= p.t.stats[img].nkp) {
+        k -= p.t.stats[img].nkp;
+        img++;
+      }
     }
     const akz_image_desc I = p.t.im[img];
     akz_kp *kpp = p.kp + I.kp_base + k;

@@ -823,7 +823,7 @@ static akz_status akz_stage_describe(akz_batch *b, cudaStream_t s)
   /* exp(-r2/12.5) with the shared deterministic exp (the CPU restatement
    * uses the same routine), so the weights are identical on every host */
   for (int r2 = 0; r2 < 36; r2++) p.gw[r2] = akz_expf((float)(-r2) / (2.5f * 2.5f * 2.0f));
-  CK(akz_launch_describe(p, 4 * b->nsm, s));
+  CK(akz_launch_describe(p, 8 * b->nsm, s));
   return AKZ_OK;
 }
 
