@@ -21,6 +21,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 
 #include "akz_device.cuh"
@@ -60,18 +61,20 @@ __device__ __forceinline__ int akz_border_hi(float border, int n)
  * derivative pass the entries just outside the image (within ST) are
  * replaced by their in-image mirrors.
  *
- * Layout: tile 64 x 32, 64-bit pair accesses in row-major flat order. */
+ * Layout: tile (62 - 2 ST) x 32, so the Lx, Ly region is exactly 64 columns
+ * (32 pairs): one warp per row in both passes, no row wraps inside a warp,
+ * hence no shared-memory bank conflicts for the 64-bit pair accesses. */
 template <int ST, bool BORDER>
 __device__ __forceinline__ void akz_detect_tile(const akz_detect_params &p, const akz_level_desc &L, float *sm, int tx0,
                                                 int ty0)
 {
-  constexpr int TW = AKZ_DETECT_TW, TH = AKZ_DETECT_TH;
+  constexpr int TW = 62 - 2 * ST, TH = AKZ_DETECT_TH;
   constexpr int DW = TW + 2 * ST + 2, DH = TH + 2 * ST + 2; /* Lx, Ly:  tile +- (ST+1)  */
   constexpr int SW = TW + 4 * ST + 2, SH = TH + 4 * ST + 2; /* Lsmooth: tile +- (2ST+1) */
   constexpr int SWS = SW;                                   /* Lsmooth row stride */
   constexpr int EW = TW + 2, EH = TH + 2;                   /* Ldet:    tile +- 1       */
   constexpr int DP = DW / 2, EP = EW / 2;                   /* column pairs */
-  static_assert(DW % 2 == 0 && EW % 2 == 0 && SW % 2 == 0, "pair layout");
+  static_assert(DW == 64 && EP <= 32 && EW % 2 == 0 && SW % 2 == 0, "pair layout");
   static_assert(EW * EH <= SWS * SH, "determinant plane fits the Lsmooth region");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int W = L.width, H = L.height;
@@ -108,8 +111,8 @@ __device__ __forceinline__ void akz_detect_tile(const akz_detect_params &p, cons
    * outer taps are aligned pairs for every ST (cuda_akaze.cu:651-671) */
   const int dx0 = tx0 - ST - 1, dy0 = ty0 - ST - 1; /* image coordinates of D (0, 0) */
   float *lxp = p.t.planes + L.lx, *lyp = p.t.planes + L.ly;
-  for (int i = tid; i < DH * DP; i += 256) {
-    const int n = i / DP, d = 2 * (i - n * DP);
+  for (int n = warp; n < DH; n += 8) {
+    const int d = 2 * lane;
     const float *su = sS + n * SWS + d, *sc = su + ST * SWS, *sd = su + 2 * ST * SWS;
     const float2 ul = ld2(su), ur = ld2(su + 2 * ST), ll = ld2(sd), lr = ld2(sd + 2 * ST);
     const float2 cl = ld2(sc), cr = ld2(sc + 2 * ST);
@@ -162,8 +165,9 @@ __device__ __forceinline__ void akz_detect_tile(const akz_detect_params &p, cons
   }
   /* Hessian determinant on the tile +- 1 (cuda_akaze.cu:673-701): E column e
    * is D column e + ST */
-  for (int i = tid; i < EH * EP; i += 256) {
-    const int n = i / EP, e = 2 * (i - n * EP);
+  for (int n = warp; n < EH; n += 8) {
+    const int e = 2 * lane;
+    if (lane >= EP) continue;
     const float *xu = sX + n * DW + e, *xc = xu + ST * DW, *xd = xu + 2 * ST * DW;
     const float *yu = sY + n * DW + e, *yd = yu + 2 * ST * DW;
     const float2 ul = ld2(xu), ur = ld2(xu + 2 * ST), ll = ld2(xd), lr = ld2(xd + 2 * ST);
@@ -217,7 +221,8 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const int W = L.width, H = L.height, st = L.deriv_step;
   const int lt = blockIdx.x - sg.tile_begin;
-  const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
+  const int tw = akz_detect_tile_width(st);
+  const int tx0 = (lt % sg.tiles_x) * tw, ty0 = (lt / sg.tiles_x) * TH;
   const int tx1 = min(tx0 + TW, W), ty1 = min(ty0 + TH, H);
   const int sx0 = max(tx0 - 2 * st - 1, 0), sx1 = min(tx1 + 2 * st + 1, W);
   const int sy0 = max(ty0 - 2 * st - 1, 0), sy1 = min(ty1 + 2 * st + 1, H);
@@ -226,7 +231,7 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   const int ex0 = max(tx0 - 1, 0), ex1 = min(tx1 + 1, W), ey0 = max(ty0 - 1, 0), ey1 = min(ty1 + 1, H);
   const int sw = sx1 - sx0, dw = dx1 - dx0, ew = ex1 - ex0;
   if (st >= 2 && st <= 4 && st <= max_step) {
-    const bool border = tx0 - 2 * st - 1 < 0 || ty0 - 2 * st - 1 < 0 || tx0 + TW + 2 * st + 1 > W ||
+    const bool border = tx0 - 2 * st - 1 < 0 || ty0 - 2 * st - 1 < 0 || tx0 + tw + 2 * st + 1 > W ||
                         ty0 + TH + 2 * st + 1 > H;
     if (border) {
       if (st == 2)
@@ -681,10 +686,14 @@ cudaError_t akz_launch_detect(const akz_detect_params &p, int ntiles, int max_st
 {
   if (ntiles <= 0) return cudaSuccess;
   /* Lsmooth region + Lx, Ly regions; the determinant plane reuses the
-   * Lsmooth region */
-  const size_t SM = (size_t)(AKZ_DETECT_TW + 4 * max_step + 2) * (AKZ_DETECT_TH + 4 * max_step + 2);
-  const size_t DM = (size_t)(AKZ_DETECT_TW + 2 * max_step + 2) * (AKZ_DETECT_TH + 2 * max_step + 2);
-  const size_t smem = (SM + 2 * DM) * sizeof(float);
+   * Lsmooth region.  General path at AKZ_DETECT_TW, akz_detect_tile at its
+   * narrower per-step width. */
+  size_t words = 0;
+  for (int st = 1; st <= max_step; st++) {
+    const size_t tw = (size_t)akz_detect_tile_width(st);
+    words = std::max(words, (tw + 4 * st + 2) * (AKZ_DETECT_TH + 4 * st + 2) + 2 * (tw + 2 * st + 2) * (AKZ_DETECT_TH + 2 * st + 2));
+  }
+  const size_t smem = words * sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(k_detect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k_detect<<<ntiles, 256, smem, s>>>(p, max_step);

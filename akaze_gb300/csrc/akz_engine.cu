@@ -575,7 +575,8 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
   b->detect_off = (int)b->segs.size();
   for (int i = 0; i < n; i++)
     for (int l = 0; l < b->im[i].nlev; l++)
-      add_tiles(b->im[i].first_level + l, b->geo[i][l].w, b->geo[i][l].h, AKZ_DETECT_TW, AKZ_DETECT_TH, 0, b->detect_tiles);
+      add_tiles(b->im[i].first_level + l, b->geo[i][l].w, b->geo[i][l].h, akz_detect_tile_width(b->geo[i][l].deriv_step),
+                AKZ_DETECT_TH, 0, b->detect_tiles);
   b->detect_n = (int)b->segs.size() - b->detect_off;
   b->extract_off = (int)b->segs.size();
   for (int i = 0; i < n; i++)

@@ -149,6 +149,10 @@ cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaS
 
 #define AKZ_DETECT_TW 64
 #define AKZ_DETECT_TH 32
+/* Detector tile width of a level with derivative step st: 62 - 2 st for the
+ * compiled steps 2..4 (the Lx, Ly region is then exactly 64 columns, 32
+ * pairs: one warp per row), AKZ_DETECT_TW otherwise. */
+static inline __host__ __device__ int akz_detect_tile_width(int st) { return st >= 2 && st <= 4 ? 62 - 2 * st : AKZ_DETECT_TW; }
 #define AKZ_GAUSS_TW 64
 #define AKZ_GAUSS_TH 32
 #define AKZ_CONTRAST_TW 64
