@@ -182,6 +182,165 @@ __global__ void __launch_bounds__(128) k_sg_conv_mma(const __nv_bfloat16 *__rest
     }
 }
 
+/* ------------------------------------------------------------------------ */
+/* tcgen05 path for the 32 -> 32 layers (layer 1 as 1 x 1, layers 2-4 as
+ * 3 x 3): a CTA of 4 warps computes 128 consecutive pixels of one row,
+ * D[128 x 32] (FP32, in TMEM) += A[128 x K] * B[K x 32] in K steps of 16.
+ *
+ * Shared-memory operands use the canonical K-major layout without swizzle:
+ * 8-row x 16-byte core matrices, row r of a core matrix at r * 16 bytes;
+ * core matrices adjacent in K are LBO = 128 bytes apart, adjacent in M / N
+ * SBO bytes apart.  A: per tap a [16 row groups][4 K groups] block (SBO =
+ * 512, 8 KB per tap); B: [4 row groups][K / 8 K groups] (SBO = K * 16).
+ * One elected thread issues the MMAs and commits them to an mbarrier; the
+ * wait is bounded (AKZ_SG_TC_SPIN polls), after which the CTA records an
+ * error and still frees its TMEM. */
+
+#define AKZ_SG_TC_SPIN (1 << 24)
+
+__device__ __forceinline__ uint64_t sg_smem_desc(const void *p, uint32_t lbo, uint32_t sbo)
+{
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  uint64_t d = 0;
+  d |= (uint64_t)((a & 0x3FFFF) >> 4);          /* start address, bits 0-13 */
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;   /* leading dimension byte offset */
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;   /* stride dimension byte offset */
+  d |= (uint64_t)1 << 46;                       /* descriptor version */
+  return d;                                     /* base offset 0, no swizzle */
+}
+
+/* kind::f16 instruction descriptor: D F32, A and B BF16, both K-major */
+__host__ __device__ constexpr uint32_t sg_idesc(int M, int N)
+{
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+template <int NTAPS>
+__global__ void __launch_bounds__(128) k_sg_conv_tc(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ wt,
+                                                    const float *__restrict__ bias, __nv_bfloat16 *__restrict__ out,
+                                                    akz_sg_level lv, int *err)
+{
+  constexpr int K = NTAPS * 32;
+  constexpr int A_BYTES = NTAPS * 128 * 64, B_BYTES = 32 * K * 2;
+  extern __shared__ __align__(1024) unsigned char tcsm[];
+  unsigned char *sA = tcsm, *sB = tcsm + A_BYTES;
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ uint32_t tbase;
+  __shared__ float sBias[32];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int W = lv.W, H = lv.H;
+  const int x0 = blockIdx.x * 128, y = blockIdx.y;
+
+  /* B: weight row n, K group kg -> core matrix (n / 8, kg), row n % 8 */
+  for (int i = tid; i < 32 * (K / 8); i += 128) {
+    const int n = i / (K / 8), kg = i - n * (K / 8);
+    *(uint4 *)(sB + (n >> 3) * (K * 16) + kg * 128 + (n & 7) * 16) = *(const uint4 *)(wt + n * K + kg * 8);
+  }
+  /* A: tap t, pixel m (x0 + m), channel group kg -> tap block t, core (m / 8, kg), row m % 8 */
+  for (int i = tid; i < NTAPS * 128 * 4; i += 128) {
+    const int t = i / 512, r = i - t * 512, m = r >> 2, kg = r & 3;
+    const int dy = NTAPS == 9 ? t / 3 - 1 : 0, dx = NTAPS == 9 ? t % 3 - 1 : 0;
+    const int yy = sg_clamp(y + dy, 0, H - 1), xx = sg_clamp(x0 + m + dx, 0, W - 1);
+    *(uint4 *)(sA + t * 8192 + (m >> 3) * 512 + kg * 128 + (m & 7) * 16) =
+        *(const uint4 *)(in + ((long long)yy * W + xx) * 32 + kg * 8);
+  }
+  if (tid < 32) sBias[tid] = bias[tid];
+  if (warp == 0) {
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tbase);
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(dst));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;"); /* generic-proxy writes -> tensor core reads */
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tbase;
+  if (tid == 0) {
+    constexpr uint32_t idesc = sg_idesc(128, 32);
+#pragma unroll 1
+    for (int s = 0; s < K / 16; s++) {
+      const int t = s >> 1, kc = s & 1;
+      const uint64_t ad = sg_smem_desc(sA + t * 8192 + kc * 256, 128, 512);
+      const uint64_t bd = sg_smem_desc(sB + (2 * s) * 128, 128, K * 16);
+      const uint32_t acc = s > 0 ? 1u : 0u;
+      asm volatile(
+          "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+          "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+    }
+    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb));
+  }
+  /* bounded wait for the MMAs */
+  {
+    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
+    uint32_t done = 0;
+    for (int it = 0; it < AKZ_SG_TC_SPIN && !done; it++)
+      asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
+                   : "=r"(done)
+                   : "r"(mb));
+    if (!done) atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  /* epilogue: warp w reads TMEM lanes 32w .. 32w+31 (its 32 pixels) x 32 columns */
+  uint32_t r[32];
+  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+  const int x = x0 + warp * 32 + lane;
+  if (x < W) {
+    __align__(16) __nv_bfloat162 v[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++)
+      v[c] = __floats2bfloat162_rn(fmaxf(__uint_as_float(r[2 * c]) + sBias[2 * c], 0.0f),
+                                   fmaxf(__uint_as_float(r[2 * c + 1]) + sBias[2 * c + 1], 0.0f));
+    uint4 *dst = (uint4 *)(out + ((long long)y * W + x) * 32);
+    const uint4 *src = (const uint4 *)v;
+#pragma unroll
+    for (int c = 0; c < 4; c++) dst[c] = src[c];
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem));
+}
+
+/* tcgen05 path switch for the 32 -> 32 layers (off: mma.sync), and the
+ * flag its kernels set when an MMA wait ran out. */
+static int g_sg_tc = 0;
+static __device__ int g_sg_tc_err;
+
+extern "C" AKZ_API akz_status akz_sg_set_tcgen05(int on)
+{
+  g_sg_tc = on ? 1 : 0;
+  return AKZ_OK;
+}
+
+extern "C" AKZ_API akz_status akz_sg_tcgen05_status(int *timed_out)
+{
+  if (!timed_out) return akz_report(AKZ_ERR_INVALID_ARG, "akz_sg_tcgen05_status: NULL");
+  int v = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, g_sg_tc_err, sizeof(int));
+  if (e == cudaSuccess) {
+    const int z = 0;
+    e = cudaMemcpyToSymbol(g_sg_tc_err, &z, sizeof(int));
+  }
+  if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
+  *timed_out = v;
+  return AKZ_OK;
+}
+
 /* Packed weights (bf16): layer 1 [32][32], layers 2-4 [32][288], layer 5
  * [8][288] (rows 1-7 zero); biases (f32): 4 x 32 + 8. */
 #define SG_W1 (32 * 32)
@@ -212,10 +371,24 @@ extern "C" AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g
   __nv_bfloat16 *a0 = (__nv_bfloat16 *)scratch, *a1 = a0 + (size_t)width * height * 32;
   k_sg_im2col<<<dim3((width + 127) / 128, height), 128, 0, s>>>(lv, a0);
   const dim3 grid((width + SG_BX - 1) / SG_BX, (height + SG_BY - 1) / SG_BY);
-  k_sg_conv_mma<1, 4, false><<<grid, 128, 0, s>>>(a0, w, biases, a1, lv);
-  k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a1, w + SG_W1, biases + 32, a0, lv);
-  k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a0, w + SG_W1 + SG_W3, biases + 64, a1, lv);
-  k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a1, w + SG_W1 + 2 * SG_W3, biases + 96, a0, lv);
+  if (g_sg_tc) {
+    int *err = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&err, g_sg_tc_err);
+    constexpr int smem1 = 1 * 128 * 64 + 32 * 32 * 2, smem9 = 9 * 128 * 64 + 32 * 288 * 2;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sg_conv_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sg_conv_tc<9>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem9);
+    if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
+    const dim3 gt((width + 127) / 128, height);
+    k_sg_conv_tc<1><<<gt, 128, smem1, s>>>(a0, w, biases, a1, lv, err);
+    k_sg_conv_tc<9><<<gt, 128, smem9, s>>>(a1, w + SG_W1, biases + 32, a0, lv, err);
+    k_sg_conv_tc<9><<<gt, 128, smem9, s>>>(a0, w + SG_W1 + SG_W3, biases + 64, a1, lv, err);
+    k_sg_conv_tc<9><<<gt, 128, smem9, s>>>(a1, w + SG_W1 + 2 * SG_W3, biases + 96, a0, lv, err);
+  } else {
+    k_sg_conv_mma<1, 4, false><<<grid, 128, 0, s>>>(a0, w, biases, a1, lv);
+    k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a1, w + SG_W1, biases + 32, a0, lv);
+    k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a0, w + SG_W1 + SG_W3, biases + 64, a1, lv);
+    k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a1, w + SG_W1 + 2 * SG_W3, biases + 96, a0, lv);
+  }
   k_sg_conv_mma<9, 1, true><<<grid, 128, 0, s>>>(a0, w + SG_W1 + 3 * SG_W3, biases + 128, nullptr, lv);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));

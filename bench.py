@@ -56,6 +56,8 @@ def parse():
                     help="small case for ncu: --batch images, one graph-less run of every stage, no timing line")
     ap.add_argument("--weights", default=os.path.join(ROOT, "akaze_gb300", "surrogate_weights.npz"),
                     help="surrogate4k: trained surrogate weights (python -m akaze_gb300.surrogate train)")
+    ap.add_argument("--sg-tcgen05", type=int, default=0, choices=[0, 1],
+                    help="surrogate4k: run the net's 32-channel layers on tcgen05 (1) or mma.sync (0)")
     ap.add_argument("--check-tol", type=float, default=2e-3,
                     help="surrogate4k: per-level tolerance of the surrogate against plain FED before it falls back")
     ap.add_argument("--workload", default="batch1080p",
@@ -424,6 +426,7 @@ def workload_surrogate4k(args):
         print(json.dumps({"workload": "surrogate4k", "unavailable": f"no trained weights at {args.weights}"}))
         return 0
     params = sg.load_params(args.weights)
+    akz._lib.check(akz._lib.load().akz_sg_set_tcgen05(args.sg_tcgen05))
     W, H, B = 3840, 2160, min(args.batch, 8)
     imgs = [synth.synth_image(9000 + i, W, H) for i in range(B)]
     opt = akz.AKAZEOptions(omax=6)
@@ -449,7 +452,8 @@ def workload_surrogate4k(args):
         res[mode] = out
         b.close()
     line = {"workload": "surrogate4k", "config": f"{B} synthetic 3840x2160 u8, 6 octaves x 4 sublevels, surrogate on "
-            "octaves >= 1 (BF16 tensor-core net, 5 layers x 32 channels)", "check_tol": args.check_tol}
+            "octaves >= 1 (BF16 tensor-core net, 5 layers x 32 channels)", "check_tol": args.check_tol,
+            "tensor_path": "tcgen05" if args.sg_tcgen05 else "mma.sync"}
     for mode, out in res.items():
         r = {k: v for k, v in out.items() if k != "results"}
         if mode != "plain":

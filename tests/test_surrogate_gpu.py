@@ -42,7 +42,8 @@ def test_training_kernels_match_numpy(gpu_lib):
         assert _close(net.gb[i].cpu().numpy(), db, 1e-3), f"db {i}"
 
 
-def test_inference_kernel_matches_bf16_emulation(gpu_lib):
+@pytest.mark.parametrize("tcgen05", [False, True])
+def test_inference_kernel_matches_bf16_emulation(gpu_lib, tcgen05):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(5)
     params = [(rng.normal(0, np.sqrt(2.0 / (ci * 9)), (co, ci, 3, 3)).astype(np.float32),
@@ -62,12 +63,16 @@ def test_inference_kernel_matches_bf16_emulation(gpu_lib):
     dw = torch.from_numpy(blob.view(np.int16).copy()).cuda()
     db = torch.from_numpy(biases).cuda()
     scratch = torch.empty(2 * H * W * 64, dtype=torch.uint8, device="cuda")
+    lib.akz_sg_set_tcgen05(int(tcgen05))
     st = lib.akz_sg_infer_level(ctypes.c_void_p(dl.data_ptr()), ctypes.c_void_p(dg.data_ptr()), pitch, W, H,
                                 ctypes.c_float(dtf), ctypes.c_float(s_out), ctypes.c_void_p(dw.data_ptr()),
                                 ctypes.c_void_p(db.data_ptr()), ctypes.c_void_p(scratch.data_ptr()),
                                 ctypes.c_void_p(dout.data_ptr()), None)
     assert st == 0, lib.akz_last_error()
     torch.cuda.synchronize()
+    lib.akz_sg_set_tcgen05(0)
+    timed_out = ctypes.c_int(-1)
+    assert lib.akz_sg_tcgen05_status(ctypes.byref(timed_out)) == 0 and timed_out.value == 0
     got = (dout.cpu().numpy()[:, :W].astype(np.float64) - l0) / s_out
 
     def bf(a):
