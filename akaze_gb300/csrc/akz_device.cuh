@@ -117,6 +117,13 @@ __device__ __forceinline__ float2 f2sub(float2 a, float2 b)
   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(akz_f2u(a)), "l"(akz_f2u(b)));
   return akz_u2f(r);
 }
+/* Explicit packed fused multiply-add (one rounding per lane, as fmaf). */
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c)
+{
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(akz_f2u(a)), "l"(akz_f2u(b)), "l"(akz_f2u(c)));
+  return akz_u2f(r);
+}
 __device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
 __device__ __forceinline__ void st2(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
 

@@ -20,8 +20,11 @@
  */
 #include <cuda_runtime.h>
 
+#include "../../include/akaze_gb300.h"
 #include "akz_device.cuh"
 #include "akz_fmath.h"
+
+akz_status akz_report(akz_status s, const char *msg);
 
 /* ------------------------------------------------------------------------ */
 /* Contrast factor                                                          */
@@ -445,6 +448,41 @@ __device__ __forceinline__ float akz_conductance_m(float m, float inv_k, int typ
   return (float)(1.0 / (double)den);
 }
 
+/* PM-g2 conductance of two pixels, (float)(1.0 / (1.0 + (double)f)) with
+ * f = inv_k * m per lane, exactly as akz_recip1pf gives it.  The reciprocal
+ * of s = fl(1 + f) starts from the hardware approximation (relative error
+ * below 2^-22); one Newton step against the exact float-float sum s + lo
+ * (Fast2Sum) leaves the value before the final rounding within about 2^-43
+ * of 1 / (1 + f), inside the 2^-41 band of the rounding-midpoint test, so
+ * every lane that could round differently takes the double evaluation. */
+__device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
+{
+  const float2 f = make_float2(inv_k * m.x, inv_k * m.y);
+  const float2 one = make_float2(1.0f, 1.0f);
+  const float2 s = f2add(one, f);
+  const float2 a = f2sub(one, f2sub(s, f)), b = f2sub(f, f2sub(s, one)); /* Fast2Sum, both orderings */
+  const float2 lo = make_float2(f.x >= 1.0f ? a.x : b.x, f.y >= 1.0f ? a.y : b.y);
+  float2 q;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(q.x) : "f"(s.x));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(q.y) : "f"(s.y));
+  const float2 nq = make_float2(-q.x, -q.y);
+  const float2 r = f2fma(nq, lo, f2fma(nq, s, one)); /* 1 - q (s + lo) */
+  const float2 res = f2fma(q, r, q);
+  const float2 e = f2sub(make_float2(q.x * r.x, q.y * r.y), f2sub(res, q));
+  float out[2] = {res.x, res.y};
+  const float ff[2] = {f.x, f.y}, ee[2] = {e.x, e.y};
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const unsigned int u = __float_as_uint(out[k]);
+    const float up = __uint_as_float((u & 0x7f800000u) - (23u << 23));
+    const float dn = (u & 0x007fffffu) ? up : up * 0.5f;
+    const float tol = up * 0x1p-18f, err = fabsf(ee[k]);
+    if (!(ff[k] <= 0x1p100f) || fabsf(err - 0.5f * up) <= tol || fabsf(err - 0.5f * dn) <= tol)
+      out[k] = (float)(1.0 / (1.0 + (double)ff[k]));
+  }
+  return make_float2(out[0], out[1]);
+}
+
 /* First-chunk prologue of k_fed: the level's starting image on R0 +- 3, its
  * sigma-1 smoothing Lsmooth (written to HBM for the tile) and the conductance
  * on R0 (written to HBM for the tile when more chunks follow).
@@ -613,7 +651,9 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
     const float2 gx = f2add(make_float2(3.0f * u.x, 3.0f * u.y), make_float2(10.0f * dh[r + 1].x, 10.0f * dh[r + 1].y));
     const float2 gy = f2sub(sh[r + 2], sh[r]);
     const float2 m = f2add(make_float2(gx.x * gx.x, gx.y * gx.y), make_float2(gy.x * gy.x, gy.y * gy.y));
-    const float2 gv = make_float2(akz_conductance_m(m.x, inv_k, p.diffusivity), akz_conductance_m(m.y, inv_k, p.diffusivity));
+    const float2 gv = p.diffusivity == 1 ? akz_pm_g2_pair(m, inv_k)
+                                         : make_float2(akz_conductance_m(m.x, inv_k, p.diffusivity),
+                                                       akz_conductance_m(m.y, inv_k, p.diffusivity));
     st2(sG + (ly0 + r) * RW + lx0, gv);
     const int y = oy + ly0 + r;
     if (y >= ty0 && y < ty1) {
@@ -866,4 +906,31 @@ cudaError_t akz_launch_area(const akz_area_params &p, int maxw, int maxh, cudaSt
   const dim3 grid((maxw + 31) / 32, (maxh + 7) / 8, p.nsegs);
   k_area<<<grid, block, 0, s>>>(p);
   return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------ */
+/* Device self-check of the exact PM-g2 reciprocal: out[i] = the conductance
+ * of f = in[i] (inv_k = 1) from the pair routine (fn 0) or the scalar one
+ * (fn 1), for comparison with (float)(1 / (1 + (double)f)) on the host. */
+__global__ void k_pm_g2_check(const float *in, float *out, int n, int fn)
+{
+  const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= n) return;
+  const float a = in[i], b = i + 1 < n ? in[i + 1] : 0.0f;
+  float2 r;
+  if (fn == 0)
+    r = akz_pm_g2_pair(make_float2(a, b), 1.0f);
+  else
+    r = make_float2(akz_recip1pf(a), akz_recip1pf(b));
+  out[i] = r.x;
+  if (i + 1 < n) out[i + 1] = r.y;
+}
+
+extern "C" AKZ_API akz_status akz_selfcheck_pm_g2(const float *in, float *out, int n, int fn, void *stream)
+{
+  if (n < 0 || (n > 0 && (!in || !out)) || fn < 0 || fn > 1) return akz_report(AKZ_ERR_INVALID_ARG, "akz_selfcheck_pm_g2: bad arguments");
+  if (n == 0) return AKZ_OK;
+  k_pm_g2_check<<<((n + 1) / 2 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(in, out, n, fn);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? AKZ_OK : akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
 }

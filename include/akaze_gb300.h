@@ -294,6 +294,12 @@ AKZ_API akz_status akz_batch_detect_describe_packed(akz_batch *b, const uint8_t 
                                                     akz_keypoint *kpts, uint8_t *desc, int capacity, int *counts,
                                                     int *total);
 
+/* Self-check of the device's exact PM-g2 reciprocal (no counterpart in the
+ * reference): out[i] = (float)(1 / (1 + (double)in[i])) as the level kernel
+ * computes it, by its two-pixel routine (fn 0) or the scalar one (fn 1).
+ * Device buffers; asynchronous on stream.  For tests of that exactness. */
+AKZ_API akz_status akz_selfcheck_pm_g2(const float *in, float *out, int n, int fn, void *stream);
+
 /* ---- evaluation and output ---------------------------------------------- */
 
 /* NNDR matches and homography inliers of a 2-NN result, on the device:
