@@ -302,6 +302,17 @@ class Batch:
                                                 ctypes.c_float(surrogate.S_OUT if s_out is None else s_out),
                                                 int(first_octave), ctypes.c_float(check_tol)))
 
+    def autotune(self):
+        """Pick the FED blocking depth (4..8) by timing the uploaded batch;
+        returns (depth, {depth: ms})."""
+        ms = np.zeros(5, np.float32)
+        d = ctypes.c_int()
+        check(self._lib.akz_batch_autotune(self._h, _ptr(ms), 5, ctypes.byref(d)))
+        return d.value, {4 + k: float(v) for k, v in enumerate(ms)}
+
+    def set_fed_depth(self, depth):
+        check(self._lib.akz_batch_set_fed_depth(self._h, int(depth)))
+
     def surrogate_errors(self):
         n = ctypes.c_int()
         check(self._lib.akz_batch_surrogate_errors(self._h, None, 0, ctypes.byref(n)))

@@ -228,6 +228,9 @@ static akz_status akz_validate(const akz_options *o)
 /* ------------------------------------------------------------------------ */
 /* batch                                                                    */
 
+#define AKZ_DEPTH_MIN 4            /* smallest FED blocking depth the autotuner tries */
+#define AKZ_MAX_STEPS_PER_LAUNCH 8 /* k_fed's largest depth */
+
 struct akz_fed_launch {
   int seg_off, nsegs, ntiles, tw, th;
   akz_fed_params p;
@@ -255,7 +258,12 @@ struct akz_batch {
   int l0_off = 0, l0_n = 0, l0_tiles = 0; /* k_level0 tiles */
   int detect_off = 0, detect_n = 0, detect_tiles = 0;
   int extract_off = 0, extract_n = 0, extract_rows = 0;
-  std::vector<std::vector<akz_fed_launch>> fed;  /* per level index */
+  std::vector<std::vector<akz_fed_launch>> fed;  /* per level index: the launches in use */
+  /* the level stage's launches for every FED blocking depth (most steps per
+   * launch) AKZ_DEPTH_MIN .. AKZ_MAX_STEPS_PER_LAUNCH; akz_batch_autotune
+   * picks one, the default is the largest */
+  std::vector<std::vector<std::vector<akz_fed_launch>>> fed_alt;
+  int fed_depth = 8;
   /* learned surrogate (akz_batch_set_surrogate): per level, the zero-step
    * launch that forms Lsmooth, the conductance and the start image, and the
    * plain chunks of image 0 into the check plane */
@@ -483,12 +491,12 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
   b->l0_n = (int)b->segs.size() - b->l0_off;
 
   b->fed.resize(b->maxlev);
+  b->fed_alt.assign(AKZ_MAX_STEPS_PER_LAUNCH - AKZ_DEPTH_MIN + 1, std::vector<std::vector<akz_fed_launch>>(b->maxlev));
   b->area.resize(b->maxlev);
   b->sg_prep.resize(b->maxlev);
   b->sg_check.resize(b->maxlev);
   for (int l = 1; l < b->maxlev; l++) {
     const int nsteps = (int)b->tau[l].size();
-    const int nch = std::max(1, (nsteps + 7) / 8);
     /* area tables for octave starts whose predecessor is not exactly 2x */
     akz_area_launch al{(int)b->area_segs.size(), 0, 0, 0};
     for (int i = 0; i < n; i++) {
@@ -509,46 +517,54 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
       }
     }
     b->area[l] = al;
-    int done = 0;
-    for (int c = 0; c < nch; c++) {
-      const int steps = (nsteps - done + (nch - c) - 1) / (nch - c);
-      akz_fed_launch fl;
-      memset(&fl, 0, sizeof(fl));
-      fl.tw = 128 - 2 * steps; /* k_fed region is 128 x 40 = tile +- steps */
-      fl.th = 40 - 2 * steps;
-      fl.seg_off = (int)b->segs.size();
-      for (int i = 0; i < n; i++) {
-        if (b->im[i].nlev <= l) continue;
-        const akz_geo &g = b->geo[i][l], &gp = b->geo[i][l - 1];
-        int src = 0;
-        if (g.octave > gp.octave) src = (gp.w == 2 * g.w && gp.h == 2 * g.h) ? 1 : 2;
-        add_tiles(b->im[i].first_level + l, g.w, g.h, fl.tw, fl.th, src, fl.ntiles);
+    /* FED chunks of at most `depth` steps; with chk, the same chunks for
+     * image 0 alone, the last one into the check plane */
+    auto chunks = [&](int depth, std::vector<akz_fed_launch> &out, std::vector<akz_fed_launch> *chk) {
+      const int nch = std::max(1, (nsteps + depth - 1) / depth);
+      int done = 0;
+      for (int c = 0; c < nch; c++) {
+        const int steps = (nsteps - done + (nch - c) - 1) / (nch - c);
+        akz_fed_launch fl;
+        memset(&fl, 0, sizeof(fl));
+        fl.tw = 128 - 2 * steps; /* k_fed region is 128 x 40 = tile +- steps */
+        fl.th = 40 - 2 * steps;
+        fl.seg_off = (int)b->segs.size();
+        for (int i = 0; i < n; i++) {
+          if (b->im[i].nlev <= l) continue;
+          const akz_geo &g = b->geo[i][l], &gp = b->geo[i][l - 1];
+          int src = 0;
+          if (g.octave > gp.octave) src = (gp.w == 2 * g.w && gp.h == 2 * g.h) ? 1 : 2;
+          add_tiles(b->im[i].first_level + l, g.w, g.h, fl.tw, fl.th, src, fl.ntiles);
+        }
+        fl.nsegs = (int)b->segs.size() - fl.seg_off;
+        fl.p.steps = steps;
+        fl.p.first = c == 0;
+        fl.p.src = c == 0 ? 0 : ((c - 1) % 2 == 0 ? 1 : 2);
+        fl.p.dst = c == nch - 1 ? 0 : (c % 2 == 0 ? 1 : 2);
+        fl.p.write_g = (c == 0 && nch > 1) ? 1 : 0;
+        fl.p.diffusivity = opt->diffusivity;
+        for (int k = 0; k < 5; k++) fl.p.taps1[k] = b->taps1[k];
+        for (int k = 0; k < steps; k++) fl.p.h[k] = 0.5f * b->tau[l][done + k];
+        done += steps;
+        out.push_back(fl);
+        if (!chk) continue;
+        akz_fed_launch cl = fl;
+        cl.seg_off = (int)b->segs.size();
+        cl.ntiles = 0;
+        if (b->im[0].nlev > l) {
+          const akz_geo &g = b->geo[0][l], &gp = b->geo[0][l - 1];
+          int src = 0;
+          if (g.octave > gp.octave) src = (gp.w == 2 * g.w && gp.h == 2 * g.h) ? 1 : 2;
+          add_tiles(b->im[0].first_level + l, g.w, g.h, cl.tw, cl.th, src, cl.ntiles);
+        }
+        cl.nsegs = (int)b->segs.size() - cl.seg_off;
+        if (c == nch - 1) cl.p.dst = 3;
+        chk->push_back(cl);
       }
-      fl.nsegs = (int)b->segs.size() - fl.seg_off;
-      fl.p.steps = steps;
-      fl.p.first = c == 0;
-      fl.p.src = c == 0 ? 0 : ((c - 1) % 2 == 0 ? 1 : 2);
-      fl.p.dst = c == nch - 1 ? 0 : (c % 2 == 0 ? 1 : 2);
-      fl.p.write_g = (c == 0 && nch > 1) ? 1 : 0;
-      fl.p.diffusivity = opt->diffusivity;
-      for (int k = 0; k < 5; k++) fl.p.taps1[k] = b->taps1[k];
-      for (int k = 0; k < steps; k++) fl.p.h[k] = 0.5f * b->tau[l][done + k];
-      done += steps;
-      b->fed[l].push_back(fl);
-      /* the same chunk for image 0 alone, the last one into the check plane */
-      akz_fed_launch cl = fl;
-      cl.seg_off = (int)b->segs.size();
-      cl.ntiles = 0;
-      if (b->im[0].nlev > l) {
-        const akz_geo &g = b->geo[0][l], &gp = b->geo[0][l - 1];
-        int src = 0;
-        if (g.octave > gp.octave) src = (gp.w == 2 * g.w && gp.h == 2 * g.h) ? 1 : 2;
-        add_tiles(b->im[0].first_level + l, g.w, g.h, cl.tw, cl.th, src, cl.ntiles);
-      }
-      cl.nsegs = (int)b->segs.size() - cl.seg_off;
-      if (c == nch - 1) cl.p.dst = 3;
-      b->sg_check[l].push_back(cl);
-    }
+    };
+    for (int depth = AKZ_DEPTH_MIN; depth < AKZ_MAX_STEPS_PER_LAUNCH; depth++)
+      chunks(depth, b->fed_alt[depth - AKZ_DEPTH_MIN][l], nullptr);
+    chunks(AKZ_MAX_STEPS_PER_LAUNCH, b->fed[l], &b->sg_check[l]);
     /* zero FED steps over 128 x 40 tiles: Lsmooth, the conductance (kept)
      * and the start image in Lt */
     akz_fed_launch pl;
@@ -571,7 +587,9 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
     pl.p.diffusivity = opt->diffusivity;
     for (int k = 0; k < 5; k++) pl.p.taps1[k] = b->taps1[k];
     b->sg_prep[l] = pl;
+    b->fed_alt[AKZ_MAX_STEPS_PER_LAUNCH - AKZ_DEPTH_MIN][l] = b->fed[l];
   }
+  b->fed_depth = AKZ_MAX_STEPS_PER_LAUNCH;
   b->detect_off = (int)b->segs.size();
   for (int i = 0; i < n; i++)
     for (int l = 0; l < b->im[i].nlev; l++)
@@ -1447,6 +1465,52 @@ AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *q64
   if (nq == 0) return AKZ_OK;
   if (!q64 || !out || (nt > 0 && !t64)) return akz_fail(AKZ_ERR_INVALID_ARG, "NULL matcher buffer");
   return akz_match_device(m, q64, nq, t64, nt, out);
+}
+
+AKZ_API akz_status akz_batch_set_fed_depth(akz_batch *b, int depth)
+{
+  AKZ_GUARD(b);
+  if (depth < AKZ_DEPTH_MIN || depth > AKZ_MAX_STEPS_PER_LAUNCH)
+    return akz_report(AKZ_ERR_INVALID_ARG, "akz_batch_set_fed_depth: depth must be 4..8");
+  b->fed = b->fed_alt[depth - AKZ_DEPTH_MIN];
+  b->fed_depth = depth;
+  if (b->graph) { /* the captured graph holds the old launches */
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  return AKZ_OK;
+}
+
+/* FED blocking depth autotuner: times the level stage of the uploaded
+ * batch for each depth and keeps the fastest. */
+AKZ_API akz_status akz_batch_autotune(akz_batch *b, float *ms_per_depth, int cap, int *depth)
+{
+  AKZ_GUARD(b);
+  const int nd = AKZ_MAX_STEPS_PER_LAUNCH - AKZ_DEPTH_MIN + 1;
+  cudaEvent_t e0 = b->ev[6], e1 = b->ev[7];
+  float best = 1e30f;
+  int best_d = b->fed_depth;
+  for (int k = 0; k < nd; k++) {
+    b->fed = b->fed_alt[k];
+    float tmin = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+      CK(cudaEventRecord(e0, b->stream));
+      akz_status st = akz_stage_scale(b, b->stream);
+      if (st != AKZ_OK) return st;
+      CK(cudaEventRecord(e1, b->stream));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep > 0) tmin = std::min(tmin, ms); /* the first repetition warms up */
+    }
+    if (ms_per_depth && k < cap) ms_per_depth[k] = tmin;
+    if (tmin < best) {
+      best = tmin;
+      best_d = AKZ_DEPTH_MIN + k;
+    }
+  }
+  if (depth) *depth = best_d;
+  return akz_batch_set_fed_depth(b, best_d);
 }
 
 /* Learned FED surrogate for the levels of octave >= first_octave

@@ -37,8 +37,10 @@ sys.path.insert(0, ROOT)
 METRIC = "1080p images/s detect+MLDB, surrogate vs plain FED at fixed repeatability"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the 27 k_fed
 # launches of one 1920x1080 image, from an ncu capture of an 8-image batch
-# (618.3 MB / 8); the level stage's traffic per step is this times the batch.
+# (618.3 MB / 8) at a blocking depth of 8 FED steps per launch; the level
+# stage's traffic per step is this times the batch.
 FED_TRAFFIC_PER_1080P_IMAGE = 77.29e6
+FED_TRAFFIC_DEPTH = 8
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
 
@@ -60,6 +62,8 @@ def parse():
                     help="surrogate4k: run the net's 32-channel layers on tcgen05 (1) or mma.sync (0)")
     ap.add_argument("--check-tol", type=float, default=2e-3,
                     help="surrogate4k: per-level tolerance of the surrogate against plain FED before it falls back")
+    ap.add_argument("--fed-depth", default="auto", choices=["auto", "4", "5", "6", "7", "8"],
+                    help="FED steps per level-kernel launch; auto times each depth on the batch first")
     ap.add_argument("--workload", default="batch1080p",
                     choices=["batch1080p", "single640", "uneven64", "matcher", "surrogate4k"],
                     help="batch1080p: the headline line (default); single640: one 640x480 pair, GPU and CPU; "
@@ -301,6 +305,16 @@ def workload_single640(args):
     return 0
 
 
+def _pick_fed_depth(batch, args):
+    """FED blocking depth: the autotuner's pick (timed on the uploaded batch)
+    or the one asked for."""
+    if args.fed_depth == "auto":
+        d, ms = batch.autotune()
+        return d, {str(k): round(v, 4) for k, v in ms.items()}
+    batch.set_fed_depth(int(args.fed_depth))
+    return int(args.fed_depth), None
+
+
 def workload_uneven64(args):
     """64 images of uneven sizes in one graph-replayed batch (images/s), and
     each image alone (per-image latency, p50/p99)."""
@@ -313,6 +327,7 @@ def workload_uneven64(args):
     b = akz.Batch(opt, sizes)
     b.set_stream(stream.cuda_stream)
     b.upload(imgs)
+    fed_depth, depth_ms = _pick_fed_depth(b, args)
     for _ in range(max(args.warmup, 3)):
         b.run()
     step_ms = _event_ms(torch, stream, b.run, args.steps)
@@ -334,6 +349,7 @@ def workload_uneven64(args):
         "latency_ms_alone": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                              "min": float(lat.min()), "max": float(lat.max())},
         "latency_ms_in_batch": step_ms, "keypoints_total": int(sum(counts)),
+        "fed_depth": fed_depth, "level_stage_ms_by_depth": depth_ms,
     }))
     return 0
 
@@ -497,6 +513,7 @@ def main():
     stream = torch.cuda.Stream()
     batch.set_stream(stream.cuda_stream)
     batch.upload(imgs)
+    fed_depth, depth_ms = _pick_fed_depth(batch, args)
     torch.cuda.synchronize()
     if args.profile_case:
         ms = batch.profile()
@@ -570,11 +587,13 @@ def main():
                    "fed": "plain (the learned surrogate is built but 2.6x slower at 4K on this GPU: --workload surrogate4k)",
                    "images_per_step_per_gpu": B, "parallelism": f"replicas x{ws}",
                    "l2": "inputs and working set larger than L2 (~%.1f GB per step)" % (B * image_algorithmic_bytes(W, H, 0) / 1e9),
-                   "keypoints_per_image": nkp},
+                   "keypoints_per_image": nkp,
+                   "fed_depth": fed_depth, "level_stage_ms_by_depth": depth_ms},
         "roofline": {"bound": "hbm", "kernel": "k_fed (level stage: 15 levels, 166 FED steps)",
                      "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"],
-                     "traffic": FED_TRAFFIC_PER_1080P_IMAGE * B if (W, H) == (1920, 1080) else None,
+                     "traffic": (FED_TRAFFIC_PER_1080P_IMAGE * B
+                                 if (W, H) == (1920, 1080) and fed_depth == FED_TRAFFIC_DEPTH else None),
                      "traffic_note": "ncu DRAM bytes of the level stage, 8-image capture scaled to the batch",
                      "algorithmic_bytes_per_image": fed_algorithmic_bytes(W, H), "launch_ms": fed_ms,
                      "peak_kind": f"{pk_kind} hbm_gbs"},

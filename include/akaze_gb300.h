@@ -284,6 +284,16 @@ AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pi
                                      float dt_feature, float s_out, const void *weights_bf16, const float *biases,
                                      void *scratch, float *out, void *stream);
 
+/* Autotuner of the FED temporal-blocking depth (FED steps per level-kernel
+ * launch, 4..8; no counterpart in the reference): on the uploaded images,
+ * times the scale-space stage for each depth, keeps the fastest for later
+ * runs and returns it in *depth; ms_per_depth (cap entries, may be NULL)
+ * receives the times of depths 4, 5, ...  Synchronises the batch's stream. */
+AKZ_API akz_status akz_batch_autotune(akz_batch *b, float *ms_per_depth, int cap, int *depth);
+
+/* Sets the FED blocking depth (4..8; 8 at creation) without timing. */
+AKZ_API akz_status akz_batch_set_fed_depth(akz_batch *b, int depth);
+
 /* akz_batch_detect_describe with packed host output: kpts (capacity
  * records) and desc (capacity x 61 bytes) receive every image's keypoints
  * and descriptors back to back, image i starting at row sum_{j<i} counts[j];

@@ -124,3 +124,27 @@ def test_packed_output_equals_per_image_results(gpu_lib):
         off += len(k)
     with pytest.raises(gpu_lib.AkazeError):
         b.detect_describe_packed(imgs, kp[: total - 1], d[: total - 1])
+
+
+def test_fed_blocking_depths_give_identical_results(gpu_lib):
+    """Every FED blocking depth (steps per level-kernel launch) computes the
+    same arithmetic; the autotuner only picks the fastest."""
+    sizes = synth.uneven_sizes(11, 6)
+    imgs = [synth.synth_image(1100 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    b = gpu_lib.Batch(gpu_lib.AKAZEOptions(), sizes)
+    b.upload(imgs)
+    b.run()
+    want = [b.results(i) for i in range(len(sizes))]
+    for depth in (4, 5, 6, 7, 8):
+        b.set_fed_depth(depth)
+        b.run()
+        for i, (k, d) in enumerate(want):
+            kk, dd = b.results(i)
+            assert kk.tobytes() == k.tobytes() and np.array_equal(dd, d), (depth, i)
+    best, ms = b.autotune()
+    assert 4 <= best <= 8 and sorted(ms) == [4, 5, 6, 7, 8] and all(v > 0 for v in ms.values())
+    b.upload(imgs)
+    b.run()
+    assert all(b.results(i)[0].tobytes() == want[i][0].tobytes() for i in range(len(sizes)))
+    with pytest.raises(gpu_lib.AkazeError):
+        b.set_fed_depth(3)
