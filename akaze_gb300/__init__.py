@@ -303,12 +303,13 @@ class Batch:
                                                 int(first_octave), ctypes.c_float(check_tol)))
 
     def autotune(self):
-        """Pick the FED blocking depth (4..8) by timing the uploaded batch;
-        returns (depth, {depth: ms})."""
+        """Pick the FED blocking depth (4..8) of every level by timing the
+        uploaded batch; returns (depth per level from 1, {depth: stage ms
+        with every level at that depth})."""
         ms = np.zeros(5, np.float32)
-        d = ctypes.c_int()
-        check(self._lib.akz_batch_autotune(self._h, _ptr(ms), 5, ctypes.byref(d)))
-        return d.value, {4 + k: float(v) for k, v in enumerate(ms)}
+        dl = np.full(64, -1, np.int32)
+        check(self._lib.akz_batch_autotune(self._h, _ptr(ms), 5, _ptr(dl), 64))
+        return [int(x) for x in dl[1:] if x > 0], {4 + k: float(v) for k, v in enumerate(ms)}
 
     def set_fed_depth(self, depth):
         check(self._lib.akz_batch_set_fed_depth(self._h, int(depth)))

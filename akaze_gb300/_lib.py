@@ -122,7 +122,7 @@ def load():
         "akz_sg_set_tcgen05": ([I], I),
         "akz_sg_tcgen05_status": ([IP], I),
         "akz_selfcheck_pm_g2": ([P, P, I, I, P], I),
-        "akz_batch_autotune": ([P, P, I, IP], I),
+        "akz_batch_autotune": ([P, P, I, P, I], I),
         "akz_batch_set_fed_depth": ([P, I], I),
         "akz_sg_infer_level": ([P, P, ctypes.c_size_t, I, I, ctypes.c_float, ctypes.c_float, P, P, P, P, P], I),
     }

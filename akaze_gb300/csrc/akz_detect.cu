@@ -1,13 +1,15 @@
 /*
  * akz_detect.cu - Hessian detector, extrema, ordering and suppression.
  *
- *   k_detect   one fused tile kernel per launch over every (image, level):
- *              Lsmooth tile -> scaled Scharr derivatives Lx, Ly with step
- *              sigma_size and reflect-101 border (cuda_akaze.cu:651-671,
- *              written to HBM for orientation and M-LDB) -> Hessian
- *              determinant in shared memory (:673-701) -> strict 3x3 maxima
- *              above the threshold inside the border (:727-743), recorded as
- *              one bit per pixel plus a per-row count.
+ *   k_detect_strip  one launch over every (image, level) with derivative
+ *              step 2..4 (all levels of the default options): each CTA
+ *              streams down a column strip, Lsmooth rows -> scaled Scharr
+ *              derivatives Lx, Ly with step sigma_size and reflect-101
+ *              border (cuda_akaze.cu:651-671, written to HBM for orientation
+ *              and M-LDB) -> Hessian determinant (:673-701) -> strict 3x3
+ *              maxima above the threshold inside the border (:727-743),
+ *              recorded as one bit per pixel plus a per-row count.
+ *   k_detect   the same per 64 x 32 tile for any other step.
  *   k_rowscan  exclusive scan of the row counts of each image: the raw
  *              extrema come out in (level, y, x) order, which is the order
  *              the reference's per-level bitonic sort gives (:884-939),
@@ -48,167 +50,238 @@ __device__ __forceinline__ int akz_border_hi(float border, int n)
   return v;
 }
 
-/* k_detect for every tile of a level with derivative step ST (2..4, the steps
- * of the default options): compile-time region sizes, straight-line loops,
- * column pairs with packed FP32x2 additions (products scalar), in the
- * reference's operation order.
+/* ------------------------------------------------------------------------ */
+/* Streaming detector for derivative steps 2..4 (every level of the default
+ * options).
  *
- * Borders: the Lsmooth region is staged with reflect-101 coordinates, which
- * makes Lx and Ly exact at every pixel inside the image (their taps at +-ST
- * are the reference's reflect-101 indices, cuda_akaze.cu:657-660).  The
- * determinant reads Lx and Ly at reflect-101 indices too, i.e. the mirrored
- * in-image value, not a derivative of the mirrored image, so after the
- * derivative pass the entries just outside the image (within ST) are
- * replaced by their in-image mirrors.
- *
- * Layout: tile (62 - 2 ST) x 32, so the Lx, Ly region is exactly 64 columns
- * (32 pairs): one warp per row in both passes, no row wraps inside a warp,
- * hence no shared-memory bank conflicts for the 64-bit pair accesses. */
-template <int ST, bool BORDER>
-__device__ __forceinline__ void akz_detect_tile(const akz_detect_params &p, const akz_level_desc &L, float *sm, int tx0,
-                                                int ty0)
+ * A CTA owns a strip of TW output columns and AKZ_STRIP_CH rows and walks
+ * down it 8 rows per iteration, one row per warp in each phase:
+ *   Lsmooth rows  -> ring of 32 rows (cp.async, issued one iteration ahead)
+ *   Lx, Ly rows   -> ring of 16 rows, and to HBM for the strip's own pixels
+ *   determinant   -> ring of 16 rows
+ *   3x3 maxima above the threshold inside the border range.
+ * Column grids (image x of column 0):
+ *   D (Lx, Ly)     tx0 - A,        128 columns = 64 aligned pairs, A = ST+1 rounded up to even
+ *   S (Lsmooth)    tx0 - A - ST,   128 + 2 ST columns; D column d has its taps at S d, d+ST, d+2ST
+ *   E (det)        tx0 + EO,       2 NEP columns, EO = -1 for odd ST, -2 otherwise; E column e
+ *                                  has its centre at D column e + EO + A, an offset of ST's parity,
+ *                                  so its outer taps (+-ST) are aligned pairs
+ * The strip's vertical halo is paid once per AKZ_STRIP_CH rows instead of
+ * once per tile.  Lsmooth rows and columns outside the image are read at
+ * their reflect-101 index (clamped into the image where the reflection
+ * itself would leave it), so Lx and Ly are exact at every pixel inside the
+ * image (cuda_akaze.cu:651-671).  The determinant is exact wherever the
+ * maxima test reads it: the border range of a level with step ST starts at
+ * x >= 10 sqrt(2) ST (cuda_akaze.cu:734-740), and the determinant at
+ * distance <= 1 from it reads Lx, Ly inside the image only, so no mirrored
+ * Lx, Ly value is ever needed.  Same expressions, same order as the
+ * reference's kernels (cuda_akaze.cu:651-701, :727-743). */
+template <int ST>
+struct akz_strip_geo {
+  static constexpr int A = (ST + 2) & ~1;
+  static constexpr int TW = (127 - A - ST) & ~1;
+  static constexpr int SW = 128 + 2 * ST;
+  static constexpr int EO = (ST & 1) ? -1 : -2;
+  static constexpr int NEP = (128 - ST - EO - A) / 2; /* E pairs: right tap pair of the last one ends at D 127 */
+  static_assert(TW - EO + 1 <= 2 * NEP, "E covers tx0 - 1 .. tx0 + TW");
+  static_assert(EO + A - ST >= 0 && 2 * (NEP - 1) + EO + A + ST + 1 <= 127, "E taps inside the D ring row");
+  static_assert(A >= ST + 1 && TW + A + ST <= 127 && A % 2 == 0 && TW % 2 == 0, "D covers tx0 - ST - 1 .. tx0 + TW + ST");
+  static_assert(2 * ST < 9, "ring depths (S 32, D 16, E 16 rows) hold every live row");
+};
+
+static inline __host__ __device__ int akz_strip_tile_width_rt(int st)
 {
-  constexpr int TW = 62 - 2 * ST, TH = AKZ_DETECT_TH;
-  constexpr int DW = TW + 2 * ST + 2, DH = TH + 2 * ST + 2; /* Lx, Ly:  tile +- (ST+1)  */
-  constexpr int SW = TW + 4 * ST + 2, SH = TH + 4 * ST + 2; /* Lsmooth: tile +- (2ST+1) */
-  constexpr int SWS = SW;                                   /* Lsmooth row stride */
-  constexpr int EW = TW + 2, EH = TH + 2;                   /* Ldet:    tile +- 1       */
-  constexpr int DP = DW / 2, EP = EW / 2;                   /* column pairs */
-  static_assert(DW == 64 && EP <= 32 && EW % 2 == 0 && SW % 2 == 0, "pair layout");
-  static_assert(EW * EH <= SWS * SH, "determinant plane fits the Lsmooth region");
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  return st == 2 ? akz_strip_geo<2>::TW : st == 3 ? akz_strip_geo<3>::TW : st == 4 ? akz_strip_geo<4>::TW : 0;
+}
+int akz_strip_tile_width(int st) { return akz_strip_tile_width_rt(st); }
+
+#define AKZ_STRIP_NS 32 /* Lsmooth ring rows */
+#define AKZ_STRIP_ND 16 /* Lx, Ly ring rows */
+#define AKZ_STRIP_NE 16 /* determinant ring rows */
+#define AKZ_STRIP_EW 128
+
+__device__ __forceinline__ void akz_cp_async4(float *dst, const float *src)
+{
+  const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void akz_cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void akz_cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+/* reflect-101 into [0, n), clamped where the reflection would leave it */
+__device__ __forceinline__ int akz_refl_clamp(int i, int n)
+{
+  if (i < 0) i = -i;
+  if (i >= n) i = 2 * n - 2 - i;
+  return akz_clampi(i, 0, n - 1);
+}
+
+template <int ST>
+__device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, const akz_level_desc &L, float *sm, int tx0,
+                                                 int ty0)
+{
+  using G = akz_strip_geo<ST>;
+  constexpr int A = G::A, TW = G::TW, SW = G::SW, EO = G::EO, NEP = G::NEP;
+  constexpr int NS = AKZ_STRIP_NS, ND = AKZ_STRIP_ND, NE = AKZ_STRIP_NE, EW = AKZ_STRIP_EW;
+  constexpr int SJ = (SW + 31) / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int W = L.width, H = L.height;
-  /* the determinant plane reuses the Lsmooth region, dead after the derivative pass */
-  float *sS = sm, *sX = sm + SWS * SH, *sY = sX + DW * DH, *sD = sm;
+  const int ch = min(AKZ_STRIP_CH, H - ty0); /* rows of this CTA */
+  const int iters = (ch + 7) >> 3;
+  float *sS = sm, *sX = sS + NS * SW, *sY = sX + ND * 128, *sE = sY + ND * 128;
   const float fac1 = p.fac1, fac2 = p.fac2;
   const float *ls = p.t.planes + L.ls;
-  if (BORDER) {
-#pragma unroll
-    for (int n = warp; n < SH; n += 8) {
-      const int y = akz_refl101(min(ty0 - 2 * ST - 1 + n, H + 2 * ST), H);
-      const float *q = ls + (long long)y * L.pitch;
-#pragma unroll
-      for (int j = 0; j < (SW + 31) / 32; j++) {
-        const int m = lane + 32 * j;
-        if (m < SW) sS[n * SWS + m] = __ldg(q + akz_refl101(min(tx0 - 2 * ST - 1 + m, W + 2 * ST), W));
-      }
-    }
-  } else {
-    const float *q0 = ls + (long long)(ty0 - 2 * ST - 1) * L.pitch + (tx0 - 2 * ST - 1);
-#pragma unroll
-    for (int n = warp; n < SH; n += 8) {
-      const float *q = q0 + (long long)n * L.pitch;
-#pragma unroll
-      for (int j = 0; j < (SW + 31) / 32; j++) {
-        const int m = lane + 32 * j;
-        if (m < SW) sS[n * SWS + m] = __ldg(q + m);
-      }
-    }
-  }
-  __syncthreads();
-  /* Lx, Ly on the tile +- (ST+1), two columns per item: D column d is
-   * Lsmooth column d + ST; its taps sit at d, d + ST and d + 2ST, so the
-   * outer taps are aligned pairs for every ST (cuda_akaze.cu:651-671) */
-  const int dx0 = tx0 - ST - 1, dy0 = ty0 - ST - 1; /* image coordinates of D (0, 0) */
   float *lxp = p.t.planes + L.lx, *lyp = p.t.planes + L.ly;
-  for (int n = warp; n < DH; n += 8) {
-    const int d = 2 * lane;
-    const float *su = sS + n * SWS + d, *sc = su + ST * SWS, *sd = su + 2 * ST * SWS;
-    const float2 ul = ld2(su), ur = ld2(su + 2 * ST), ll = ld2(sd), lr = ld2(sd + 2 * ST);
-    const float2 cl = ld2(sc), cr = ld2(sc + 2 * ST);
-    const float2 uc = (ST & 1) ? make_float2(su[ST], su[ST + 1]) : ld2(su + ST);
-    const float2 lc = (ST & 1) ? make_float2(sd[ST], sd[ST + 1]) : ld2(sd + ST);
-    const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
-    const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(lc, uc);
-    const float2 a = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
-    const float2 b = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
-    st2(sX + n * DW + d, a);
-    st2(sY + n * DW + d, b);
-    const int y = dy0 + n, x = dx0 + d;
-    if (n >= ST + 1 && n < ST + 1 + TH && (!BORDER || y < H)) {
-      float *ox = lxp + (long long)y * L.pitch + x, *oy = lyp + (long long)y * L.pitch + x;
-      if (d >= ST + 1 && d < ST + 1 + TW && (!BORDER || x < W)) {
-        ox[0] = a.x;
-        oy[0] = b.x;
-      }
-      if (d + 1 >= ST + 1 && d + 1 < ST + 1 + TW && (!BORDER || x + 1 < W)) {
-        ox[1] = a.y;
-        oy[1] = b.y;
-      }
-    }
-  }
-  __syncthreads();
-  /* reflect-101 mirrors of Lx, Ly within ST outside the image: columns
-   * first, then whole rows (which covers the corners); the sources are
-   * in-image entries, which these passes do not write */
-  if (BORDER && (dx0 < 0 || dx0 + DW > W)) {
-    for (int i = tid; i < DH * DW; i += 256) {
-      const int n = i / DW, c = i - n * DW, x = dx0 + c;
-      const int xm = x < 0 ? -x : (x >= W && x <= W - 1 + ST ? 2 * W - 2 - x : -1);
-      if (xm >= 0) {
-        sX[n * DW + c] = sX[n * DW + xm - dx0];
-        sY[n * DW + c] = sY[n * DW + xm - dx0];
-      }
-    }
-    __syncthreads();
-  }
-  if (BORDER && (dy0 < 0 || dy0 + DH > H)) {
-    for (int i = tid; i < DH * DW; i += 256) {
-      const int n = i / DW, c = i - n * DW, y = dy0 + n;
-      const int ym = y < 0 ? -y : (y >= H && y <= H - 1 + ST ? 2 * H - 2 - y : -1);
-      if (ym >= 0) {
-        sX[n * DW + c] = sX[(ym - dy0) * DW + c];
-        sY[n * DW + c] = sY[(ym - dy0) * DW + c];
-      }
-    }
-    __syncthreads();
-  }
-  /* Hessian determinant on the tile +- 1 (cuda_akaze.cu:673-701): E column e
-   * is D column e + ST */
-  for (int n = warp; n < EH; n += 8) {
-    const int e = 2 * lane;
-    if (lane >= EP) continue;
-    const float *xu = sX + n * DW + e, *xc = xu + ST * DW, *xd = xu + 2 * ST * DW;
-    const float *yu = sY + n * DW + e, *yd = yu + 2 * ST * DW;
-    const float2 ul = ld2(xu), ur = ld2(xu + 2 * ST), ll = ld2(xd), lr = ld2(xd + 2 * ST);
-    const float2 cl = ld2(xc), cr = ld2(xc + 2 * ST);
-    const float2 xuc = (ST & 1) ? make_float2(xu[ST], xu[ST + 1]) : ld2(xu + ST);
-    const float2 xdc = (ST & 1) ? make_float2(xd[ST], xd[ST + 1]) : ld2(xd + ST);
-    const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
-    const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(xdc, xuc);
-    const float2 lxx = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
-    const float2 lyx = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
-    const float2 vul = ld2(yu), vur = ld2(yu + 2 * ST), vll = ld2(yd), vlr = ld2(yd + 2 * ST);
-    const float2 yuc = (ST & 1) ? make_float2(yu[ST], yu[ST + 1]) : ld2(yu + ST);
-    const float2 ydc = (ST & 1) ? make_float2(yd[ST], yd[ST + 1]) : ld2(yd + ST);
-    const float2 cy = f2sub(f2sub(f2add(vlr, vll), vur), vul), dy = f2sub(ydc, yuc);
-    const float2 lyy = f2add(make_float2(fac1 * cy.x, fac1 * cy.y), make_float2(fac2 * dy.x, fac2 * dy.y));
-    st2(sD + n * EW + e, f2sub(make_float2(lxx.x * lyy.x, lxx.y * lyy.y), make_float2(lyx.x * lyx.x, lyx.y * lyx.y)));
-  }
-  __syncthreads();
-  /* strict 3x3 maxima above the threshold inside the border (cuda_akaze.cu:727-743);
-   * the border range also rejects tile pixels outside the image */
-  const int xlo = akz_border_lo(L.border), xhi = akz_border_hi(L.border, W);
-  const int ylo = akz_border_lo(L.border), yhi = akz_border_hi(L.border, H);
-  for (int j = warp; j < TH; j += 8) {
-    const int y = ty0 + j;
-    if (y < ylo || y > yhi) continue;
+  const long long pitch = L.pitch;
+
+  int xs[SJ]; /* source column of this lane's S columns lane + 32 j */
 #pragma unroll
-    for (int k = 0; k < (TW + 31) / 32; k++) {
-      const int i = lane + 32 * k;
-      const int x = tx0 + i;
-      if (i >= TW || x < xlo || x > xhi) continue;
-      const float *c = sD + (j + 1) * EW + (i + 1);
-      const float v = c[0];
+  for (int j = 0; j < SJ; j++) xs[j] = akz_refl_clamp(tx0 - A - ST + lane + 32 * j, W);
+
+  auto load_s = [&](int r) { /* S row r into its ring slot */
+    const float *src = ls + (long long)akz_refl_clamp(r, H) * pitch;
+    float *dst = sS + (r & (NS - 1)) * SW;
+#pragma unroll
+    for (int j = 0; j < SJ; j++) {
+      const int c = lane + 32 * j;
+      if (c < SW) akz_cp_async4(dst + c, src + xs[j]);
+    }
+  };
+  auto comp_d = [&](int r) { /* Lx, Ly row r; HBM for the strip's own pixels */
+    const float *su = sS + ((r - ST) & (NS - 1)) * SW, *sc = sS + (r & (NS - 1)) * SW,
+                *sd = sS + ((r + ST) & (NS - 1)) * SW;
+    float *ox = sX + (r & (ND - 1)) * 128, *oy = sY + (r & (ND - 1)) * 128;
+    const bool wrow = r >= ty0 && r < ty0 + ch;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const int d = 2 * (lane + 32 * k);
+      const float2 ul = ld2(su + d), ur = ld2(su + d + 2 * ST), ll = ld2(sd + d), lr = ld2(sd + d + 2 * ST);
+      const float2 cl = ld2(sc + d), cr = ld2(sc + d + 2 * ST);
+      const float2 uc = (ST & 1) ? make_float2(su[d + ST], su[d + ST + 1]) : ld2(su + d + ST);
+      const float2 lc = (ST & 1) ? make_float2(sd[d + ST], sd[d + ST + 1]) : ld2(sd + d + ST);
+      const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
+      const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(lc, uc);
+      const float2 a = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
+      const float2 b = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+      st2(ox + d, a);
+      st2(oy + d, b);
+      const int x = tx0 - A + d; /* even */
+      if (wrow && d >= A && d < A + TW && x < W) {
+        float *gx = lxp + (long long)r * pitch + x, *gy = lyp + (long long)r * pitch + x;
+        if (x + 1 < W) {
+          st2(gx, a);
+          st2(gy, b);
+        } else {
+          gx[0] = a.x;
+          gy[0] = b.x;
+        }
+      }
+    }
+  };
+  auto comp_e = [&](int r) { /* determinant row r */
+    const float *xu = sX + ((r - ST) & (ND - 1)) * 128, *xc = sX + (r & (ND - 1)) * 128,
+                *xd = sX + ((r + ST) & (ND - 1)) * 128;
+    const float *yu = sY + ((r - ST) & (ND - 1)) * 128, *yd = sY + ((r + ST) & (ND - 1)) * 128;
+    float *o = sE + (r & (NE - 1)) * EW;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const int q = lane + 32 * k;
+      if (q >= NEP) continue;
+      const int e = 2 * q, d = e + EO + A; /* centre D column */
+      const float2 ul = ld2(xu + d - ST), ur = ld2(xu + d + ST), ll = ld2(xd + d - ST), lr = ld2(xd + d + ST);
+      const float2 cl = ld2(xc + d - ST), cr = ld2(xc + d + ST);
+      const float2 xuc = (ST & 1) ? make_float2(xu[d], xu[d + 1]) : ld2(xu + d);
+      const float2 xdc = (ST & 1) ? make_float2(xd[d], xd[d + 1]) : ld2(xd + d);
+      const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
+      const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(xdc, xuc);
+      const float2 lxx = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
+      const float2 lyx = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+      const float2 vul = ld2(yu + d - ST), vur = ld2(yu + d + ST), vll = ld2(yd + d - ST), vlr = ld2(yd + d + ST);
+      const float2 yuc = (ST & 1) ? make_float2(yu[d], yu[d + 1]) : ld2(yu + d);
+      const float2 ydc = (ST & 1) ? make_float2(yd[d], yd[d + 1]) : ld2(yd + d);
+      const float2 cy = f2sub(f2sub(f2add(vlr, vll), vur), vul), dy = f2sub(ydc, yuc);
+      const float2 lyy = f2add(make_float2(fac1 * cy.x, fac1 * cy.y), make_float2(fac2 * dy.x, fac2 * dy.y));
+      st2(o + e, f2sub(make_float2(lxx.x * lyy.x, lxx.y * lyy.y), make_float2(lyx.x * lyx.x, lyx.y * lyx.y)));
+    }
+  };
+  const int xlo = max(akz_border_lo(L.border), tx0), xhi = min(akz_border_hi(L.border, W), tx0 + TW - 1);
+  const int ylo = max(akz_border_lo(L.border), ty0), yhi = min(akz_border_hi(L.border, H), ty0 + ch - 1);
+  auto maxima = [&](int y) {
+    if (y < ylo || y > yhi) return;
+    const float *eu = sE + ((y - 1) & (NE - 1)) * EW, *ec = sE + (y & (NE - 1)) * EW, *ed = sE + ((y + 1) & (NE - 1)) * EW;
+#pragma unroll
+    for (int j = 0; j < (TW + 31) / 32; j++) {
+      const int x = tx0 + lane + 32 * j;
+      if (x < xlo || x > xhi) continue;
+      const int e = x - tx0 - EO;
+      const float v = ec[e];
       if (v > p.thr) {
-        if (v > c[-EW - 1] && v > c[EW + 1] && v > c[EW - 1] && v > c[-EW + 1] && v > c[-1] && v > c[1] &&
-            v > c[EW] && v > c[-EW]) {
+        if (v > eu[e - 1] && v > ed[e + 1] && v > ed[e - 1] && v > eu[e + 1] && v > ec[e - 1] && v > ec[e + 1] &&
+            v > ed[e] && v > eu[e]) {
           atomicOr(&p.bitmap[L.bitmap + (long long)y * L.bitmap_pitch + (x >> 5)], 1u << (x & 31));
           atomicAdd(&p.rowcnt[L.rows + y], 1);
         }
       }
     }
+  };
+
+  /* pre-roll: S rows ty0-1-2ST .. ty0+2ST, D rows ty0-1-ST .. ty0+ST,
+   * E rows ty0-1, ty0; then iteration 0's S rows in flight */
+  for (int r = ty0 - 1 - 2 * ST + warp; r <= ty0 + 2 * ST; r += 8) load_s(r);
+  akz_cp_async_commit();
+  akz_cp_async_wait_all();
+  __syncthreads();
+  for (int r = ty0 + 2 * ST + 1 + warp; r <= ty0 + 2 * ST + 8; r += 8) load_s(r);
+  akz_cp_async_commit();
+  for (int r = ty0 - 1 - ST + warp; r <= ty0 + ST; r += 8) comp_d(r);
+  __syncthreads();
+  if (warp < 2) comp_e(ty0 - 1 + warp);
+  for (int k = 0; k < iters; k++) {
+    const int r = ty0 + 8 * k;
+    akz_cp_async_wait_all();
+    __syncthreads(); /* S rows up to r+8+2ST landed; E rows up to r visible */
+    if (k + 1 < iters) load_s(r + 2 * ST + 9 + warp);
+    akz_cp_async_commit();
+    comp_d(r + ST + 1 + warp);
+    __syncthreads();
+    comp_e(r + 1 + warp);
+    __syncthreads();
+    maxima(r + warp);
   }
+  akz_cp_async_wait_all();
+}
+
+__global__ void __launch_bounds__(256) k_detect_strip(akz_detect_params p)
+{
+  extern __shared__ float sm[];
+  const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
+  const akz_tile_seg sg = p.segs[si];
+  const akz_level_desc L = p.t.lv[sg.level_desc];
+  const int st = L.deriv_step;
+  const int lt = blockIdx.x - sg.tile_begin;
+  const int tx0 = (lt % sg.tiles_x) * akz_strip_tile_width_rt(st), ty0 = (lt / sg.tiles_x) * AKZ_STRIP_CH;
+  if (st == 2)
+    akz_detect_strip<2>(p, L, sm, tx0, ty0);
+  else if (st == 3)
+    akz_detect_strip<3>(p, L, sm, tx0, ty0);
+  else if (st == 4)
+    akz_detect_strip<4>(p, L, sm, tx0, ty0);
+}
+
+size_t akz_detect_strip_smem()
+{
+  return (size_t)(AKZ_STRIP_NS * akz_strip_geo<4>::SW + 2 * AKZ_STRIP_ND * 128 + AKZ_STRIP_NE * AKZ_STRIP_EW) *
+         sizeof(float);
+}
+
+cudaError_t akz_launch_detect_strip(const akz_detect_params &p, int ntiles, cudaStream_t s)
+{
+  if (ntiles <= 0) return cudaSuccess;
+  const size_t smem = akz_detect_strip_smem();
+  cudaError_t e = cudaFuncSetAttribute(k_detect_strip, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_detect_strip<<<ntiles, 256, smem, s>>>(p);
+  return cudaGetLastError();
 }
 
 __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_step)
@@ -221,8 +294,7 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const int W = L.width, H = L.height, st = L.deriv_step;
   const int lt = blockIdx.x - sg.tile_begin;
-  const int tw = akz_detect_tile_width(st);
-  const int tx0 = (lt % sg.tiles_x) * tw, ty0 = (lt / sg.tiles_x) * TH;
+  const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
   const int tx1 = min(tx0 + TW, W), ty1 = min(ty0 + TH, H);
   const int sx0 = max(tx0 - 2 * st - 1, 0), sx1 = min(tx1 + 2 * st + 1, W);
   const int sy0 = max(ty0 - 2 * st - 1, 0), sy1 = min(ty1 + 2 * st + 1, H);
@@ -230,26 +302,6 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   const int dy0 = max(ty0 - st - 1, 0), dy1 = min(ty1 + st + 1, H);
   const int ex0 = max(tx0 - 1, 0), ex1 = min(tx1 + 1, W), ey0 = max(ty0 - 1, 0), ey1 = min(ty1 + 1, H);
   const int sw = sx1 - sx0, dw = dx1 - dx0, ew = ex1 - ex0;
-  if (st >= 2 && st <= 4 && st <= max_step) {
-    const bool border = tx0 - 2 * st - 1 < 0 || ty0 - 2 * st - 1 < 0 || tx0 + tw + 2 * st + 1 > W ||
-                        ty0 + TH + 2 * st + 1 > H;
-    if (border) {
-      if (st == 2)
-        akz_detect_tile<2, true>(p, L, sm, tx0, ty0);
-      else if (st == 3)
-        akz_detect_tile<3, true>(p, L, sm, tx0, ty0);
-      else
-        akz_detect_tile<4, true>(p, L, sm, tx0, ty0);
-    } else {
-      if (st == 2)
-        akz_detect_tile<2, false>(p, L, sm, tx0, ty0);
-      else if (st == 3)
-        akz_detect_tile<3, false>(p, L, sm, tx0, ty0);
-      else
-        akz_detect_tile<4, false>(p, L, sm, tx0, ty0);
-    }
-    return;
-  }
   const int SM = (TW + 4 * max_step + 2) * (TH + 4 * max_step + 2);
   const int DM = (TW + 2 * max_step + 2) * (TH + 2 * max_step + 2);
   float *sS = sm, *sX = sm + SM, *sY = sX + DM, *sD = sm; /* determinant plane over the dead Lsmooth region */
@@ -686,14 +738,9 @@ cudaError_t akz_launch_detect(const akz_detect_params &p, int ntiles, int max_st
 {
   if (ntiles <= 0) return cudaSuccess;
   /* Lsmooth region + Lx, Ly regions; the determinant plane reuses the
-   * Lsmooth region.  General path at AKZ_DETECT_TW, akz_detect_tile at its
-   * narrower per-step width. */
-  size_t words = 0;
-  for (int st = 1; st <= max_step; st++) {
-    const size_t tw = (size_t)akz_detect_tile_width(st);
-    words = std::max(words, (tw + 4 * st + 2) * (AKZ_DETECT_TH + 4 * st + 2) + 2 * (tw + 2 * st + 2) * (AKZ_DETECT_TH + 2 * st + 2));
-  }
-  const size_t smem = words * sizeof(float);
+   * Lsmooth region */
+  const size_t tw = AKZ_DETECT_TW, th = AKZ_DETECT_TH, ms = (size_t)max_step;
+  const size_t smem = ((tw + 4 * ms + 2) * (th + 4 * ms + 2) + 2 * (tw + 2 * ms + 2) * (th + 2 * ms + 2)) * sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(k_detect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k_detect<<<ntiles, 256, smem, s>>>(p, max_step);

@@ -257,13 +257,14 @@ struct akz_batch {
   int gauss_off = 0, gauss_n = 0, gauss_tiles = 0;
   int l0_off = 0, l0_n = 0, l0_tiles = 0; /* k_level0 tiles */
   int detect_off = 0, detect_n = 0, detect_tiles = 0;
+  int strip_off = 0, strip_n = 0, strip_tiles = 0;
   int extract_off = 0, extract_n = 0, extract_rows = 0;
   std::vector<std::vector<akz_fed_launch>> fed;  /* per level index: the launches in use */
   /* the level stage's launches for every FED blocking depth (most steps per
    * launch) AKZ_DEPTH_MIN .. AKZ_MAX_STEPS_PER_LAUNCH; akz_batch_autotune
    * picks one, the default is the largest */
   std::vector<std::vector<std::vector<akz_fed_launch>>> fed_alt;
-  int fed_depth = 8;
+  std::vector<int> fed_depth; /* per level */
   /* learned surrogate (akz_batch_set_surrogate): per level, the zero-step
    * launch that forms Lsmooth, the conductance and the start image, and the
    * plain chunks of image 0 into the check plane */
@@ -589,12 +590,21 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
     b->sg_prep[l] = pl;
     b->fed_alt[AKZ_MAX_STEPS_PER_LAUNCH - AKZ_DEPTH_MIN][l] = b->fed[l];
   }
-  b->fed_depth = AKZ_MAX_STEPS_PER_LAUNCH;
+  b->fed_depth.assign(b->maxlev, AKZ_MAX_STEPS_PER_LAUNCH);
+  /* detector: the streaming strip kernel for steps 2..4, tiles otherwise */
+  b->strip_off = (int)b->segs.size();
+  for (int i = 0; i < n; i++)
+    for (int l = 0; l < b->im[i].nlev; l++) {
+      const int tw = akz_strip_tile_width(b->geo[i][l].deriv_step);
+      if (tw > 0) add_tiles(b->im[i].first_level + l, b->geo[i][l].w, b->geo[i][l].h, tw, AKZ_STRIP_CH, 0, b->strip_tiles);
+    }
+  b->strip_n = (int)b->segs.size() - b->strip_off;
   b->detect_off = (int)b->segs.size();
   for (int i = 0; i < n; i++)
     for (int l = 0; l < b->im[i].nlev; l++)
-      add_tiles(b->im[i].first_level + l, b->geo[i][l].w, b->geo[i][l].h, akz_detect_tile_width(b->geo[i][l].deriv_step),
-                AKZ_DETECT_TH, 0, b->detect_tiles);
+      if (akz_strip_tile_width(b->geo[i][l].deriv_step) == 0)
+        add_tiles(b->im[i].first_level + l, b->geo[i][l].w, b->geo[i][l].h, AKZ_DETECT_TW, AKZ_DETECT_TH, 0,
+                  b->detect_tiles);
   b->detect_n = (int)b->segs.size() - b->detect_off;
   b->extract_off = (int)b->segs.size();
   for (int i = 0; i < n; i++)
@@ -688,7 +698,9 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
 
 /* stage groups ------------------------------------------------------------ */
 
-static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe = nullptr)
+/* pe: events of the level-0 split (profile); lev: one event per level,
+ * recorded when that level is done (level 0 included) */
+static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe = nullptr, cudaEvent_t *lev = nullptr)
 {
   const akz_tables t = akz_make_tables(b);
   if (b->sg_on) CK(cudaMemsetAsync(b->d_sg_err, 0, (size_t)b->maxlev * sizeof(float), s));
@@ -735,6 +747,7 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe 
     CK(akz_launch_gauss0(gp, b->gauss_tiles, s));
     if (pe) CK(cudaEventRecord(pe[2], s));
   }
+  if (lev) CK(cudaEventRecord(lev[0], s));
   for (int l = 1; l < b->maxlev; l++) {
     if (b->area[l].nsegs > 0) {
       akz_area_params ap;
@@ -760,6 +773,7 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe 
     };
     if (!b->sg_on || l / b->opt.nsublevels < b->sg_first_octave) {
       for (auto &fl : b->fed[l]) CK(run_fed(fl, nullptr));
+      if (lev) CK(cudaEventRecord(lev[l], s));
       continue;
     }
     /* learned surrogate: start image, Lsmooth and conductance, then the net
@@ -781,6 +795,7 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe 
       CK(akz_sg_maxdiff(b->d_sg_chk, b->planes + L0.lt, L0.pitch, L0.width, L0.height, b->d_sg_err + l, s));
       for (auto &fl : b->fed[l]) CK(run_fed(fl, b->d_sg_err + l));
     }
+    if (lev) CK(cudaEventRecord(lev[l], s));
   }
   return AKZ_OK;
 }
@@ -803,6 +818,9 @@ static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s, cudaEvent_t *pe
   dp.fac1 = fac1;
   dp.fac2 = fac2;
   CK(akz_launch_detect(dp, b->detect_tiles, b->max_step, s));
+  dp.segs = b->d_segs + b->strip_off;
+  dp.nsegs = b->strip_n;
+  CK(akz_launch_detect_strip(dp, b->strip_tiles, s));
   if (pe) CK(cudaEventRecord(pe[4], s));
   CK(akz_launch_rowscan(t, b->d_rowcnt, b->d_rowscan, s));
   akz_extract_params ep;
@@ -1321,9 +1339,9 @@ AKZ_API akz_status akz_batch_level_plane(akz_batch *b, int i, int level, int pla
 static int akz_batch_nkernels(const akz_batch *b)
 {
   /* level 0 + contrast: k_level0, k_contrast_hist, k_contrast_final (radius <= 4),
-   * else k_contrast x2, k_contrast_final, k_gauss0; then detect, scan,
-   * extract, nms, describe */
-  int n = (b->R0 <= 4 ? 3 : 4) + 5;
+   * else k_contrast x2, k_contrast_final, k_gauss0; then the detector
+   * (strip and/or tile kernel), scan, extract, nms, describe */
+  int n = (b->R0 <= 4 ? 3 : 4) + 4 + (b->strip_tiles > 0) + (b->detect_tiles > 0);
   for (int l = 1; l < b->maxlev; l++) {
     n += b->area[l].nsegs > 0 ? 1 : 0;
     if (b->sg_on && l / b->opt.nsublevels >= b->sg_first_octave) {
@@ -1467,50 +1485,69 @@ AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *q64
   return akz_match_device(m, q64, nq, t64, nt, out);
 }
 
+static void akz_use_fed_depths(akz_batch *b)
+{
+  for (int l = 1; l < b->maxlev; l++) b->fed[l] = b->fed_alt[b->fed_depth[l] - AKZ_DEPTH_MIN][l];
+  if (b->graph) { /* the captured graph holds the old launches */
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+}
+
 AKZ_API akz_status akz_batch_set_fed_depth(akz_batch *b, int depth)
 {
   AKZ_GUARD(b);
   if (depth < AKZ_DEPTH_MIN || depth > AKZ_MAX_STEPS_PER_LAUNCH)
     return akz_report(AKZ_ERR_INVALID_ARG, "akz_batch_set_fed_depth: depth must be 4..8");
-  b->fed = b->fed_alt[depth - AKZ_DEPTH_MIN];
-  b->fed_depth = depth;
-  if (b->graph) { /* the captured graph holds the old launches */
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  for (int l = 1; l < b->maxlev; l++) b->fed_depth[l] = depth;
+  akz_use_fed_depths(b);
   return AKZ_OK;
 }
 
-/* FED blocking depth autotuner: times the level stage of the uploaded
- * batch for each depth and keeps the fastest. */
-AKZ_API akz_status akz_batch_autotune(akz_batch *b, float *ms_per_depth, int cap, int *depth)
+/* FED blocking depth autotuner: times every level of the uploaded batch at
+ * each depth (the levels' launches do not depend on one another's chunking)
+ * and keeps the fastest depth per level. */
+AKZ_API akz_status akz_batch_autotune(akz_batch *b, float *ms_per_depth, int cap, int *depths, int ndepths)
 {
   AKZ_GUARD(b);
-  const int nd = AKZ_MAX_STEPS_PER_LAUNCH - AKZ_DEPTH_MIN + 1;
-  cudaEvent_t e0 = b->ev[6], e1 = b->ev[7];
-  float best = 1e30f;
-  int best_d = b->fed_depth;
-  for (int k = 0; k < nd; k++) {
+  const int nd = AKZ_MAX_STEPS_PER_LAUNCH - AKZ_DEPTH_MIN + 1, nl = b->maxlev;
+  std::vector<cudaEvent_t> ev(nl + 1, nullptr);
+  cudaError_t ce = cudaSuccess;
+  for (auto &e : ev)
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e);
+  std::vector<std::vector<float>> tl(nd, std::vector<float>(nl, 1e30f));
+  std::vector<float> tot(nd, 1e30f);
+  akz_status st = AKZ_OK;
+  for (int k = 0; k < nd && ce == cudaSuccess && st == AKZ_OK; k++) {
     b->fed = b->fed_alt[k];
-    float tmin = 1e30f;
-    for (int rep = 0; rep < 4; rep++) {
-      CK(cudaEventRecord(e0, b->stream));
-      akz_status st = akz_stage_scale(b, b->stream);
-      if (st != AKZ_OK) return st;
-      CK(cudaEventRecord(e1, b->stream));
-      CK(cudaEventSynchronize(e1));
+    for (int rep = 0; rep < 4 && ce == cudaSuccess && st == AKZ_OK; rep++) {
+      ce = cudaEventRecord(ev[nl], b->stream);
+      if (ce == cudaSuccess) st = akz_stage_scale(b, b->stream, nullptr, ev.data());
+      if (ce == cudaSuccess && st == AKZ_OK) ce = cudaEventSynchronize(ev[nl - 1]);
+      if (rep == 0) continue; /* the first repetition warms up */
       float ms = 0.0f;
-      CK(cudaEventElapsedTime(&ms, e0, e1));
-      if (rep > 0) tmin = std::min(tmin, ms); /* the first repetition warms up */
-    }
-    if (ms_per_depth && k < cap) ms_per_depth[k] = tmin;
-    if (tmin < best) {
-      best = tmin;
-      best_d = AKZ_DEPTH_MIN + k;
+      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, ev[nl], ev[nl - 1]);
+      tot[k] = std::min(tot[k], ms);
+      for (int l = 1; l < nl && ce == cudaSuccess; l++) {
+        ce = cudaEventElapsedTime(&ms, ev[l - 1], ev[l]);
+        tl[k][l] = std::min(tl[k][l], ms);
+      }
     }
   }
-  if (depth) *depth = best_d;
-  return akz_batch_set_fed_depth(b, best_d);
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
+  if (st != AKZ_OK) return st;
+  if (ce != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(ce));
+  for (int k = 0; k < nd && k < cap && ms_per_depth; k++) ms_per_depth[k] = tot[k];
+  for (int l = 1; l < nl; l++) {
+    int best = nd - 1;
+    for (int k = 0; k < nd; k++)
+      if (tl[k][l] < tl[best][l]) best = k;
+    b->fed_depth[l] = AKZ_DEPTH_MIN + best;
+  }
+  for (int l = 0; l < ndepths && depths; l++) depths[l] = l < nl ? (l ? b->fed_depth[l] : 0) : -1;
+  akz_use_fed_depths(b);
+  return AKZ_OK;
 }
 
 /* Learned FED surrogate for the levels of octave >= first_octave

@@ -142,6 +142,11 @@ cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int tw, int th, 
 size_t akz_fed_smem_bytes(int tw, int th, int steps, int first);
 cudaError_t akz_launch_area(const akz_area_params &p, int maxw, int maxh, cudaStream_t s);
 cudaError_t akz_launch_detect(const akz_detect_params &p, int ntiles, int max_step, cudaStream_t s);
+/* streaming detector for derivative steps 2..4: strips of
+ * akz_strip_tile_width(st) columns and AKZ_STRIP_CH rows */
+#define AKZ_STRIP_CH 256
+int akz_strip_tile_width(int st); /* 0 for steps the strip kernel does not compile */
+cudaError_t akz_launch_detect_strip(const akz_detect_params &p, int ntiles, cudaStream_t s);
 cudaError_t akz_launch_rowscan(const akz_tables &t, const int *rowcnt, int *rowscan, cudaStream_t s);
 cudaError_t akz_launch_extract(const akz_extract_params &p, int nrows, cudaStream_t s);
 cudaError_t akz_launch_nms(const akz_nms_params &p, cudaStream_t s);
@@ -149,10 +154,6 @@ cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaS
 
 #define AKZ_DETECT_TW 64
 #define AKZ_DETECT_TH 32
-/* Detector tile width of a level with derivative step st: 62 - 2 st for the
- * compiled steps 2..4 (the Lx, Ly region is then exactly 64 columns, 32
- * pairs: one warp per row), AKZ_DETECT_TW otherwise. */
-static inline __host__ __device__ int akz_detect_tile_width(int st) { return st >= 2 && st <= 4 ? 62 - 2 * st : AKZ_DETECT_TW; }
 #define AKZ_GAUSS_TW 64
 #define AKZ_GAUSS_TH 32
 #define AKZ_CONTRAST_TW 64

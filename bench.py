@@ -306,13 +306,13 @@ def workload_single640(args):
 
 
 def _pick_fed_depth(batch, args):
-    """FED blocking depth: the autotuner's pick (timed on the uploaded batch)
-    or the one asked for."""
+    """FED blocking depth per level: the autotuner's picks (timed on the
+    uploaded batch) or the one asked for."""
     if args.fed_depth == "auto":
         d, ms = batch.autotune()
         return d, {str(k): round(v, 4) for k, v in ms.items()}
     batch.set_fed_depth(int(args.fed_depth))
-    return int(args.fed_depth), None
+    return [int(args.fed_depth)], None
 
 
 def workload_uneven64(args):
@@ -349,7 +349,7 @@ def workload_uneven64(args):
         "latency_ms_alone": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                              "min": float(lat.min()), "max": float(lat.max())},
         "latency_ms_in_batch": step_ms, "keypoints_total": int(sum(counts)),
-        "fed_depth": fed_depth, "level_stage_ms_by_depth": depth_ms,
+        "fed_depth_per_level": fed_depth, "level_stage_ms_by_depth": depth_ms,
     }))
     return 0
 
@@ -588,12 +588,12 @@ def main():
                    "images_per_step_per_gpu": B, "parallelism": f"replicas x{ws}",
                    "l2": "inputs and working set larger than L2 (~%.1f GB per step)" % (B * image_algorithmic_bytes(W, H, 0) / 1e9),
                    "keypoints_per_image": nkp,
-                   "fed_depth": fed_depth, "level_stage_ms_by_depth": depth_ms},
+                   "fed_depth_per_level": fed_depth, "level_stage_ms_by_depth": depth_ms},
         "roofline": {"bound": "hbm", "kernel": "k_fed (level stage: 15 levels, 166 FED steps)",
                      "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"],
                      "traffic": (FED_TRAFFIC_PER_1080P_IMAGE * B
-                                 if (W, H) == (1920, 1080) and fed_depth == FED_TRAFFIC_DEPTH else None),
+                                 if (W, H) == (1920, 1080) and set(fed_depth) == {FED_TRAFFIC_DEPTH} else None),
                      "traffic_note": "ncu DRAM bytes of the level stage, 8-image capture scaled to the batch",
                      "algorithmic_bytes_per_image": fed_algorithmic_bytes(W, H), "launch_ms": fed_ms,
                      "peak_kind": f"{pk_kind} hbm_gbs"},

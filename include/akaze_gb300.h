@@ -286,10 +286,12 @@ AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pi
 
 /* Autotuner of the FED temporal-blocking depth (FED steps per level-kernel
  * launch, 4..8; no counterpart in the reference): on the uploaded images,
- * times the scale-space stage for each depth, keeps the fastest for later
- * runs and returns it in *depth; ms_per_depth (cap entries, may be NULL)
- * receives the times of depths 4, 5, ...  Synchronises the batch's stream. */
-AKZ_API akz_status akz_batch_autotune(akz_batch *b, float *ms_per_depth, int cap, int *depth);
+ * times every level of the scale-space stage at each depth and keeps the
+ * fastest depth per level for later runs.  ms_per_depth (cap entries, may be
+ * NULL) receives the stage time with every level at depth 4, 5, ...;
+ * depths (ndepths entries, may be NULL) the depth chosen per level (0 for
+ * level 0, -1 past the batch's last level).  Synchronises the batch's stream. */
+AKZ_API akz_status akz_batch_autotune(akz_batch *b, float *ms_per_depth, int cap, int *depths, int ndepths);
 
 /* Sets the FED blocking depth (4..8; 8 at creation) without timing. */
 AKZ_API akz_status akz_batch_set_fed_depth(akz_batch *b, int depth);

@@ -63,6 +63,20 @@ def test_keypoints_and_descriptors_match_oracle(gpu_lib, oracle, w, h, seed):
     assert np.array_equal(desc, od)
 
 
+@pytest.mark.parametrize("dfac", [0.8, 2.0])
+def test_other_derivative_steps_match_oracle(gpu_lib, oracle, dfac):
+    """derivative_factor 0.8 gives steps 1 and 2, 2.0 steps 3..5: levels of
+    the tile detector (steps other than 2..4) and of the strip detector in
+    one run."""
+    img = synth.synth_image(21, 640, 480)
+    ak, kp, desc, orc, okp, od = _run_both(gpu_lib, oracle, img, derivative_factor=dfac)
+    for l in range(orc.nlevels):
+        for name in ("Lx", "Ly"):
+            assert np.array_equal(ak.plane(l, name), orc.plane(l, name)), (l, name)
+    assert _exact(ak.extrema(), orc.extrema())
+    assert _exact(kp, okp) and np.array_equal(desc, od)
+
+
 def test_pair_matches(gpu_lib, oracle):
     a, b, H = synth.synth_pair(11, 640, 480)
     _, kpa, da, _, _, oda = _run_both(gpu_lib, oracle, a)
@@ -141,8 +155,9 @@ def test_fed_blocking_depths_give_identical_results(gpu_lib):
         for i, (k, d) in enumerate(want):
             kk, dd = b.results(i)
             assert kk.tobytes() == k.tobytes() and np.array_equal(dd, d), (depth, i)
-    best, ms = b.autotune()
-    assert 4 <= best <= 8 and sorted(ms) == [4, 5, 6, 7, 8] and all(v > 0 for v in ms.values())
+    depths, ms = b.autotune()
+    assert depths and all(4 <= x <= 8 for x in depths)
+    assert sorted(ms) == [4, 5, 6, 7, 8] and all(v > 0 for v in ms.values())
     b.upload(imgs)
     b.run()
     assert all(b.results(i)[0].tobytes() == want[i][0].tobytes() for i in range(len(sizes)))
