@@ -496,8 +496,8 @@ __device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
  * (nldiffusion_functions.cpp:50-53).  Values outside the image are finite
  * and unused: their conductance pair sums are zero.
  *
- * Leaves the level values of R0 in sT (RW x RH) and the conductance in sP
- * (RW x RH).  Filter passes work on column pairs with packed FP32x2 additions
+ * Leaves the level values of R0 in sP (stride RW + 6, R0 at row 3, column 3)
+ * and the conductance in sT (stride RW).  Filter passes work on column pairs with packed FP32x2 additions
  * and scalar products, in the reference's operation order:
  *   Gaussian  k0*(v[-2] + v[+2]) + k1*(v[-1] + v[+1]) + k2*v[0], rows then columns;
  *   Scharr    gx = 3*(d[y-1] + d[y+1]) + 10*d[y],  d = v[x+1] - v[x-1],
@@ -556,22 +556,27 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
   }
   __syncthreads();
 
-  /* 2. rows of the Gaussian on columns R0 +- 1 (sT column c is x = ox - 1 + c) */
+  /* 2. rows of the Gaussian on columns R0 +- 1 (sT column c is x = ox - 1 + c):
+   *    column pairs 0..63 by (tid & 63) on rows (tid >> 6) + 8k, pair 64
+   *    by the first PH threads */
   const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
+  static_assert(NP == 65 && NT == 512, "k_fed row-pass mapping");
+  auto hrow = [&](int row, int c) {
+    const float *r = sP + row * PS + c;
+    const float2 A = ld2(r), B = ld2(r + 2), C = ld2(r + 4);
+    const float2 s04 = f2add(A, C);
+    const float2 s13 = f2add(make_float2(A.y, B.x), make_float2(B.y, C.x));
+    float2 acc = make_float2(k0 * s04.x, k0 * s04.y);
+    acc = f2add(acc, make_float2(k1 * s13.x, k1 * s13.y));
+    acc = f2add(acc, make_float2(k2 * B.x, k2 * B.y));
+    st2(sT + row * SS + c, acc);
+  };
+  {
+    const int c = 2 * (tid & 63), r0 = tid >> 6;
 #pragma unroll
-  for (int k = 0; k < (PH * NP + NT - 1) / NT; k++) {
-    const int i = tid + NT * k;
-    if (i < PH * NP) {
-      const int row = i / NP, c = 2 * (i - row * NP);
-      const float *r = sP + row * PS + c;
-      const float2 A = ld2(r), B = ld2(r + 2), C = ld2(r + 4);
-      const float2 s04 = f2add(A, C);
-      const float2 s13 = f2add(make_float2(A.y, B.x), make_float2(B.y, C.x));
-      float2 acc = make_float2(k0 * s04.x, k0 * s04.y);
-      acc = f2add(acc, make_float2(k1 * s13.x, k1 * s13.y));
-      acc = f2add(acc, make_float2(k2 * B.x, k2 * B.y));
-      st2(sT + row * SS + c, acc);
-    }
+    for (int k = 0; k < (PH + 7) / 8; k++)
+      if (r0 + 8 * k < PH) hrow(r0 + 8 * k, c);
+    if (tid < PH) hrow(tid, 2 * 64);
   }
   __syncthreads();
 
@@ -604,13 +609,8 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
   }
   __syncthreads();
 
-  /* 4. level values of R0 into sT (free now), and the reflect-101 border
-   *    of Lsmooth: columns first, then whole rows (which fixes the corners) */
-#pragma unroll
-  for (int k = 0; k < RW * RH / NT; k++) {
-    const int i = tid + NT * k;
-    sT[i] = sP[(i / RW + 3) * PS + i % RW + 3];
-  }
+  /* 4. the reflect-101 border of Lsmooth: columns first, then whole rows
+   *    (which fixes the corners) */
   const int cm = -ox, cp = W - ox + 1; /* sS columns of x = -1 and x = W */
   const int nm = -oy, np = H - oy + 1; /* sS rows of y = -1 and y = H */
   if (cm >= 0 || cp < SS) {
@@ -630,8 +630,10 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
   }
 
   /* 5. Scharr gradient of Lsmooth and the conductance on R0, in this
-   *    thread's k_fed geometry: columns lx0, lx0+1, rows ly0 .. ly0+RB-1 */
-  float *sG = sP;
+   *    thread's k_fed geometry: columns lx0, lx0+1, rows ly0 .. ly0+RB-1;
+   *    the conductance goes to sT (free since pass 3), the level values
+   *    stay in sP */
+  float *sG = sT;
   const float inv_k = p.kc[L.image * 16 + L.octave].y;
   float2 dh[RB + 2], sh[RB + 2];
 #pragma unroll
@@ -666,7 +668,9 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
 }
 
 /* Registers of one k_fed thread (columns x0, x0+1 of R0, RB rows) from the
- * level values and the conductance on R0 in shared memory:
+ * level values (sL, row stride LS, at R0's origin) and the conductance on R0
+ * (sG, row stride RW) in shared memory (PAIRS: sL's column pairs are 8-byte
+ * aligned):
  *   Lp[r]   the two level values;
  *   gw[r]   c(x0-1) + c(x0)   the west flux pair of column x0;
  *   gm[r]   c(x0) + c(x0+1)   the flux pair between the two columns;
@@ -674,32 +678,88 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
  *   gs[r]   c(x, y) + c(x, y+1) of both columns; gn0 the pair above row 0.
  * A pair that crosses the image border is zero: the reference omits that
  * flux term (nldiffusion_functions.cpp:241-307), and zero times any finite
- * difference adds nothing. */
+ * difference adds nothing.  INTERIOR: R0 +- 1 lies inside the image, so no
+ * pair crosses the border. */
+template <bool INTERIOR, int LS, bool PAIRS>
 __device__ __forceinline__ void akz_fed_gather_smem(const float *sL, const float *sG, int lx0, int ly0, int x0, int ytop,
                                                     int W, int H, float2 *Lp, float *gw, float *gm, float *ge,
                                                     float2 *gs, float2 &gn0)
 {
   constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
-  const bool x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
   const int lxw = max(lx0 - 1, 0), lxe = min(lx0 + 2, RW - 1);
+  float2 c[RB + 2]; /* conductance pairs of rows ly0 - 1 .. ly0 + RB (clamped to R0) */
+#pragma unroll
+  for (int r = 0; r < RB + 2; r++) c[r] = ld2(sG + akz_clampi(ly0 - 1 + r, 0, RH - 1) * RW + lx0);
 #pragma unroll
   for (int r = 0; r < RB; r++) {
-    const int ly = ly0 + r, y = ytop + r;
-    const bool yin = y >= 0 && y < H;
-    Lp[r] = ld2(sL + ly * RW + lx0);
-    const float2 c = ld2(sG + ly * RW + lx0);
-    const float2 cs = ld2(sG + min(ly + 1, RH - 1) * RW + lx0);
+    const int ly = ly0 + r;
+    const float *lr = sL + ly * LS + lx0;
+    Lp[r] = PAIRS ? ld2(lr) : make_float2(lr[0], lr[1]);
     const float cw = sG[ly * RW + lxw], ce = sG[ly * RW + lxe];
-    gw[r] = (yin && x0in && x0 >= 1) ? cw + c.x : 0.0f;
-    gm[r] = (yin && x0 >= 0 && x0 + 1 < W) ? c.x + c.y : 0.0f;
-    ge[r] = (yin && x1in && x0 + 2 < W) ? c.y + ce : 0.0f;
-    gs[r].x = (x0in && y >= 0 && y + 1 < H) ? c.x + cs.x : 0.0f;
-    gs[r].y = (x1in && y >= 0 && y + 1 < H) ? c.y + cs.y : 0.0f;
+    const float2 cc = c[r + 1], cs = c[r + 2];
+    if (INTERIOR) {
+      gw[r] = cw + cc.x;
+      gm[r] = cc.x + cc.y;
+      ge[r] = cc.y + ce;
+      gs[r] = f2add(cc, cs);
+    } else {
+      const int y = ytop + r;
+      const bool yin = y >= 0 && y < H, x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
+      gw[r] = (yin && x0in && x0 >= 1) ? cw + cc.x : 0.0f;
+      gm[r] = (yin && x0 >= 0 && x0 + 1 < W) ? cc.x + cc.y : 0.0f;
+      ge[r] = (yin && x1in && x0 + 2 < W) ? cc.y + ce : 0.0f;
+      gs[r].x = (x0in && y >= 0 && y + 1 < H) ? cc.x + cs.x : 0.0f;
+      gs[r].y = (x1in && y >= 0 && y + 1 < H) ? cc.y + cs.y : 0.0f;
+    }
   }
-  const float2 cn = ld2(sG + max(ly0 - 1, 0) * RW + lx0), c0 = ld2(sG + ly0 * RW + lx0);
-  const bool nin = ytop >= 1 && ytop < H;
-  gn0.x = (x0in && nin) ? cn.x + c0.x : 0.0f;
-  gn0.y = (x1in && nin) ? cn.y + c0.y : 0.0f;
+  if (INTERIOR) {
+    gn0 = f2add(c[0], c[1]);
+  } else {
+    const bool nin = ytop >= 1 && ytop < H, x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
+    gn0.x = (x0in && nin) ? c[0].x + c[1].x : 0.0f;
+    gn0.y = (x1in && nin) ? c[0].y + c[1].y : 0.0f;
+  }
+}
+
+/* One FED step of this thread's RB x 2 pixels (nld_step_scalar,
+ * nldiffusion_functions.cpp:232-237, :309-316):
+ *   L += h * (((xpos - xneg) + ypos) - yneg)
+ * Each flux product is formed once and used twice, which is exact: the
+ * reference's xneg at x+1 is (c(x) + c(x+1)) * (L(x+1) - L(x)), the same
+ * operands in the same order as xpos at x, and likewise yneg at y+1 and ypos
+ * at y.  Additions run as packed FP32x2 pairs of the two columns; products
+ * stay scalar.  cur: level values (row stride CS, at R0's origin; PAIRS: its
+ * column pairs are 8-byte aligned); nxt: the new values (row stride RW). */
+template <int CS, bool PAIRS>
+__device__ __forceinline__ void akz_fed_step(const float *cur, float *nxt, float h, int lx0, int ly0, float2 *Lp,
+                                             const float *gw, const float *gm, const float *ge, const float2 *gs,
+                                             float2 gn0)
+{
+  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
+  const int lyn = max(ly0 - 1, 0), lys = min(ly0 + RB, RH - 1);
+  const int lxw = max(lx0 - 1, 0), lxe = min(lx0 + 2, RW - 1);
+  const float *an = cur + lyn * CS + lx0, *bs = cur + lys * CS + lx0;
+  const float2 above = PAIRS ? ld2(an) : make_float2(an[0], an[1]);
+  const float2 below = PAIRS ? ld2(bs) : make_float2(bs[0], bs[1]);
+  const float2 dn = f2sub(Lp[0], above);
+  float2 Fn = make_float2(gn0.x * dn.x, gn0.y * dn.y);
+#pragma unroll
+  for (int r = 0; r < RB; r++) {
+    const int ly = ly0 + r;
+    const float2 Lc = Lp[r];
+    const float Lw = cur[ly * CS + lxw], Le = cur[ly * CS + lxe];
+    const float2 dwm = f2sub(Lc, make_float2(Lw, Lc.x)); /* L(x0)-L(x0-1), L(x0+1)-L(x0) */
+    const float de = Le - Lc.y;                          /* L(x0+2)-L(x0+1) */
+    const float Fw = gw[r] * dwm.x, Fm = gm[r] * dwm.y, Fe = ge[r] * de;
+    const float2 xs = f2sub(make_float2(Fm, Fe), make_float2(Fw, Fm)); /* xpos - xneg */
+    const float2 ds = f2sub(r < RB - 1 ? Lp[r + 1] : below, Lc);
+    const float2 Fs = make_float2(gs[r].x * ds.x, gs[r].y * ds.y); /* ypos */
+    const float2 t = f2sub(f2add(xs, Fs), Fn);
+    const float2 nv = f2add(Lc, make_float2(h * t.x, h * t.y));
+    st2(nxt + ly * RW + lx0, nv);
+    Lp[r] = nv;
+    Fn = Fs;
+  }
 }
 
 __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
@@ -741,9 +801,18 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
       akz_fed_prologue<0>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
     else
       akz_fed_prologue<2>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
-    akz_fed_gather_smem(sT, sP, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
-    cur = sT; /* holds the level values of R0 */
-    nxt = sS; /* free once the conductance is done */
+    const float *sL = sP + 3 * PS + 3; /* level values of R0 */
+    const bool interior = ox >= 1 && oy >= 1 && ox + RW + 1 <= W && oy + RH + 1 <= H;
+    if (interior)
+      akz_fed_gather_smem<true, PS, false>(sL, sT, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
+    else
+      akz_fed_gather_smem<false, PS, false>(sL, sT, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
+    if (d > 0) { /* the first step reads the level values where the prologue left them */
+      akz_fed_step<PS, false>(sL, sS, p.h[0], lx0, ly0, Lp, gw, gm, ge, gs, gn0);
+      __syncthreads();
+    }
+    cur = sS;
+    nxt = sT; /* the conductance plane, read into registers before the barrier above */
   } else {
     cur = sm;
     nxt = sm + RW * RH;
@@ -782,38 +851,8 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
     __syncthreads();
   }
 
-  /* FED steps (nld_step_scalar, nldiffusion_functions.cpp:232-237, :309-316):
-   *   L += h * (((xpos - xneg) + ypos) - yneg)
-   * Each flux product is formed once and used twice, which is exact: the
-   * reference's xneg at x+1 is (c(x) + c(x+1)) * (L(x+1) - L(x)), the same
-   * operands in the same order as xpos at x, and likewise yneg at y+1 and ypos
-   * at y.  Additions run as packed FP32x2 pairs of the two columns; products
-   * stay scalar. */
-  const int lyn = max(ly0 - 1, 0), lys = min(ly0 + RB, RH - 1);
-  const int lxw = max(lx0 - 1, 0), lxe = min(lx0 + 2, RW - 1);
-  for (int s = 0; s < d; s++) {
-    const float h = p.h[s];
-    const float2 above = ld2(cur + lyn * RW + lx0);
-    const float2 below = ld2(cur + lys * RW + lx0);
-    const float2 dn = f2sub(Lp[0], above);
-    float2 Fn = make_float2(gn0.x * dn.x, gn0.y * dn.y);
-#pragma unroll
-    for (int r = 0; r < RB; r++) {
-      const int ly = ly0 + r;
-      const float2 Lc = Lp[r];
-      const float Lw = cur[ly * RW + lxw], Le = cur[ly * RW + lxe];
-      const float2 dwm = f2sub(Lc, make_float2(Lw, Lc.x)); /* L(x0)-L(x0-1), L(x0+1)-L(x0) */
-      const float de = Le - Lc.y;                          /* L(x0+2)-L(x0+1) */
-      const float Fw = gw[r] * dwm.x, Fm = gm[r] * dwm.y, Fe = ge[r] * de;
-      const float2 xs = f2sub(make_float2(Fm, Fe), make_float2(Fw, Fm)); /* xpos - xneg */
-      const float2 ds = f2sub(r < RB - 1 ? Lp[r + 1] : below, Lc);
-      const float2 Fs = make_float2(gs[r].x * ds.x, gs[r].y * ds.y); /* ypos */
-      const float2 t = f2sub(f2add(xs, Fs), Fn);
-      const float2 nv = f2add(Lc, make_float2(h * t.x, h * t.y));
-      st2(nxt + ly * RW + lx0, nv);
-      Lp[r] = nv;
-      Fn = Fs;
-    }
+  for (int s = p.first ? 1 : 0; s < d; s++) {
+    akz_fed_step<RW, true>(cur, nxt, p.h[s], lx0, ly0, Lp, gw, gm, ge, gs, gn0);
     __syncthreads();
     float *t = cur;
     cur = nxt;
