@@ -20,6 +20,7 @@
 #include "akz_fmath.h"
 
 #define AKZ_DESC_WARPS 4
+#define AKZ_DESC_HALF 7 /* 2 x 7 x 32 = 448 >= 21 x 21 window samples */
 #define AKZ_DESC_MAXIMG 1024 /* images whose keypoint offsets a CTA keeps in shared memory */
 #define AKZ_CV_PI 3.1415926535897932384626433832795
 
@@ -35,7 +36,6 @@ struct akz_warp_smem {
   float v[87];
   float bx[42], by[42];
   float wx[42], wy[42];
-  unsigned char bin[112];
 };
 
 __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_params p)
@@ -58,6 +58,16 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
     }
     __syncthreads();
   }
+  /* orientation sample offsets (packed i, j) and Gaussian weights, indexed
+   * by sample: lane-consecutive shared loads instead of divergent constant
+   * reads */
+  __shared__ int sOrIJ[112];
+  __shared__ float sOrW[112];
+  for (int t = threadIdx.x; t < 109; t += blockDim.x) {
+    sOrIJ[t] = ((int)c_oi[t] & 0xffff) + (int)c_oj[t] * 65536;
+    sOrW[t] = p.gw[c_or2[t]];
+  }
+  __syncthreads();
   int total = 0;
   if (table)
     total = sOff[p.t.nimg];
@@ -97,34 +107,66 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
       const int step = (int)(0.5f * kp.size + 0.5f) >> octave;
       const int x = (int)(kp.x + 0.5f) >> octave;
       const int y = (int)(kp.y + 0.5f) >> octave;
-      for (int s = lane; s < 109; s += 32) {
-        const int r2 = c_or2[s];
-        const int sx = akz_clampi(x + step * c_oi[s], 0, W - 1), sy = akz_clampi(y + step * c_oj[s], 0, H - 1);
-        const long long pos = (long long)sy * pitch + sx;
-        const float dx = p.gw[r2] * __ldg(lxp + pos);
-        const float dy = p.gw[r2] * __ldg(lyp + pos);
-        const float a = akz_atan2f(dy, dx);
-        int bin = (int)((double)a * (21 / AKZ_CV_PI)) + 21;
-        bin = bin > 41 ? 41 : (bin < 0 ? 0 : bin);
-        S.s[0][s] = dx;
-        S.s[1][s] = dy;
-        S.bin[s] = (unsigned char)bin;
+      /* every gather of the 109 samples in flight before the first use */
+      float gxv[4], gyv[4];
+#pragma unroll
+      for (int it = 0; it < 4; it++) {
+        const int s = lane + 32 * it;
+        if (s < 109) {
+          const int ij = sOrIJ[s];
+          const int sx = akz_clampi(x + step * (int)(short)(ij & 0xffff), 0, W - 1);
+          const int sy = akz_clampi(y + step * (ij >> 16), 0, H - 1);
+          const long long pos = (long long)sy * pitch + sx;
+          gxv[it] = __ldg(lxp + pos);
+          gyv[it] = __ldg(lyp + pos);
+        }
+      }
+      /* per bin, a 109-bit mask of its samples (4 words in the third
+       * sample channel, free until the M-LDB samples) */
+      uint32_t *bm = reinterpret_cast<uint32_t *>(S.s[2]);
+      for (int t = lane; t < 42 * 4; t += 32) bm[t] = 0u;
+      __syncwarp();
+#pragma unroll
+      for (int it = 0; it < 4; it++) {
+        const int s = lane + 32 * it;
+        int bin = 64; /* no sample */
+        if (s < 109) {
+          const float w = sOrW[s];
+          const float dx = w * gxv[it];
+          const float dy = w * gyv[it];
+          const float a = akz_atan2f(dy, dx);
+          /* (int)((double)a * (21 / pi)): the float product is within
+           * 2.5e-6 of the double one, so away from integers their
+           * truncations agree; near an integer the double product decides */
+          const float tf = a * (float)(21 / AKZ_CV_PI);
+          const int ib = fabsf(tf - rintf(tf)) > 0x1p-17f ? (int)tf : (int)((double)a * (21 / AKZ_CV_PI));
+          bin = ib + 21;
+          bin = bin > 41 ? 41 : (bin < 0 ? 0 : bin);
+          S.s[0][s] = dx;
+          S.s[1][s] = dy;
+        }
+        const uint32_t grp = __match_any_sync(0xffffffffu, bin);
+        if (bin < 42 && (grp & ((1u << lane) - 1u)) == 0u) bm[bin * 4 + it] = grp; /* the group's lowest lane */
       }
       __syncwarp();
       {
-        /* bins lane and lane + 32 in one pass, each summed in sample order */
+        /* bins lane and lane + 32, each summed over its samples in sample order */
         const int b1 = lane + 32;
         float rx0 = 0.0f, ry0 = 0.0f, rx1 = 0.0f, ry1 = 0.0f;
-        for (int s = 0; s < 109; s++) {
-          const int b = S.bin[s];
-          const float sx = S.s[0][s], sy = S.s[1][s];
-          if (b == lane) {
-            rx0 += sx;
-            ry0 += sy;
+#pragma unroll
+        for (int w = 0; w < 4; w++) {
+          uint32_t m0 = bm[lane * 4 + w], m1 = b1 < 42 ? bm[b1 * 4 + w] : 0u;
+          while (m0) {
+            const int s = 32 * w + __ffs(m0) - 1;
+            m0 &= m0 - 1u;
+            rx0 += S.s[0][s];
+            ry0 += S.s[1][s];
           }
-          if (b == b1) {
-            rx1 += sx;
-            ry1 += sy;
+          while (m1) {
+            const int s = 32 * w + __ffs(m1) - 1;
+            m1 &= m1 - 1u;
+            rx1 += S.s[0][s];
+            ry1 += S.s[1][s];
           }
         }
         S.bx[lane] = rx0;
@@ -174,16 +216,48 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
     const int scale = (int)(0.5f * kp.size * iratio + 0.5f);
     const float xf = kp.x * iratio, yf = kp.y * iratio;
     const float fs = (float)scale;
-    for (int s = lane; s < win * win; s += 32) {
+    /* the window's samples in two halves of AKZ_DESC_HALF iterations per
+     * lane, every gather of a half in flight before the first use (the
+     * window has at most 21 x 21 = 14 x 32 samples: pattern size <= 10) */
+    const int nsmp = win * win;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      float vi[AKZ_DESC_HALF], vx[AKZ_DESC_HALF], vy[AKZ_DESC_HALF];
+#pragma unroll
+      for (int it = 0; it < AKZ_DESC_HALF; it++) {
+        const int s = lane + 32 * (h * AKZ_DESC_HALF + it);
+        if (s < nsmp) {
+          const int yy = s / win, xx = s - yy * win;
+          const int l = xx - size2, kk = yy - size2;
+          int xp = (int)(xf + fs * ((float)kk * co - (float)l * si) + 0.5f);
+          int yp = (int)(yf + fs * ((float)kk * si + (float)l * co) + 0.5f);
+          xp = akz_clampi(xp, 0, W - 1);
+          yp = akz_clampi(yp, 0, H - 1);
+          const long long pos = (long long)yp * pitch + xp;
+          vi[it] = __ldg(ltp + pos);
+          vx[it] = __ldg(lxp + pos);
+          vy[it] = __ldg(lyp + pos);
+        }
+      }
+#pragma unroll
+      for (int it = 0; it < AKZ_DESC_HALF; it++) {
+        const int s = lane + 32 * (h * AKZ_DESC_HALF + it);
+        if (s < nsmp) {
+          const float dx = vx[it], dy = vy[it];
+          S.s[0][s] = vi[it];
+          S.s[1][s] = -dx * si + dy * co;
+          S.s[2][s] = dx * co + dy * si;
+        }
+      }
+    }
+    for (int s = lane + 64 * AKZ_DESC_HALF; s < nsmp; s += 32) { /* larger windows: not reached for pattern size <= 10 */
       const int yy = s / win, xx = s - yy * win;
       const int l = xx - size2, kk = yy - size2;
-      int xp = (int)(xf + fs * ((float)kk * co - (float)l * si) + 0.5f);
-      int yp = (int)(yf + fs * ((float)kk * si + (float)l * co) + 0.5f);
-      xp = akz_clampi(xp, 0, W - 1);
-      yp = akz_clampi(yp, 0, H - 1);
+      const int xp = akz_clampi((int)(xf + fs * ((float)kk * co - (float)l * si) + 0.5f), 0, W - 1);
+      const int yp = akz_clampi((int)(yf + fs * ((float)kk * si + (float)l * co) + 0.5f), 0, H - 1);
       const long long pos = (long long)yp * pitch + xp;
-      const float im = __ldg(ltp + pos), dx = __ldg(lxp + pos), dy = __ldg(lyp + pos);
-      S.s[0][s] = im;
+      const float dx = __ldg(lxp + pos), dy = __ldg(lyp + pos);
+      S.s[0][s] = __ldg(ltp + pos);
       S.s[1][s] = -dx * si + dy * co;
       S.s[2][s] = dx * co + dy * si;
     }
