@@ -16,11 +16,13 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "akz_device.cuh"
 #include "akz_fmath.h"
 
 #define AKZ_DESC_WARPS 4
-#define AKZ_DESC_HALF 7 /* 2 x 7 x 32 = 448 >= 21 x 21 window samples */
+#define AKZ_DESC_ITERS 14 /* 14 x 32 = 448 >= 21 x 21 window samples */
 #define AKZ_DESC_MAXIMG 1024 /* images whose keypoint offsets a CTA keeps in shared memory */
 #define AKZ_CV_PI 3.1415926535897932384626433832795
 
@@ -30,6 +32,11 @@ __constant__ signed char c_oi[109], c_oj[109], c_or2[109];
  * load per warp and bit word (a __constant__ table would serialise the
  * lanes' different addresses) */
 __device__ unsigned char g_cmp1[512], g_cmp2[512];
+/* the M-LDB window's samples in the order the warp gathers them: 4 x 8
+ * blocks of the window, so one gather instruction touches a compact patch
+ * of the level (its sectors) rather than one and a half rotated rows; each
+ * entry is (row << 8) | column, the stores keep the raster index */
+__device__ unsigned short g_smp_order[32 * AKZ_DESC_ITERS];
 
 struct akz_warp_smem {
   float s[3][441];
@@ -63,10 +70,12 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
    * reads */
   __shared__ int sOrIJ[112];
   __shared__ float sOrW[112];
+  __shared__ unsigned short sOrd[32 * AKZ_DESC_ITERS];
   for (int t = threadIdx.x; t < 109; t += blockDim.x) {
     sOrIJ[t] = ((int)c_oi[t] & 0xffff) + (int)c_oj[t] * 65536;
     sOrW[t] = p.gw[c_or2[t]];
   }
+  for (int t = threadIdx.x; t < 32 * AKZ_DESC_ITERS; t += blockDim.x) sOrd[t] = g_smp_order[t];
   __syncthreads();
   int total = 0;
   if (table)
@@ -216,18 +225,17 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
     const int scale = (int)(0.5f * kp.size * iratio + 0.5f);
     const float xf = kp.x * iratio, yf = kp.y * iratio;
     const float fs = (float)scale;
-    /* the window's samples in two halves of AKZ_DESC_HALF iterations per
-     * lane, every gather of a half in flight before the first use (the
-     * window has at most 21 x 21 = 14 x 32 samples: pattern size <= 10) */
+    /* the window's samples, every gather in flight before the first use
+     * (the window has at most 21 x 21 <= 14 x 32 samples: pattern size
+     * <= 10), in the block order of g_smp_order */
     const int nsmp = win * win;
+    {
+      float vi[AKZ_DESC_ITERS], vx[AKZ_DESC_ITERS], vy[AKZ_DESC_ITERS];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      float vi[AKZ_DESC_HALF], vx[AKZ_DESC_HALF], vy[AKZ_DESC_HALF];
-#pragma unroll
-      for (int it = 0; it < AKZ_DESC_HALF; it++) {
-        const int s = lane + 32 * (h * AKZ_DESC_HALF + it);
-        if (s < nsmp) {
-          const int yy = s / win, xx = s - yy * win;
+      for (int it = 0; it < AKZ_DESC_ITERS; it++) {
+        const int idx = lane + 32 * it;
+        if (idx < nsmp) {
+          const int o = sOrd[idx], yy = o >> 8, xx = o & 255;
           const int l = xx - size2, kk = yy - size2;
           int xp = (int)(xf + fs * ((float)kk * co - (float)l * si) + 0.5f);
           int yp = (int)(yf + fs * ((float)kk * si + (float)l * co) + 0.5f);
@@ -240,9 +248,10 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
         }
       }
 #pragma unroll
-      for (int it = 0; it < AKZ_DESC_HALF; it++) {
-        const int s = lane + 32 * (h * AKZ_DESC_HALF + it);
-        if (s < nsmp) {
+      for (int it = 0; it < AKZ_DESC_ITERS; it++) {
+        const int idx = lane + 32 * it;
+        if (idx < nsmp) {
+          const int o = sOrd[idx], s = (o >> 8) * win + (o & 255);
           const float dx = vx[it], dy = vy[it];
           S.s[0][s] = vi[it];
           S.s[1][s] = -dx * si + dy * co;
@@ -250,7 +259,7 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
         }
       }
     }
-    for (int s = lane + 64 * AKZ_DESC_HALF; s < nsmp; s += 32) { /* larger windows: not reached for pattern size <= 10 */
+    for (int s = lane + 32 * AKZ_DESC_ITERS; s < nsmp; s += 32) { /* larger windows: not reached for pattern size <= 10 */
       const int yy = s / win, xx = s - yy * win;
       const int l = xx - size2, kk = yy - size2;
       const int xp = akz_clampi((int)(xf + fs * ((float)kk * co - (float)l * si) + 0.5f), 0, W - 1);
@@ -299,10 +308,18 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
   }
 }
 
-static int akz_describe_tables_ready = -1;
+static int akz_describe_tables_ready = -1, akz_describe_tables_win = -1;
 
-static cudaError_t akz_init_describe_tables()
+static cudaError_t akz_init_describe_tables(int win)
 {
+  unsigned short ord[32 * AKZ_DESC_ITERS];
+  int no = 0;
+  for (int tr = 0; tr < win; tr += 4)
+    for (int tc = 0; tc < win; tc += 8)
+      for (int r = tr; r < tr + 4 && r < win; r++)
+        for (int c = tc; c < tc + 8 && c < win; c++)
+          if (no < 32 * AKZ_DESC_ITERS) ord[no++] = (unsigned short)((r << 8) | c);
+  while (no < 32 * AKZ_DESC_ITERS) ord[no++] = 0;
   signed char oi[109], oj[109], orr[109];
   int n = 0;
   for (int tx = 0; tx < 208; tx++) {
@@ -329,6 +346,7 @@ static cudaError_t akz_init_describe_tables()
   if ((e = cudaMemcpyToSymbol(c_oi, oi, sizeof(oi))) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_oj, oj, sizeof(oj))) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_or2, orr, sizeof(orr))) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(g_smp_order, ord, sizeof(ord))) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(g_cmp1, c1, sizeof(c1))) != cudaSuccess) return e;
   return cudaMemcpyToSymbol(g_cmp2, c2, sizeof(c2));
 }
@@ -337,10 +355,13 @@ cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaS
 {
   int dev = 0;
   cudaGetDevice(&dev);
-  if (akz_describe_tables_ready != dev) {
-    const cudaError_t e = akz_init_describe_tables();
+  const int ps = p.pattern_size, s3 = (int)ceilf(2.0f * (float)ps / 3.0f), s4 = (int)ceilf(0.5f * (float)ps);
+  const int win = std::max(3 * s3, 4 * s4);
+  if (akz_describe_tables_ready != dev || akz_describe_tables_win != win) {
+    const cudaError_t e = akz_init_describe_tables(win);
     if (e != cudaSuccess) return e;
     akz_describe_tables_ready = dev;
+    akz_describe_tables_win = win;
   }
   if (nblocks <= 0) return cudaSuccess;
   k_describe<<<nblocks, 32 * AKZ_DESC_WARPS, 0, s>>>(p);
