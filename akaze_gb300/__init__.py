@@ -361,10 +361,104 @@ class Batch:
                                                          _ptr(counts), ctypes.byref(total)))
         return counts
 
+    def submit(self, imgs):
+        """First half of detect_describe_packed: enqueues the upload, the
+        graph and the count read-back, and returns at once; the images must
+        stay unchanged until collect_packed."""
+        self._sub = [np.ascontiguousarray(im, np.uint8) for im in imgs]
+        ptrs = (ctypes.c_void_p * self.n)(*[im.ctypes.data for im in self._sub])
+        strides = (ctypes.c_size_t * self.n)(*[im.strides[0] for im in self._sub])
+        check(self._lib.akz_batch_submit(self._h, ptrs, strides))
+
+    def collect_packed(self, kp_out, d_out):
+        """Second half: waits for this batch, writes its results packed into
+        kp_out / d_out; returns (per-image counts, total)."""
+        counts = np.zeros(self.n, np.int32)
+        total = ctypes.c_int()
+        check(self._lib.akz_batch_collect_packed(self._h, _ptr(kp_out), _ptr(d_out), len(kp_out), _ptr(counts),
+                                                 ctypes.byref(total)))
+        self._sub = None
+        return counts, total.value
+
     def plane(self, i, level, name="Lt", shape=None):
         out = np.empty(shape, np.float32)
         check(self._lib.akz_batch_level_plane(self._h, i, level, _PLANES[name], _ptr(out)))
         return out
+
+
+class BatchGroup:
+    """A batch split into `groups` native batches of consecutive images, each
+    with its own CUDA stream and captured graph, so that the stages of one
+    group overlap those of the others on the GPU (suppression is one CTA per
+    image, the small FED levels leave SMs idle, and host<->device copies of
+    one group overlap the kernels of another).  Results equal those of one
+    Batch over the same images; image i keeps its index."""
+
+    def __init__(self, options, sizes, groups=2):
+        sizes = [(int(w), int(h)) for w, h in sizes]
+        groups = max(1, min(int(groups), len(sizes)))
+        bounds = [len(sizes) * g // groups for g in range(groups + 1)]
+        self.parts = [Batch(options, sizes[bounds[g]:bounds[g + 1]]) for g in range(groups)]
+        self.bounds = bounds
+        self.sizes = sizes
+        self.n = len(sizes)
+        self.options = options
+
+    def _locate(self, i):
+        for g, b in enumerate(self.parts):
+            if i < self.bounds[g + 1]:
+                return b, i - self.bounds[g]
+        raise IndexError(i)
+
+    def close(self):
+        for b in self.parts:
+            b.close()
+
+    def set_streams(self, handles):
+        for b, h in zip(self.parts, handles):
+            b.set_stream(h)
+
+    def set_fed_depth(self, depth):
+        for b in self.parts:
+            b.set_fed_depth(depth)
+
+    def autotune(self):
+        return [b.autotune() for b in self.parts]
+
+    def upload(self, images):
+        for g, b in enumerate(self.parts):
+            b.upload(images[self.bounds[g]:self.bounds[g + 1]])
+
+    def run(self):
+        """Launches every group (asynchronous, each on its own stream)."""
+        for b in self.parts:
+            b.run()
+
+    def counts(self):
+        return np.concatenate([b.counts() for b in self.parts])
+
+    def results(self, i):
+        b, k = self._locate(i)
+        return b.results(k)
+
+    def plane(self, i, level, name="Lt", shape=None):
+        b, k = self._locate(i)
+        return b.plane(k, level, name, shape)
+
+    def detect_describe_packed(self, imgs, kp_out, d_out):
+        """Whole job with host buffers: every group is submitted (upload,
+        graph, count read-back, all asynchronous on its own stream), then
+        collected in order, each into kp_out / d_out right after the groups
+        before it, so a group's copies overlap the others' kernels.  Returns
+        the per-image counts."""
+        for g, b in enumerate(self.parts):
+            b.submit(imgs[self.bounds[g]:self.bounds[g + 1]])
+        at, counts = 0, []
+        for b in self.parts:
+            c, n = b.collect_packed(kp_out[at:], d_out[at:])
+            counts.append(c)
+            at += n
+        return np.concatenate(counts)
 
 
 def save_keypoints(path, kpts, desc=None):

@@ -31,7 +31,7 @@ EXPORTS = [
     "akz_sg_weight_elems", "akz_sg_infer_level", "akz_sg_mse_grad", "akz_batch_set_surrogate",
     "akz_batch_surrogate_errors", "akz_nndr_homography_inliers", "akz_save_keypoints",
     "akz_batch_detect_describe_packed", "akz_sg_set_tcgen05", "akz_sg_tcgen05_status", "akz_selfcheck_pm_g2",
-    "akz_batch_autotune", "akz_batch_set_fed_depth",
+    "akz_batch_autotune", "akz_batch_set_fed_depth", "akz_batch_submit", "akz_batch_collect_packed",
 ]
 
 
@@ -124,6 +124,8 @@ def load():
         "akz_selfcheck_pm_g2": ([P, P, I, I, P], I),
         "akz_batch_autotune": ([P, P, I, P, I], I),
         "akz_batch_set_fed_depth": ([P, I], I),
+        "akz_batch_submit": ([P, P, P], I),
+        "akz_batch_collect_packed": ([P, P, P, I, P, IP], I),
         "akz_sg_infer_level": ([P, P, ctypes.c_size_t, I, I, ctypes.c_float, ctypes.c_float, P, P, P, P, P], I),
     }
     for name, (args, res) in sig.items():

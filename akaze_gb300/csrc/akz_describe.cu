@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "akz_device.cuh"
 #include "akz_fmath.h"
@@ -36,7 +37,8 @@ __device__ unsigned char g_cmp1[512], g_cmp2[512];
  * blocks of the window, so one gather instruction touches a compact patch
  * of the level (its sectors) rather than one and a half rotated rows; each
  * entry is (row << 8) | column, the stores keep the raster index */
-__device__ unsigned short g_smp_order[32 * AKZ_DESC_ITERS];
+#define AKZ_DESC_MAXWIN 21 /* window of pattern size 10 */
+__device__ unsigned short g_smp_order[AKZ_DESC_MAXWIN + 1][32 * AKZ_DESC_ITERS]; /* per window size */
 
 struct akz_warp_smem {
   float s[3][441];
@@ -75,7 +77,12 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
     sOrIJ[t] = ((int)c_oi[t] & 0xffff) + (int)c_oj[t] * 65536;
     sOrW[t] = p.gw[c_or2[t]];
   }
-  for (int t = threadIdx.x; t < 32 * AKZ_DESC_ITERS; t += blockDim.x) sOrd[t] = g_smp_order[t];
+  {
+    const int ps0 = p.pattern_size;
+    const int w0 = max(3 * (int)ceilf(2.0f * (float)ps0 / 3.0f), 4 * (int)ceilf(0.5f * (float)ps0));
+    const unsigned short *ord = g_smp_order[min(w0, AKZ_DESC_MAXWIN)];
+    for (int t = threadIdx.x; t < 32 * AKZ_DESC_ITERS; t += blockDim.x) sOrd[t] = ord[t];
+  }
   __syncthreads();
   int total = 0;
   if (table)
@@ -308,18 +315,21 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
   }
 }
 
-static int akz_describe_tables_ready = -1, akz_describe_tables_win = -1;
+#define AKZ_DESC_MAXDEV 64
+static bool akz_describe_tables_ready[AKZ_DESC_MAXDEV];
+static std::mutex akz_describe_tables_mutex;
 
-static cudaError_t akz_init_describe_tables(int win)
+static cudaError_t akz_init_describe_tables()
 {
-  unsigned short ord[32 * AKZ_DESC_ITERS];
-  int no = 0;
-  for (int tr = 0; tr < win; tr += 4)
-    for (int tc = 0; tc < win; tc += 8)
-      for (int r = tr; r < tr + 4 && r < win; r++)
-        for (int c = tc; c < tc + 8 && c < win; c++)
-          if (no < 32 * AKZ_DESC_ITERS) ord[no++] = (unsigned short)((r << 8) | c);
-  while (no < 32 * AKZ_DESC_ITERS) ord[no++] = 0;
+  static unsigned short ord[AKZ_DESC_MAXWIN + 1][32 * AKZ_DESC_ITERS];
+  for (int win = 1; win <= AKZ_DESC_MAXWIN; win++) {
+    int no = 0;
+    for (int tr = 0; tr < win; tr += 4)
+      for (int tc = 0; tc < win; tc += 8)
+        for (int r = tr; r < tr + 4 && r < win; r++)
+          for (int c = tc; c < tc + 8 && c < win; c++) ord[win][no++] = (unsigned short)((r << 8) | c);
+    while (no < 32 * AKZ_DESC_ITERS) ord[win][no++] = 0;
+  }
   signed char oi[109], oj[109], orr[109];
   int n = 0;
   for (int tx = 0; tx < 208; tx++) {
@@ -355,13 +365,14 @@ cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaS
 {
   int dev = 0;
   cudaGetDevice(&dev);
-  const int ps = p.pattern_size, s3 = (int)ceilf(2.0f * (float)ps / 3.0f), s4 = (int)ceilf(0.5f * (float)ps);
-  const int win = std::max(3 * s3, 4 * s4);
-  if (akz_describe_tables_ready != dev || akz_describe_tables_win != win) {
-    const cudaError_t e = akz_init_describe_tables(win);
-    if (e != cudaSuccess) return e;
-    akz_describe_tables_ready = dev;
-    akz_describe_tables_win = win;
+  if (dev < 0 || dev >= AKZ_DESC_MAXDEV || p.pattern_size < 1 || p.pattern_size > 10) return cudaErrorInvalidValue;
+  {
+    std::lock_guard<std::mutex> lock(akz_describe_tables_mutex);
+    if (!akz_describe_tables_ready[dev]) {
+      const cudaError_t e = akz_init_describe_tables();
+      if (e != cudaSuccess) return e;
+      akz_describe_tables_ready[dev] = true;
+    }
   }
   if (nblocks <= 0) return cudaSuccess;
   k_describe<<<nblocks, 32 * AKZ_DESC_WARPS, 0, s>>>(p);

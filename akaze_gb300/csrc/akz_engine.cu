@@ -306,7 +306,8 @@ struct akz_batch {
   uint32_t *d_desc = nullptr;
   int *d_nbr = nullptr;
   unsigned char *d_nbc = nullptr;
-  void *d_pack = nullptr; /* packed results of akz_batch_detect_describe_packed, grown on demand */
+  void *d_pack = nullptr; /* packed results of akz_batch_collect_packed, grown on demand */
+  bool submitted = false; /* akz_batch_submit issued, akz_batch_collect_packed not yet */
   size_t cap_pack = 0;    /* rows */
   size_t raw_all = 0;
   int input_f32 = 0;
@@ -316,7 +317,7 @@ struct akz_batch {
   cudaStream_t graph_stream = nullptr;
   akz_image_stats *h_stats = nullptr;
   int nsm = 152;
-  cudaEvent_t ev[8] = {};
+  cudaEvent_t ev[9] = {}; /* 0-7 stage timing, 8 submit/collect */
 };
 
 static size_t akz_align(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -1293,16 +1294,31 @@ AKZ_API akz_status akz_batch_detect_describe(akz_batch *b, const uint8_t *const 
   return AKZ_OK;
 }
 
-AKZ_API akz_status akz_batch_detect_describe_packed(akz_batch *b, const uint8_t *const *images, const size_t *strides,
-                                                    akz_keypoint *kpts, uint8_t *desc, int capacity, int *counts,
-                                                    int *total)
+AKZ_API akz_status akz_batch_submit(akz_batch *b, const uint8_t *const *images, const size_t *strides)
 {
   AKZ_GUARD(b);
-  if (!counts || !total || capacity < 0) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_batch_detect_describe_packed: bad arguments");
   akz_status st = akz_batch_upload(b, images, strides, 0);
   if (st == AKZ_OK) st = akz_batch_launch(b);
-  if (st == AKZ_OK) st = akz_batch_sync_stats(b);
   if (st != AKZ_OK) return st;
+  CK(cudaMemcpyAsync(b->h_stats, b->d_stats, (size_t)b->nimg * sizeof(akz_image_stats), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaEventRecord(b->ev[8], b->stream));
+  b->submitted = true;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_batch_collect_packed(akz_batch *b, akz_keypoint *kpts, uint8_t *desc, int capacity, int *counts,
+                                            int *total)
+{
+  AKZ_GUARD(b);
+  if (!counts || !total || capacity < 0) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_batch_collect_packed: bad arguments");
+  if (!b->submitted) return akz_fail(AKZ_ERR_STATE, "akz_batch_collect_packed: nothing submitted");
+  b->submitted = false;
+  CK(cudaEventSynchronize(b->ev[8]));
+  for (int i = 0; i < b->nimg; i++) {
+    if (b->h_stats[i].overflow)
+      return akz_fail(AKZ_ERR_OVERFLOW, "image %d: %d raw extrema exceed maxkeypoints=%d", i, b->h_stats[i].nraw, b->opt.maxkeypoints);
+    if (b->h_stats[i].status == AKZ_ERR_TIMEOUT) return akz_fail(AKZ_ERR_TIMEOUT, "image %d: suppression did not settle", i);
+  }
   long long n = 0;
   for (int i = 0; i < b->nimg; i++) {
     counts[i] = b->h_stats[i].nkp;
@@ -1310,7 +1326,7 @@ AKZ_API akz_status akz_batch_detect_describe_packed(akz_batch *b, const uint8_t 
   }
   *total = (int)n;
   if (n > capacity)
-    return akz_fail(AKZ_ERR_OVERFLOW, "akz_batch_detect_describe_packed: %lld keypoints exceed the capacity %d", n, capacity);
+    return akz_fail(AKZ_ERR_OVERFLOW, "akz_batch_collect_packed: %lld keypoints exceed the capacity %d", n, capacity);
   if (n == 0) return AKZ_OK;
   if ((size_t)n > b->cap_pack) {
     if (b->d_pack) cudaFree(b->d_pack);
@@ -1327,6 +1343,17 @@ AKZ_API akz_status akz_batch_detect_describe_packed(akz_batch *b, const uint8_t 
   if (desc) CK(cudaMemcpyAsync(desc, pd, (size_t)n * 61, cudaMemcpyDeviceToHost, b->stream));
   CK(cudaStreamSynchronize(b->stream));
   return AKZ_OK;
+}
+
+AKZ_API akz_status akz_batch_detect_describe_packed(akz_batch *b, const uint8_t *const *images, const size_t *strides,
+                                                    akz_keypoint *kpts, uint8_t *desc, int capacity, int *counts,
+                                                    int *total)
+{
+  AKZ_GUARD(b);
+  if (!counts || !total || capacity < 0) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_batch_detect_describe_packed: bad arguments");
+  const akz_status st = akz_batch_submit(b, images, strides);
+  if (st != AKZ_OK) return st;
+  return akz_batch_collect_packed(b, kpts, desc, capacity, counts, total);
 }
 
 AKZ_API akz_status akz_batch_level_plane(akz_batch *b, int i, int level, int plane, float *out)

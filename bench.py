@@ -62,6 +62,8 @@ def parse():
                     help="surrogate4k: run the net's 32-channel layers on tcgen05 (1) or mma.sync (0)")
     ap.add_argument("--check-tol", type=float, default=2e-3,
                     help="surrogate4k: per-level tolerance of the surrogate against plain FED before it falls back")
+    ap.add_argument("--groups", type=int, default=4,
+                    help="1080p batch: images split into this many native batches on their own streams (BatchGroup)")
     ap.add_argument("--fed-depth", default=None, choices=["auto", "4", "5", "6", "7", "8"],
                     help="FED steps per level-kernel launch; auto times each depth per level on the batch first "
                          "(default: 8 for the 1080p batch, whose HBM traffic was captured at 8; auto for uneven64)")
@@ -310,6 +312,9 @@ def _pick_fed_depth(batch, args, default):
     """FED blocking depth per level: the autotuner's picks (timed on the
     uploaded batch) or the one asked for."""
     depth = args.fed_depth or default
+    if depth == "auto" and hasattr(batch, "parts"):
+        d, ms = batch.autotune()[0]
+        return d, {str(k): round(v, 4) for k, v in ms.items()}
     if depth == "auto":
         d, ms = batch.autotune()
         return d, {str(k): round(v, 4) for k, v in ms.items()}
@@ -511,19 +516,24 @@ def main():
     B, W, H = args.batch, args.width, args.height
     imgs = [synth.synth_image(s, W, H) for s in replicas.rank_seeds(rank, B)]
     opt = akz.AKAZEOptions()
-    batch = akz.Batch(opt, [(W, H)] * B)
-    stream = torch.cuda.Stream()
-    batch.set_stream(stream.cuda_stream)
-    batch.upload(imgs)
-    fed_depth, depth_ms = _pick_fed_depth(batch, args, "8")
-    torch.cuda.synchronize()
     if args.profile_case:
+        batch = akz.Batch(opt, [(W, H)] * B)
+        batch.upload(imgs)
+        _pick_fed_depth(batch, args, "8")
+        torch.cuda.synchronize()
         ms = batch.profile()
         print(json.dumps({"profile_case": f"{B} x {W}x{H}", "stage_ms": [float(x) for x in ms],
                           "keypoints": [int(c) for c in batch.counts()]}))
         return 0
+    batch = akz.BatchGroup(opt, [(W, H)] * B, groups=args.groups)
+    stream = torch.cuda.Stream()
+    gstreams = [torch.cuda.Stream() for _ in batch.parts]
+    batch.set_streams([g.cuda_stream for g in gstreams])
+    batch.upload(imgs)
+    fed_depth, depth_ms = _pick_fed_depth(batch, args, "8")
+    torch.cuda.synchronize()
 
-    # device-resident throughput
+    # device-resident throughput: every group stream starts after e0, e1 after all of them
     for _ in range(max(args.warmup, 3)):
         batch.run()
     counts = batch.counts()
@@ -537,8 +547,12 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(stream)
+    for g in gstreams:
+        g.wait_event(e0)
     for _ in range(args.steps):
         batch.run()
+    for g in gstreams:
+        stream.wait_stream(g)
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop() if sampler else None
@@ -546,12 +560,13 @@ def main():
     value = replicas.job_throughput(B * args.steps, ws, ms_max / 1000.0)
 
     # stage profile (one non-graph run) for the roofline of the level stage
-    stage = [float(x) for x in batch.profile()]
+    stages = [[float(x) for x in b.profile()] for b in batch.parts]
+    stage = [sum(st[k] for st in stages) for k in range(7)]
     fed_ms = stage[2]
     fed_bytes = fed_algorithmic_bytes(W, H) * B
     pk, pk_kind = peaks()
     achieved = fed_bytes / (fed_ms / 1000.0) / 1e9
-    n_launch = batch.kernel_count()
+    n_launch = sum(b.kernel_count() for b in batch.parts)
 
     # end to end through the C ABI: pinned host u8 in, host results out
     pin_in = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(B)]
@@ -588,6 +603,7 @@ def main():
         "config": {"workload": f"plain A-KAZE detect+MLDB, {W}x{H} u8, 4 octaves x 4 sublevels, default options",
                    "fed": "plain (the learned surrogate is built but 2.6x slower at 4K on this GPU: --workload surrogate4k)",
                    "images_per_step_per_gpu": B, "parallelism": f"replicas x{ws}",
+                   "groups": f"{len(batch.parts)} native batches of {B // len(batch.parts)} images, one stream and graph each",
                    "l2": "inputs and working set larger than L2 (~%.1f GB per step)" % (B * image_algorithmic_bytes(W, H, 0) / 1e9),
                    "keypoints_per_image": nkp,
                    "fed_depth_per_level": fed_depth, "level_stage_ms_by_depth": depth_ms},

@@ -296,6 +296,18 @@ AKZ_API akz_status akz_batch_autotune(akz_batch *b, float *ms_per_depth, int cap
 /* Sets the FED blocking depth (4..8; 8 at creation) without timing. */
 AKZ_API akz_status akz_batch_set_fed_depth(akz_batch *b, int depth);
 
+/* The two halves of akz_batch_detect_describe_packed, for overlapping
+ * several batches (each on its own stream) from one host thread:
+ * akz_batch_submit enqueues the upload of the host images, the batch's
+ * graph and the read-back of the per-image counts, and returns at once;
+ * akz_batch_collect_packed waits for that batch only, then packs and copies
+ * its keypoints and descriptors as akz_batch_detect_describe_packed does.
+ * A collect without a submit is AKZ_ERR_STATE; the host images must stay
+ * unchanged until the collect returns. */
+AKZ_API akz_status akz_batch_submit(akz_batch *b, const uint8_t *const *images, const size_t *strides);
+AKZ_API akz_status akz_batch_collect_packed(akz_batch *b, akz_keypoint *kpts, uint8_t *desc, int capacity, int *counts,
+                                            int *total);
+
 /* akz_batch_detect_describe with packed host output: kpts (capacity
  * records) and desc (capacity x 61 bytes) receive every image's keypoints
  * and descriptors back to back, image i starting at row sum_{j<i} counts[j];

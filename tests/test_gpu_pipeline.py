@@ -163,3 +163,34 @@ def test_fed_blocking_depths_give_identical_results(gpu_lib):
     assert all(b.results(i)[0].tobytes() == want[i][0].tobytes() for i in range(len(sizes)))
     with pytest.raises(gpu_lib.AkazeError):
         b.set_fed_depth(3)
+
+
+def test_batch_group_equals_one_batch(gpu_lib):
+    """Groups on their own streams (overlapping on the GPU, packed output
+    from one host thread per group) give the single batch's results."""
+    sizes = synth.uneven_sizes(13, 7)
+    imgs = [synth.synth_image(1300 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    one = gpu_lib.Batch(gpu_lib.AKAZEOptions(), sizes)
+    one.upload(imgs)
+    one.run()
+    want = [one.results(i) for i in range(len(sizes))]
+    grp = gpu_lib.BatchGroup(gpu_lib.AKAZEOptions(), sizes, groups=3)
+    assert [len(b.sizes) for b in grp.parts] == [2, 2, 3]
+    grp.upload(imgs)
+    grp.run()
+    grp.run()
+    assert list(grp.counts()) == [len(k) for k, _ in want]
+    for i, (k, d) in enumerate(want):
+        kk, dd = grp.results(i)
+        assert kk.tobytes() == k.tobytes() and np.array_equal(dd, d), i
+    total = sum(len(k) for k, _ in want)
+    kp = np.zeros(total + 300, gpu_lib.KEYPOINT_DTYPE)
+    d = np.zeros((total + 300, 61), np.uint8)
+    counts = grp.detect_describe_packed(imgs, kp, d)
+    assert list(counts) == [len(k) for k, _ in want]
+    off = 0
+    for k, dd in want:
+        assert kp[off:off + len(k)].tobytes() == k.tobytes() and np.array_equal(d[off:off + len(k)], dd)
+        off += len(k)
+    with pytest.raises(gpu_lib.AkazeError):  # nothing submitted
+        grp.parts[0].collect_packed(kp, d)
