@@ -8,6 +8,8 @@
  * pipeline follow src/lib/nldiffusion_functions.cpp.  Nothing here falls
  * back to CPU computation: every stage of the path runs as a kernel.
  */
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -15,6 +17,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -283,6 +286,7 @@ struct akz_batch {
   char *arena = nullptr;
   size_t arena_bytes = 0;
   float *planes = nullptr;
+  void *d_tmaps = nullptr; /* k_fed input boxes: 2 CUtensorMaps per level descriptor */
   uint8_t *u8 = nullptr;
   float *f32 = nullptr;
   size_t staging_elems = 0;
@@ -341,7 +345,8 @@ static void akz_batch_free(akz_batch *b)
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->arena) cudaFree(b->arena);
-  for (void *q : {(void *)b->d_sg_w, b->d_sg_scratch, (void *)b->d_sg_b, (void *)b->d_sg_chk, (void *)b->d_sg_err, b->d_pack})
+  for (void *q : {(void *)b->d_sg_w, b->d_sg_scratch, (void *)b->d_sg_b, (void *)b->d_sg_chk, (void *)b->d_sg_err, b->d_pack,
+                  b->d_tmaps})
     if (q) cudaFree(q);
   if (b->f32) cudaFree(b->f32);
   if (b->h_stats) cudaFreeHost(b->h_stats);
@@ -349,6 +354,53 @@ static void akz_batch_free(akz_batch *b)
     if (e) cudaEventDestroy(e);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
+}
+
+/* The TMA descriptors of k_fed's input boxes: for every level descriptor,
+ * its Lt plane and its image's T2 plane at the level's size and pitch, each
+ * read in boxes of AKZ_FED_BOX_W x AKZ_FED_BOX_H floats with zero fill
+ * outside the plane (the kernel replaces it by the replicate border).  The
+ * encoder is the driver's cuTensorMapEncodeTiled, reached through the
+ * runtime's entry-point query (no link against the driver library). */
+static PFN_cuTensorMapEncodeTiled_v12000 akz_tmap_encoder()
+{
+  static std::mutex mu;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!fn) {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+  }
+  return fn;
+}
+
+static akz_status akz_build_tensor_maps(akz_batch *b)
+{
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = akz_tmap_encoder();
+  if (!enc) return akz_fail(AKZ_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const size_t nl = b->lv.size();
+  std::vector<CUtensorMap> maps(2 * nl);
+  for (size_t l = 0; l < nl; l++) {
+    const akz_level_desc &L = b->lv[l];
+    const akz_image_desc &I = b->im[L.image];
+    const cuuint64_t dims[2] = {(cuuint64_t)L.width, (cuuint64_t)L.height};
+    const cuuint64_t strides[1] = {(cuuint64_t)L.pitch * sizeof(float)};
+    const cuuint32_t box[2] = {AKZ_FED_BOX_W, AKZ_FED_BOX_H}, estr[2] = {1, 1};
+    float *bases[2] = {b->planes + L.lt, b->planes + I.t2};
+    for (int k = 0; k < 2; k++) {
+      const CUresult r = enc(&maps[2 * l + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, bases[k], dims, strides, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return akz_fail(AKZ_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for level %zu", (int)r, l);
+    }
+  }
+  static_assert(sizeof(CUtensorMap) == 128, "k_fed indexes tensor maps at a 128-byte stride");
+  CK(cudaMalloc(&b->d_tmaps, maps.size() * sizeof(CUtensorMap)));
+  CK(cudaMemcpy(b->d_tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+  return AKZ_OK;
 }
 
 static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, const int *Hs, akz_batch **out)
@@ -528,8 +580,8 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
         const int steps = (nsteps - done + (nch - c) - 1) / (nch - c);
         akz_fed_launch fl;
         memset(&fl, 0, sizeof(fl));
-        fl.tw = 128 - 2 * steps; /* k_fed region is 128 x 40 = tile +- steps */
-        fl.th = 40 - 2 * steps;
+        fl.tw = akz_fed_tile_w(steps); /* k_fed region is 128 x 40 = tile +- steps (aligned) */
+        fl.th = akz_fed_tile_h(steps);
         fl.seg_off = (int)b->segs.size();
         for (int i = 0; i < n; i++) {
           if (b->im[i].nlev <= l) continue;
@@ -571,8 +623,8 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
      * and the start image in Lt */
     akz_fed_launch pl;
     memset(&pl, 0, sizeof(pl));
-    pl.tw = 128;
-    pl.th = 40;
+    pl.tw = akz_fed_tile_w(0);
+    pl.th = akz_fed_tile_h(0);
     pl.seg_off = (int)b->segs.size();
     for (int i = 0; i < n; i++) {
       if (b->im[i].nlev <= l) continue;
@@ -692,6 +744,13 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
     akz_batch_free(b);
     return akz_fail_cuda(e, "batch set-up", __FILE__, __LINE__);
   }
+  if (e == cudaSuccess) {
+    const akz_status ts = akz_build_tensor_maps(b);
+    if (ts != AKZ_OK) {
+      akz_batch_free(b);
+      return ts;
+    }
+  }
   b->stream = b->own_stream;
   *out = b;
   return AKZ_OK;
@@ -767,6 +826,7 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe 
       p.segs = b->d_segs + fl.seg_off;
       p.nsegs = fl.nsegs;
       p.kc = b->d_kc;
+      p.tmaps = b->d_tmaps;
       p.chk = b->d_sg_chk;
       p.gate = gate;
       p.gate_tol = b->sg_tol;

@@ -58,8 +58,24 @@ struct akz_gauss_params {
   float taps[AKZ_MAX_TAPS];
 };
 
+/* k_fed geometry: a 128 x 40 region R0 = tile +- d per CTA (d = FED steps of
+ * the launch).  The region's left edge tx0 - d - delta sits on a multiple of
+ * 4 columns (delta = (-d) mod 4, tile origins are multiples of 4), so every
+ * column pair is 8-byte aligned in shared and global memory and the TMA box
+ * of the input (x = region - 4) starts on a 16-byte boundary; the tile
+ * width is what remains, rounded down to a multiple of 4. */
+static inline __host__ __device__ int akz_fed_delta(int d) { return (4 - (d & 3)) & 3; }
+static inline __host__ __device__ int akz_fed_tile_w(int d) { return (128 - 2 * d - akz_fed_delta(d)) & ~3; }
+static inline __host__ __device__ int akz_fed_tile_h(int d) { return 40 - 2 * d; }
+#define AKZ_FED_BOX_W 136 /* input box: region +- 4 columns */
+#define AKZ_FED_BOX_H 46  /* region +- 3 rows */
+
 struct akz_fed_params {
   akz_tables t;
+  /* two 128-byte CUtensorMaps per level descriptor l: [2l] the level's Lt
+   * plane, [2l + 1] its image's T2 plane at the level's size; boxes of
+   * AKZ_FED_BOX_W x AKZ_FED_BOX_H floats */
+  const void *tmaps;
   const akz_tile_seg *segs;
   int nsegs;
   const float2 *kc;   /* per image x 16 octaves: (k, 1/k^2) */

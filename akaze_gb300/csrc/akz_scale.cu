@@ -406,31 +406,38 @@ __global__ void __launch_bounds__(256) k_gauss0(akz_gauss_params p)
 /* FED level kernel.
  *
  * Every CTA owns a fixed 128 x 40 region R0 = tile +- d (d = FED steps of the
- * launch, tile (128-2d) x (40-2d)), so one thread geometry serves every
- * chunk size: 512 threads, 2 column groups of 32 lanes x 2 columns, 8 bands
- * of 5 rows; each thread keeps the level values of its two columns in
- * registers together with the conductance pair sums (c_x + c_x+1) and
- * (c_y + c_y+1) of the reference's flux terms, which do not change across
- * steps.  A step reads the outer east/west neighbours (and the band's outer
- * rows) from a double-buffered shared plane and writes its two values with
- * one 64-bit store: 1.5 shared-memory operations, 3 products and 3.5 packed
- * FP32x2 additions per pixel-step, one barrier per step.  Pixels outside
+ * launch; the region's left edge is rounded down to a multiple of 4 columns,
+ * akz_fed_tile_w), so one thread geometry serves every chunk size: 512
+ * threads, 2 column groups of 32 lanes x 2 columns, 8 bands of 5 rows; each
+ * thread keeps the level values of its two columns in registers together
+ * with the conductance pair sums (c_x + c_x+1) and (c_y + c_y+1) of the
+ * reference's flux terms, which do not change across steps.  A step reads
+ * the outer east/west neighbours (and the band's outer rows) from a
+ * double-buffered shared plane and writes its two values with one 64-bit
+ * store: 1.5 shared-memory operations, 3 products and 3.5 packed FP32x2
+ * additions per pixel-step, one barrier per step.  Pixels outside
  * tile +- (d - s) after step s are not needed and may hold anything; image
  * borders are replicate (clamped) neighbours, whose flux is exactly zero, as
  * in the reference's border formulas (nldiffusion_functions.cpp:241-307).
+ * Column pairs start at even image columns everywhere, so global loads and
+ * stores of a pair are single 64-bit accesses.
  */
 #define AKZ_FED_RW 128
 #define AKZ_FED_RH 40
 #define AKZ_FED_RB 5
 #define AKZ_FED_THREADS 512
+#define AKZ_FED_PS (AKZ_FED_RW + 8) /* input plane: columns R0 - 4 .. R0 + 131 */
+#define AKZ_FED_SS (AKZ_FED_RW + 4) /* Gaussian planes: columns R0 - 2 .. R0 + 129 */
+#define AKZ_FED_TMA_SPIN (1 << 22)  /* bounded wait for the input box */
+static_assert(AKZ_FED_PS == AKZ_FED_BOX_W && AKZ_FED_RH + 6 == AKZ_FED_BOX_H, "k_fed input box");
 
 size_t akz_fed_smem_bytes(int, int, int, int first)
 {
-  if (!first) return 2 * AKZ_FED_RW * AKZ_FED_RH * sizeof(float);
-  const size_t P = (size_t)(AKZ_FED_RH + 6) * (AKZ_FED_RW + 6);
-  const size_t T = (size_t)(AKZ_FED_RH + 6) * (AKZ_FED_RW + 2);
-  const size_t S = (size_t)(AKZ_FED_RH + 2) * (AKZ_FED_RW + 2);
-  return (P + T + S) * sizeof(float);
+  if (!first) return 2 * AKZ_FED_RW * AKZ_FED_RH * sizeof(float) + 128; /* the kernel aligns its base to 128 bytes */
+  const size_t P = (size_t)(AKZ_FED_RH + 6) * AKZ_FED_PS;
+  const size_t T = (size_t)(AKZ_FED_RH + 6) * AKZ_FED_SS;
+  const size_t S = (size_t)(AKZ_FED_RH + 2) * AKZ_FED_SS;
+  return (P + T + S) * sizeof(float) + 128 + 16; /* 128-byte alignment of the TMA box, the mbarrier */
 }
 
 /* Conductance of |grad|^2 = m (AKAZE.cpp:259-268 with pm_g1, pm_g2,
@@ -483,84 +490,129 @@ __device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
   return make_float2(out[0], out[1]);
 }
 
-/* First-chunk prologue of k_fed: the level's starting image on R0 +- 3, its
- * sigma-1 smoothing Lsmooth (written to HBM for the tile) and the conductance
- * on R0 (written to HBM for the tile when more chunks follow).
+/* First-chunk prologue of k_fed: the level's starting image on R0 +- 3 rows
+ * and R0 +- 4 columns, its sigma-1 smoothing Lsmooth (written to HBM for the
+ * tile) and the conductance on R0 (written to HBM for the tile when more
+ * chunks follow).
  *
- * Every tile runs the same straight-line code.  The input region is read
- * with replicate (clamped) coordinates, which makes the Gaussian's replicate
- * border (gaussian_2D_convolution, nldiffusion_functions.cpp:29-47) exact for
- * every pixel inside the image; Lsmooth's row and column just outside the
- * image are then replaced by their reflect-101 mirrors (x = -1 by x = 1,
- * x = W by x = W - 2), the border of the Scharr gradient
- * (nldiffusion_functions.cpp:50-53).  Values outside the image are finite
- * and unused: their conductance pair sums are zero.
+ * The input is the predecessor level (SRCK 0) or the INTER_AREA plane
+ * prepared in T2 (SRCK 2), fetched as one TMA box; or the exact 2x
+ * half-sample of the predecessor (SRCK 1), formed by the threads.  Rows and
+ * columns outside the image take the nearest image row and column
+ * (replicate), which makes the Gaussian's replicate border
+ * (gaussian_2D_convolution, nldiffusion_functions.cpp:29-47) exact for every
+ * pixel inside the image; Lsmooth's row and column just outside the image
+ * are then replaced by their reflect-101 mirrors (x = -1 by x = 1, x = W by
+ * x = W - 2), the border of the Scharr gradient (nldiffusion_functions.cpp:
+ * 50-53).  Values outside the image are finite and unused: their
+ * conductance pair sums are zero.
  *
- * Leaves the level values of R0 in sP (stride RW + 6, R0 at row 3, column 3)
- * and the conductance in sT (stride RW).  Filter passes work on column pairs with packed FP32x2 additions
- * and scalar products, in the reference's operation order:
+ * Leaves the level values of R0 in sP (stride AKZ_FED_PS, R0 at row 3,
+ * column 4) and the conductance in sT (stride RW).  Filter passes work on
+ * column pairs with packed FP32x2 additions and scalar products, in the
+ * reference's operation order:
  *   Gaussian  k0*(v[-2] + v[+2]) + k1*(v[-1] + v[+1]) + k2*v[0], rows then columns;
  *   Scharr    gx = 3*(d[y-1] + d[y+1]) + 10*d[y],  d = v[x+1] - v[x-1],
- *             gy = s[y+1] - s[y-1],  s = 3*(v[x-1] + v[x+1]) + 10*v[x]. */
+ *             gy = s[y+1] - s[y-1],  s = 3*(v[x-1] + v[x+1]) + 10*v[x].
+ * Returns false when the input box did not arrive within the bounded wait
+ * (the image's status is then AKZ_ERR_TIMEOUT). */
 template <int SRCK>
-__device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const akz_level_desc &L,
+__device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const akz_level_desc &L,
                                                  const akz_image_desc &I, int level_desc, float *sm, int ox, int oy,
                                                  int tx0, int ty0, int tx1, int ty1, int lx0, int ly0)
 {
   constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB, NT = AKZ_FED_THREADS;
-  constexpr int PS = RW + 6, SS = RW + 2, PH = RH + 6, SH = RH + 2;
+  constexpr int PS = AKZ_FED_PS, SS = AKZ_FED_SS, PH = RH + 6, SH = RH + 2;
   constexpr int NP = SS / 2;          /* column pairs of the smoothing regions */
   constexpr int VR = 6, VG = SH / VR; /* rows per thread and row groups of the vertical pass */
-  static_assert(SH % VR == 0 && NP * VG <= NT && (RW * RH) % NT == 0, "k_fed prologue geometry");
+  static_assert(SH % VR == 0 && NP * VG <= NT && NP == 66 && NT == 512, "k_fed prologue geometry");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int W = L.width, H = L.height;
   float *sP = sm, *sT = sm + PH * PS, *sS = sT + PH * SS;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(sS + SH * SS);
   const float *planes = p.t.planes;
 
-  /* 1. starting image on R0 +- 3: predecessor copy, its exact 2x
-   *    half-sample, or the INTER_AREA plane prepared in T2 */
-  {
-    const float *pp;
-    long long pitch;
-    if (SRCK == 2) {
-      pp = planes + I.t2;
-      pitch = L.pitch;
-    } else {
-      const akz_level_desc Lp = p.t.lv[level_desc - 1];
-      pp = planes + Lp.lt;
-      pitch = Lp.pitch;
-    }
+  /* 1. starting image on columns ox - 4 .. ox + 131, rows oy - 3 .. oy + 42 */
+  if (SRCK == 1) {
+    const akz_level_desc Lp = p.t.lv[level_desc - 1];
+    const float *pp = planes + Lp.lt;
+    const long long pitch = Lp.pitch;
 #pragma unroll
     for (int k = 0; k < (PH + 15) / 16; k++) {
       const int ly = warp + 16 * k;
       if (ly < PH) {
         const int y = akz_clampi(oy - 3 + ly, 0, H - 1);
-        const float *q0 = pp + (long long)(SRCK == 1 ? 2 * y : y) * pitch;
+        const float *q0 = pp + (long long)(2 * y) * pitch;
 #pragma unroll
         for (int j = 0; j < (PS + 31) / 32; j++) {
           const int l = lane + 32 * j;
           if (l < PS) {
-            const int x = akz_clampi(ox - 3 + l, 0, W - 1);
-            float v;
-            if (SRCK == 1) {
-              const float2 a = __ldg((const float2 *)(q0 + 2 * x)), b = __ldg((const float2 *)(q0 + pitch + 2 * x));
-              v = 0.25f * (((a.x + a.y) + b.x) + b.y);
-            } else {
-              v = __ldg(q0 + x);
-            }
-            sP[ly * PS + l] = v;
+            const int x = akz_clampi(ox - 4 + l, 0, W - 1);
+            const float2 a = __ldg((const float2 *)(q0 + 2 * x)), b = __ldg((const float2 *)(q0 + pitch + 2 * x));
+            sP[ly * PS + l] = 0.25f * (((a.x + a.y) + b.x) + b.y);
           }
         }
       }
     }
+    __syncthreads();
+  } else {
+    /* one TMA box; out-of-image parts arrive as zeros and are replaced below */
+    const char *tmap = (const char *)p.tmaps + 128 * (SRCK == 2 ? 2 * level_desc + 1 : 2 * (level_desc - 1));
+    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar);
+    if (tid == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+      asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    __syncthreads();
+    if (tid == 0) {
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sP);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(PH * PS * 4) : "memory");
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+              "r"(dst), "l"(tmap), "r"(ox - 4), "r"(oy - 3), "r"(mb)
+          : "memory");
+    }
+    uint32_t done = 0;
+    for (int it = 0; it < AKZ_FED_TMA_SPIN && !done; it++)
+      asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
+                   : "=r"(done)
+                   : "r"(mb)
+                   : "memory");
+    if (__syncthreads_or(!done)) { /* (CTA-uniform) record it, give the copy one more bounded wait, and leave */
+      if (tid == 0) atomicExch(&p.t.stats[L.image].status, (int)AKZ_ERR_TIMEOUT);
+      for (int it = 0; it < AKZ_FED_TMA_SPIN && !done; it++)
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done)
+                     : "r"(mb)
+                     : "memory");
+      return false;
+    }
+    /* replicate border: columns first (each row from its own clamped
+     * column), then whole rows; the box always contains column and row 0
+     * or W-1 / H-1 where it crosses the image edge */
+    if (ox - 4 < 0 || ox + 132 > W || oy - 3 < 0 || oy + 43 > H) {
+      if (ox - 4 < 0 || ox + 132 > W) {
+        for (int i = tid; i < PH * PS; i += NT) {
+          const int r = i / PS, c = i - r * PS, x = ox - 4 + c, xc = akz_clampi(x, 0, W - 1);
+          if (xc != x) sP[i] = sP[r * PS + (xc - (ox - 4))];
+        }
+        __syncthreads();
+      }
+      if (oy - 3 < 0 || oy + 43 > H) {
+        for (int i = tid; i < PH * PS; i += NT) {
+          const int r = i / PS, c = i - r * PS, y = oy - 3 + r, yc = akz_clampi(y, 0, H - 1);
+          if (yc != y) sP[i] = sP[(yc - (oy - 3)) * PS + c];
+        }
+        __syncthreads();
+      }
+    }
   }
-  __syncthreads();
 
-  /* 2. rows of the Gaussian on columns R0 +- 1 (sT column c is x = ox - 1 + c):
-   *    column pairs 0..63 by (tid & 63) on rows (tid >> 6) + 8k, pair 64
-   *    by the first PH threads */
+  /* 2. rows of the Gaussian on columns R0 - 2 .. R0 + 129 (sT column c is
+   *    x = ox - 2 + c, its taps sP c .. c + 4): column pairs 0..63 by
+   *    (tid & 63) on rows (tid >> 6) + 8k, pairs 64 and 65 by the first
+   *    2 PH threads */
   const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
-  static_assert(NP == 65 && NT == 512, "k_fed row-pass mapping");
   auto hrow = [&](int row, int c) {
     const float *r = sP + row * PS + c;
     const float2 A = ld2(r), B = ld2(r + 2), C = ld2(r + 4);
@@ -576,19 +628,19 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
 #pragma unroll
     for (int k = 0; k < (PH + 7) / 8; k++)
       if (r0 + 8 * k < PH) hrow(r0 + 8 * k, c);
-    if (tid < PH) hrow(tid, 2 * 64);
+    if (tid < 2 * PH) hrow(tid >> 1, 2 * (64 + (tid & 1)));
   }
   __syncthreads();
 
-  /* 3. columns of the Gaussian: Lsmooth on R0 +- 1 (sS row n is y = oy - 1 + n) */
+  /* 3. columns of the Gaussian: Lsmooth on rows R0 +- 1 (sS row n is y = oy - 1 + n) */
   if (tid < NP * VG) {
     const int g = tid / NP, c = 2 * (tid - g * NP);
     const float *col = sT + (g * VR) * SS + c;
     float2 v[VR + 4];
 #pragma unroll
     for (int j = 0; j < VR + 4; j++) v[j] = ld2(col + j * SS);
-    const int x = ox - 1 + c;
-    const bool w0 = x >= tx0 && x < tx1, w1 = x + 1 >= tx0 && x + 1 < tx1;
+    const int x = ox - 2 + c; /* even */
+    const bool w0 = x >= tx0 && x < tx1, w1 = x + 1 < tx1;
     float *lsp = p.t.planes + L.ls + x;
 #pragma unroll
     for (int j = 0; j < VR; j++) {
@@ -600,10 +652,12 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
       const int n = g * VR + j;
       st2(sS + n * SS + c, acc);
       const int y = oy - 1 + n;
-      if (y >= ty0 && y < ty1) {
+      if (w0 && y >= ty0 && y < ty1) {
         float *o = lsp + (long long)y * L.pitch;
-        if (w0) o[0] = acc.x;
-        if (w1) o[1] = acc.y;
+        if (w1)
+          st2(o, acc);
+        else
+          o[0] = acc.x;
       }
     }
   }
@@ -611,8 +665,8 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
 
   /* 4. the reflect-101 border of Lsmooth: columns first, then whole rows
    *    (which fixes the corners) */
-  const int cm = -ox, cp = W - ox + 1; /* sS columns of x = -1 and x = W */
-  const int nm = -oy, np = H - oy + 1; /* sS rows of y = -1 and y = H */
+  const int cm = 1 - ox, cp = W - ox + 2; /* sS columns of x = -1 and x = W */
+  const int nm = -oy, np = H - oy + 1;    /* sS rows of y = -1 and y = H */
   if (cm >= 0 || cp < SS) {
     if (tid < SH) {
       float *row = sS + tid * SS;
@@ -630,22 +684,23 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
   }
 
   /* 5. Scharr gradient of Lsmooth and the conductance on R0, in this
-   *    thread's k_fed geometry: columns lx0, lx0+1, rows ly0 .. ly0+RB-1;
-   *    the conductance goes to sT (free since pass 3), the level values
-   *    stay in sP */
+   *    thread's k_fed geometry: columns lx0, lx0+1 (x0 = ox + lx0, sS
+   *    column lx0 + 2), rows ly0 .. ly0+RB-1; the conductance goes to sT
+   *    (free since pass 3), the level values stay in sP */
   float *sG = sT;
   const float inv_k = p.kc[L.image * 16 + L.octave].y;
   float2 dh[RB + 2], sh[RB + 2];
 #pragma unroll
   for (int j = 0; j < RB + 2; j++) {
-    const float *row = sS + (ly0 + j) * SS + lx0; /* x0 - 1 .. x0 + 2 */
-    const float2 P = ld2(row), Q = ld2(row + 2);
+    const float *row = sS + (ly0 + j) * SS + lx0; /* x0 - 2 .. x0 + 3 */
+    const float2 A = ld2(row), B = ld2(row + 2), C = ld2(row + 4);
+    const float2 P = make_float2(A.y, B.x), Q = make_float2(B.y, C.x); /* (x0-1, x0), (x0+1, x0+2) */
     dh[j] = f2sub(Q, P);
     const float2 t = f2add(P, Q);
     sh[j] = f2add(make_float2(3.0f * t.x, 3.0f * t.y), make_float2(10.0f * P.y, 10.0f * Q.x));
   }
-  const int x0 = ox + lx0;
-  const bool w0 = p.write_g && x0 >= tx0 && x0 < tx1, w1 = p.write_g && x0 + 1 >= tx0 && x0 + 1 < tx1;
+  const int x0 = ox + lx0; /* even */
+  const bool w0 = p.write_g && x0 >= tx0 && x0 < tx1, w1 = x0 + 1 < tx1;
   float *gp = p.t.planes + I.g + x0;
 #pragma unroll
   for (int r = 0; r < RB; r++) {
@@ -658,19 +713,21 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
                                                        akz_conductance_m(m.y, inv_k, p.diffusivity));
     st2(sG + (ly0 + r) * RW + lx0, gv);
     const int y = oy + ly0 + r;
-    if (y >= ty0 && y < ty1) {
+    if (w0 && y >= ty0 && y < ty1) {
       float *o = gp + (long long)y * L.pitch;
-      if (w0) o[0] = gv.x;
-      if (w1) o[1] = gv.y;
+      if (w1)
+        st2(o, gv);
+      else
+        o[0] = gv.x;
     }
   }
   __syncthreads();
+  return true;
 }
 
 /* Registers of one k_fed thread (columns x0, x0+1 of R0, RB rows) from the
- * level values (sL, row stride LS, at R0's origin) and the conductance on R0
- * (sG, row stride RW) in shared memory (PAIRS: sL's column pairs are 8-byte
- * aligned):
+ * level values (sL, row stride LS, at R0's origin, pairs 8-byte aligned) and
+ * the conductance on R0 (sG, row stride RW) in shared memory:
  *   Lp[r]   the two level values;
  *   gw[r]   c(x0-1) + c(x0)   the west flux pair of column x0;
  *   gm[r]   c(x0) + c(x0+1)   the flux pair between the two columns;
@@ -680,7 +737,7 @@ __device__ __forceinline__ void akz_fed_prologue(const akz_fed_params &p, const 
  * flux term (nldiffusion_functions.cpp:241-307), and zero times any finite
  * difference adds nothing.  INTERIOR: R0 +- 1 lies inside the image, so no
  * pair crosses the border. */
-template <bool INTERIOR, int LS, bool PAIRS>
+template <bool INTERIOR, int LS>
 __device__ __forceinline__ void akz_fed_gather_smem(const float *sL, const float *sG, int lx0, int ly0, int x0, int ytop,
                                                     int W, int H, float2 *Lp, float *gw, float *gm, float *ge,
                                                     float2 *gs, float2 &gn0)
@@ -693,8 +750,7 @@ __device__ __forceinline__ void akz_fed_gather_smem(const float *sL, const float
 #pragma unroll
   for (int r = 0; r < RB; r++) {
     const int ly = ly0 + r;
-    const float *lr = sL + ly * LS + lx0;
-    Lp[r] = PAIRS ? ld2(lr) : make_float2(lr[0], lr[1]);
+    Lp[r] = ld2(sL + ly * LS + lx0);
     const float cw = sG[ly * RW + lxw], ce = sG[ly * RW + lxe];
     const float2 cc = c[r + 1], cs = c[r + 2];
     if (INTERIOR) {
@@ -728,9 +784,9 @@ __device__ __forceinline__ void akz_fed_gather_smem(const float *sL, const float
  * reference's xneg at x+1 is (c(x) + c(x+1)) * (L(x+1) - L(x)), the same
  * operands in the same order as xpos at x, and likewise yneg at y+1 and ypos
  * at y.  Additions run as packed FP32x2 pairs of the two columns; products
- * stay scalar.  cur: level values (row stride CS, at R0's origin; PAIRS: its
- * column pairs are 8-byte aligned); nxt: the new values (row stride RW). */
-template <int CS, bool PAIRS>
+ * stay scalar.  cur: level values (row stride CS, at R0's origin, pairs
+ * 8-byte aligned); nxt: the new values (row stride RW). */
+template <int CS>
 __device__ __forceinline__ void akz_fed_step(const float *cur, float *nxt, float h, int lx0, int ly0, float2 *Lp,
                                              const float *gw, const float *gm, const float *ge, const float2 *gs,
                                              float2 gn0)
@@ -738,9 +794,7 @@ __device__ __forceinline__ void akz_fed_step(const float *cur, float *nxt, float
   constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
   const int lyn = max(ly0 - 1, 0), lys = min(ly0 + RB, RH - 1);
   const int lxw = max(lx0 - 1, 0), lxe = min(lx0 + 2, RW - 1);
-  const float *an = cur + lyn * CS + lx0, *bs = cur + lys * CS + lx0;
-  const float2 above = PAIRS ? ld2(an) : make_float2(an[0], an[1]);
-  const float2 below = PAIRS ? ld2(bs) : make_float2(bs[0], bs[1]);
+  const float2 above = ld2(cur + lyn * CS + lx0), below = ld2(cur + lys * CS + lx0);
   const float2 dn = f2sub(Lp[0], above);
   float2 Fn = make_float2(gn0.x * dn.x, gn0.y * dn.y);
 #pragma unroll
@@ -764,10 +818,11 @@ __device__ __forceinline__ void akz_fed_step(const float *cur, float *nxt, float
 
 __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
 {
-  extern __shared__ float sm[];
-  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
-  constexpr int PS = RW + 6, SS = RW + 2; /* strides of the input and smoothing regions */
+  extern __shared__ __align__(128) float sm_raw[];
+  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB, PS = AKZ_FED_PS;
   if (p.gate && *p.gate <= p.gate_tol) return; /* a gated fallback that is not needed */
+  /* the TMA box wants a 128-byte aligned destination */
+  float *sm = sm_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(sm_raw) & 127u)) & 127u) / 4;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
   const akz_tile_seg sg = p.segs[si];
@@ -775,18 +830,18 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   const akz_image_desc I = p.t.im[L.image];
   const int W = L.width, H = L.height;
   const int d = p.steps;
-  const int TW = RW - 2 * d, TH = RH - 2 * d;
+  const int TW = akz_fed_tile_w(d), TH = akz_fed_tile_h(d);
   const int lt = blockIdx.x - sg.tile_begin;
   const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
   const int tx1 = min(tx0 + TW, W), ty1 = min(ty0 + TH, H);
-  const int ox = tx0 - d, oy = ty0 - d; /* R0 origin (may lie outside the image) */
+  const int ox = tx0 - d - akz_fed_delta(d), oy = ty0 - d; /* R0 origin (a multiple of 4; may lie outside the image) */
   const int srck = p.first ? sg.aux : p.src;
   float *planes = p.t.planes;
 
   /* this thread: columns lx0, lx0+1 of R0, rows ly0 .. ly0+RB-1 */
   const int lx0 = 2 * ((warp & 1) * 32 + lane);
   const int ly0 = (warp >> 1) * RB;
-  const int x0 = ox + lx0;
+  const int x0 = ox + lx0; /* even */
   const int ytop = oy + ly0;
 
   float2 Lp[RB], gs[RB], gn0;
@@ -794,21 +849,23 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   float *cur, *nxt;
 
   if (p.first) {
-    float *sP = sm, *sT = sm + (RH + 6) * PS, *sS = sT + (RH + 6) * SS;
+    float *sP = sm, *sT = sm + (RH + 6) * PS, *sS = sT + (RH + 6) * AKZ_FED_SS;
+    bool ok;
     if (srck == 1)
-      akz_fed_prologue<1>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
+      ok = akz_fed_prologue<1>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
     else if (srck == 0)
-      akz_fed_prologue<0>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
+      ok = akz_fed_prologue<0>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
     else
-      akz_fed_prologue<2>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
-    const float *sL = sP + 3 * PS + 3; /* level values of R0 */
+      ok = akz_fed_prologue<2>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
+    if (!ok) return; /* uniform: every thread saw the same barrier state */
+    const float *sL = sP + 3 * PS + 4; /* level values of R0 */
     const bool interior = ox >= 1 && oy >= 1 && ox + RW + 1 <= W && oy + RH + 1 <= H;
     if (interior)
-      akz_fed_gather_smem<true, PS, false>(sL, sT, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
+      akz_fed_gather_smem<true, PS>(sL, sT, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
     else
-      akz_fed_gather_smem<false, PS, false>(sL, sT, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
+      akz_fed_gather_smem<false, PS>(sL, sT, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
     if (d > 0) { /* the first step reads the level values where the prologue left them */
-      akz_fed_step<PS, false>(sL, sS, p.h[0], lx0, ly0, Lp, gw, gm, ge, gs, gn0);
+      akz_fed_step<PS>(sL, sS, p.h[0], lx0, ly0, Lp, gw, gm, ge, gs, gn0);
       __syncthreads();
     }
     cur = sS;
@@ -819,7 +876,7 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
     const float *lp = planes + (p.src == 1 ? I.t1 : I.t2);
     const float *gp = planes + I.g;
     const long long pitch = L.pitch;
-    const bool x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
+    const bool both = x0 >= 0 && x0 + 1 < W, x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
 #pragma unroll
     for (int r = 0; r < RB; r++) {
       const int y = ytop + r;
@@ -828,23 +885,39 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
       gw[r] = gm[r] = ge[r] = 0.0f;
       if (y >= 0 && y < H) {
         const float *gr = gp + (long long)y * pitch, *lr = lp + (long long)y * pitch;
-        const float c0 = x0in ? __ldg(gr + x0) : 0.0f, c1 = x1in ? __ldg(gr + x0 + 1) : 0.0f;
-        if (x0in) Lp[r].x = __ldg(lr + x0);
-        if (x1in) Lp[r].y = __ldg(lr + x0 + 1);
-        if (x0in && x0 >= 1) gw[r] = __ldg(gr + x0 - 1) + c0;
-        if (x0 >= 0 && x0 + 1 < W) gm[r] = c0 + c1;
-        if (x1in && x0 + 2 < W) ge[r] = c1 + __ldg(gr + x0 + 2);
-        if (y + 1 < H) {
-          if (x0in) gs[r].x = c0 + __ldg(gr + pitch + x0);
-          if (x1in) gs[r].y = c1 + __ldg(gr + pitch + x0 + 1);
+        float2 c = make_float2(0.0f, 0.0f), cb = make_float2(0.0f, 0.0f);
+        const bool below = y + 1 < H;
+        if (both) {
+          c = __ldg((const float2 *)(gr + x0));
+          Lp[r] = __ldg((const float2 *)(lr + x0));
+          if (below) cb = __ldg((const float2 *)(gr + pitch + x0));
+        } else if (x0in) {
+          c.x = __ldg(gr + x0);
+          Lp[r].x = __ldg(lr + x0);
+          if (below) cb.x = __ldg(gr + pitch + x0);
+        } else if (x1in) {
+          c.y = __ldg(gr + x0 + 1);
+          Lp[r].y = __ldg(lr + x0 + 1);
+          if (below) cb.y = __ldg(gr + pitch + x0 + 1);
+        }
+        if (x0in && x0 >= 1) gw[r] = __ldg(gr + x0 - 1) + c.x;
+        if (both) gm[r] = c.x + c.y;
+        if (x1in && x0 + 2 < W) ge[r] = c.y + __ldg(gr + x0 + 2);
+        if (below) {
+          if (x0in) gs[r].x = c.x + cb.x;
+          if (x1in) gs[r].y = c.y + cb.y;
         }
       }
     }
     gn0 = make_float2(0.0f, 0.0f);
     if (ytop >= 1 && ytop < H) {
       const float *ga = gp + (long long)(ytop - 1) * pitch, *gb = gp + (long long)ytop * pitch;
-      if (x0in) gn0.x = __ldg(ga + x0) + __ldg(gb + x0);
-      if (x1in) gn0.y = __ldg(ga + x0 + 1) + __ldg(gb + x0 + 1);
+      if (both) {
+        gn0 = f2add(__ldg((const float2 *)(ga + x0)), __ldg((const float2 *)(gb + x0)));
+      } else {
+        if (x0in) gn0.x = __ldg(ga + x0) + __ldg(gb + x0);
+        if (x1in) gn0.y = __ldg(ga + x0 + 1) + __ldg(gb + x0 + 1);
+      }
     }
 #pragma unroll
     for (int r = 0; r < RB; r++) st2(cur + (ly0 + r) * RW + lx0, Lp[r]);
@@ -852,22 +925,26 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   }
 
   for (int s = p.first ? 1 : 0; s < d; s++) {
-    akz_fed_step<RW, true>(cur, nxt, p.h[s], lx0, ly0, Lp, gw, gm, ge, gs, gn0);
+    akz_fed_step<RW>(cur, nxt, p.h[s], lx0, ly0, Lp, gw, gm, ge, gs, gn0);
     __syncthreads();
     float *t = cur;
     cur = nxt;
     nxt = t;
   }
-  /* tile interior from registers */
+  /* tile interior from registers, one 64-bit store per pair */
   float *out = p.dst == 3 ? p.chk : planes + (p.dst == 0 ? L.lt : (p.dst == 1 ? I.t1 : I.t2));
-  const bool w0 = x0 >= tx0 && x0 < tx1, w1 = x0 + 1 >= tx0 && x0 + 1 < tx1;
+  const bool w0 = x0 >= tx0 && x0 < tx1, w1 = x0 + 1 < tx1;
+  if (w0) {
 #pragma unroll
-  for (int r = 0; r < RB; r++) {
-    const int y = ytop + r;
-    if (y >= ty0 && y < ty1) {
-      float *o = out + (long long)y * L.pitch + x0;
-      if (w0) o[0] = Lp[r].x;
-      if (w1) o[1] = Lp[r].y;
+    for (int r = 0; r < RB; r++) {
+      const int y = ytop + r;
+      if (y >= ty0 && y < ty1) {
+        float *o = out + (long long)y * L.pitch + x0;
+        if (w1)
+          st2(o, Lp[r]);
+        else
+          o[0] = Lp[r].x;
+      }
     }
   }
 }
@@ -931,6 +1008,7 @@ cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int, int, cudaSt
 {
   if (ntiles <= 0) return cudaSuccess;
   if (p.steps < 0 || p.steps > 8) return cudaErrorInvalidValue; /* 0: Lsmooth, conductance and the start image only */
+  if (p.first && !p.tmaps) return cudaErrorInvalidValue;         /* the input box needs the tensor maps */
   const size_t smem = akz_fed_smem_bytes(0, 0, p.steps, p.first);
   cudaError_t e = cudaFuncSetAttribute(k_fed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
