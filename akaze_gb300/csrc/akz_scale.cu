@@ -186,10 +186,31 @@ __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
   const int lt = blockIdx.x - sg.tile_begin;
   const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
 
-  for (int i = tid; i < PH * PW; i += 256) {
-    const int r = i / PW, c = i - r * PW;
-    const int y = akz_clampi(ty0 - 4 + r, 0, H - 1), x = akz_clampi(tx0 - 4 + c, 0, W - 1);
-    sP[i] = akz_fetch_input(p.t, I, x, y, p.inv255);
+  if (!p.t.input_f32 && tx0 >= 4 && tx0 + TW + 4 <= W && ty0 >= 4 && ty0 + TH + 4 <= H) {
+    /* interior tile: a row per warp, 4 bytes per lane (tx0 - 4 is a
+     * multiple of 4 and u8 rows are 16-byte aligned), 4 floats per store */
+    static_assert(PW == 136 && TW % 4 == 0, "k_level0 staging");
+    const uint8_t *u8 = p.t.u8 + I.u8_off + tx0 - 4;
+#pragma unroll
+    for (int k = 0; k < PH / 8; k++) {
+      const int r = warp + 8 * k;
+      const uchar4 *src = reinterpret_cast<const uchar4 *>(u8 + (long long)(ty0 - 4 + r) * I.u8_pitch);
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const int q = lane + 32 * j;
+        if (q < PW / 4) {
+          const uchar4 b = __ldg(src + q);
+          *reinterpret_cast<float4 *>(sP + r * PW + 4 * q) =
+              make_float4((float)b.x * p.inv255, (float)b.y * p.inv255, (float)b.z * p.inv255, (float)b.w * p.inv255);
+        }
+      }
+    }
+  } else {
+    for (int i = tid; i < PH * PW; i += 256) {
+      const int r = i / PW, c = i - r * PW;
+      const int y = akz_clampi(ty0 - 4 + r, 0, H - 1), x = akz_clampi(tx0 - 4 + c, 0, W - 1);
+      sP[i] = akz_fetch_input(p.t, I, x, y, p.inv255);
+    }
   }
   __syncthreads();
   /* rows passes: soffset Gaussian on tile columns (all PH rows), sigma-1 on
@@ -316,16 +337,45 @@ __global__ void __launch_bounds__(256) k_contrast_hist(akz_level0_params p)
   const float nb = (float)p.nbins;
   const float *mp = p.t.planes + I.t1;
   const int x0 = max(tx0, 1), x1 = min(tx0 + TW, W - 1), y0 = max(ty0, 1), y1 = min(ty0 + TH, H - 1);
-  const int lane = tid & 31, warp = tid >> 5;
-  for (int y = y0 + warp; y < y1; y += 8)
-    for (int x = x0 + lane; x < x1; x += 32) {
-      const float modg = sqrtf(__ldg(mp + (long long)y * L.pitch + x));
+  /* a run of 16 consecutive pixels per thread (8 threads per 128-pixel row
+   * segment, 32 rows): neighbouring pixels mostly share a bin, so one shared
+   * atomic per run of equal bins instead of one per pixel */
+  static_assert(TW == 128 && TH == 32, "k_contrast_hist runs");
+  const int y = ty0 + (tid >> 3), xs = tx0 + 16 * (tid & 7);
+  if (y >= y0 && y < y1) {
+    const float *row = mp + (long long)y * L.pitch;
+    int cur = -1;
+    unsigned int cnt = 0;
+    float v[16];
+    if (xs >= x0 && xs + 16 <= x1) { /* pitch is a multiple of 32 floats: 16-byte aligned */
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const float4 f = __ldg(reinterpret_cast<const float4 *>(row + xs) + q);
+        v[4 * q] = f.x;
+        v[4 * q + 1] = f.y;
+        v[4 * q + 2] = f.z;
+        v[4 * q + 3] = f.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 16; k++) v[k] = (xs + k >= x0 && xs + k < x1) ? __ldg(row + xs + k) : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      const float modg = sqrtf(v[k]); /* 0 outside the interior: skipped like a zero gradient */
       if (modg != 0.0f) {
         int nbin = (int)floorf(nb * (modg / hmax));
         if (nbin == p.nbins) nbin--;
-        atomicAdd(&sHist[nbin], 1u);
+        if (nbin != cur) {
+          if (cnt) atomicAdd(&sHist[cur], cnt);
+          cur = nbin;
+          cnt = 0;
+        }
+        cnt++;
       }
     }
+    if (cnt) atomicAdd(&sHist[cur], cnt);
+  }
   __syncthreads();
   for (int b = tid; b < p.nbins; b += 256)
     if (sHist[b]) atomicAdd(&p.hist[(long long)L.image * p.nbins + b], sHist[b]);
