@@ -451,14 +451,30 @@ class BatchGroup:
         collected in order, each into kp_out / d_out right after the groups
         before it, so a group's copies overlap the others' kernels.  Returns
         the per-image counts."""
+        return self.detect_describe_packed_steps([imgs], kp_out, d_out)
+
+    def detect_describe_packed_steps(self, steps, kp_out, d_out, on_step=None):
+        """Several whole-job calls in a row (`steps`: one image list per
+        step), pipelined: group g's next step is submitted as soon as its
+        current one is collected, while the other groups are still running.
+        Each step's results are packed into kp_out / d_out (overwritten by
+        the next step); on_step(step_index, counts), if given, runs after a
+        step is collected.  Returns the last step's per-image counts."""
         for g, b in enumerate(self.parts):
-            b.submit(imgs[self.bounds[g]:self.bounds[g + 1]])
-        at, counts = 0, []
-        for b in self.parts:
-            c, n = b.collect_packed(kp_out[at:], d_out[at:])
-            counts.append(c)
-            at += n
-        return np.concatenate(counts)
+            b.submit(steps[0][self.bounds[g]:self.bounds[g + 1]])
+        counts = None
+        for si in range(len(steps)):
+            at, parts = 0, []
+            for g, b in enumerate(self.parts):
+                c, n = b.collect_packed(kp_out[at:], d_out[at:])
+                parts.append(c)
+                at += n
+                if si + 1 < len(steps):
+                    b.submit(steps[si + 1][self.bounds[g]:self.bounds[g + 1]])
+            counts = np.concatenate(parts)
+            if on_step:
+                on_step(si, counts)
+        return counts
 
 
 def save_keypoints(path, kpts, desc=None):

@@ -582,8 +582,9 @@ def main():
         dist.barrier()
     t0 = time.perf_counter()
     e_steps = max(1, min(args.steps, 10))
-    for _ in range(e_steps):
-        c2 = batch.detect_describe_packed(np_in, kp_out, d_out)
+    # consecutive steps pipelined per group: a group's next upload starts once its
+    # results are read back, while the other groups still compute
+    c2 = batch.detect_describe_packed_steps([np_in] * e_steps, kp_out, d_out)
     el = replicas.max_over_ranks(time.perf_counter() - t0, dist, device="cuda")
     e2e = replicas.job_throughput(B * e_steps, ws, el)
     h2d = B * W * H

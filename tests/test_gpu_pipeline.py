@@ -194,3 +194,28 @@ def test_batch_group_equals_one_batch(gpu_lib):
         off += len(k)
     with pytest.raises(gpu_lib.AkazeError):  # nothing submitted
         grp.parts[0].collect_packed(kp, d)
+
+
+def test_batch_group_pipelined_steps(gpu_lib):
+    """Pipelined whole-job steps give each step the results of a single call."""
+    sizes = synth.uneven_sizes(17, 6)
+    a = [synth.synth_image(1700 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    b = [synth.synth_image(1800 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    grp = gpu_lib.BatchGroup(gpu_lib.AKAZEOptions(), sizes, groups=2)
+    cap = 200000
+    kp = np.zeros(cap, gpu_lib.KEYPOINT_DTYPE)
+    d = np.zeros((cap, 61), np.uint8)
+    want = []
+    for imgs in (a, b):
+        c = grp.detect_describe_packed(imgs, kp, d)
+        n = int(c.sum())
+        want.append((c.copy(), kp[:n].tobytes(), d[:n].copy()))
+    got = []
+
+    def keep(si, c):
+        n = int(c.sum())
+        got.append((c.copy(), kp[:n].tobytes(), d[:n].copy()))
+
+    grp.detect_describe_packed_steps([a, b, a], kp, d, on_step=keep)
+    for (wc, wk, wd), (gc, gk, gd) in zip(want + [want[0]], got):
+        assert np.array_equal(wc, gc) and wk == gk and np.array_equal(wd, gd)
