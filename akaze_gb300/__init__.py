@@ -361,6 +361,14 @@ class Batch:
                                                          _ptr(counts), ctypes.byref(total)))
         return counts
 
+    def image_info(self, i):
+        """(raw extrema, keypoints, suppression rounds, contrast factor) of image i."""
+        nraw, nkp, rounds = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        kc = ctypes.c_float()
+        check(self._lib.akz_batch_image_info(self._h, int(i), ctypes.byref(nraw), ctypes.byref(nkp),
+                                             ctypes.byref(rounds), ctypes.byref(kc)))
+        return nraw.value, nkp.value, rounds.value, kc.value
+
     def submit(self, imgs):
         """First half of detect_describe_packed: enqueues the upload, the
         graph and the count read-back, and returns at once; the images must

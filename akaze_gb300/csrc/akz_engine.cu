@@ -1354,6 +1354,20 @@ AKZ_API akz_status akz_batch_detect_describe(akz_batch *b, const uint8_t *const 
   return AKZ_OK;
 }
 
+AKZ_API akz_status akz_batch_image_info(akz_batch *b, int i, int *nraw, int *nkp, int *rounds, float *kcontrast)
+{
+  AKZ_GUARD(b);
+  if (i < 0 || i >= b->nimg) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_batch_image_info: image %d out of range", i);
+  akz_image_stats st;
+  CK(cudaMemcpyAsync(&st, b->d_stats + i, sizeof(st), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  if (nraw) *nraw = st.nraw;
+  if (nkp) *nkp = st.nkp;
+  if (rounds) *rounds = st.nms_rounds;
+  if (kcontrast) *kcontrast = st.kcontrast;
+  return AKZ_OK;
+}
+
 AKZ_API akz_status akz_batch_submit(akz_batch *b, const uint8_t *const *images, const size_t *strides)
 {
   AKZ_GUARD(b);

@@ -322,22 +322,40 @@ def _pick_fed_depth(batch, args, default):
     return [int(depth)], None
 
 
+def _group_event_ms(torch, stream, gstreams, fn, steps):
+    """ms per call of fn, whose work runs on gstreams, timed with events on
+    stream that bracket every group stream."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for g in gstreams:
+        g.wait_event(e0)
+    for _ in range(steps):
+        fn()
+    for g in gstreams:
+        stream.wait_stream(g)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def workload_uneven64(args):
-    """64 images of uneven sizes in one graph-replayed batch (images/s), and
-    each image alone (per-image latency, p50/p99)."""
+    """64 images of uneven sizes, split into stream groups of graph-replayed
+    batches (images/s), and each image alone (per-image latency, p50/p99)."""
     torch, stream = _torch_stream()
     import akaze_gb300 as akz
     from akaze_gb300 import synth
     sizes = synth.uneven_sizes(2024, 64)
     imgs = [synth.synth_image(3000 + i, w, h) for i, (w, h) in enumerate(sizes)]
     opt = akz.AKAZEOptions()
-    b = akz.Batch(opt, sizes)
-    b.set_stream(stream.cuda_stream)
+    b = akz.BatchGroup(opt, sizes, groups=args.groups)
+    gstreams = [torch.cuda.Stream() for _ in b.parts]
+    b.set_streams([g.cuda_stream for g in gstreams])
     b.upload(imgs)
     fed_depth, depth_ms = _pick_fed_depth(b, args, "auto")
     for _ in range(max(args.warmup, 3)):
         b.run()
-    step_ms = _event_ms(torch, stream, b.run, args.steps)
+    step_ms = _group_event_ms(torch, stream, gstreams, b.run, args.steps)
     counts = b.counts()
     singles = []
     for (w, h), im in zip(sizes, imgs):
@@ -352,6 +370,7 @@ def workload_uneven64(args):
     mpix = sum(w * h for w, h in sizes) / 1e6
     print(json.dumps({
         "workload": "uneven64", "config": "64 synthetic images, W~U[320,1920], H~U[240,1080], multiples of 8",
+        "groups": len(b.parts),
         "images_per_s": 64 * 1000.0 / step_ms, "batch_ms": step_ms, "megapixels_per_batch": mpix,
         "latency_ms_alone": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                              "min": float(lat.min()), "max": float(lat.max())},

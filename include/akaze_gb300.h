@@ -296,6 +296,12 @@ AKZ_API akz_status akz_batch_autotune(akz_batch *b, float *ms_per_depth, int cap
 /* Sets the FED blocking depth (4..8; 8 at creation) without timing. */
 AKZ_API akz_status akz_batch_set_fed_depth(akz_batch *b, int depth);
 
+/* Diagnostics of image i after a run (no counterpart in the reference):
+ * raw extrema before suppression, keypoints after it, suppression rounds,
+ * and the contrast factor.  Any pointer may be NULL; synchronises the
+ * batch's stream. */
+AKZ_API akz_status akz_batch_image_info(akz_batch *b, int i, int *nraw, int *nkp, int *rounds, float *kcontrast);
+
 /* The two halves of akz_batch_detect_describe_packed, for overlapping
  * several batches (each on its own stream) from one host thread:
  * akz_batch_submit enqueues the upload of the host images, the batch's
