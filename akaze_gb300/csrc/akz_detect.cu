@@ -21,6 +21,7 @@
  *              the 2048-slot chunked emission and subpixel restore
  *              (:1227-1316).
  */
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -567,7 +568,7 @@ struct akz_nms_pick {
   bool wait;
   __device__ __forceinline__ bool operator()(int j)
   {
-    const int sj = state[j];
+    const int sj = __ldcg(state + j); /* other CTAs of the cluster write it */
     if (sj == -1) {
       wait = true;
       return false;
@@ -592,49 +593,66 @@ __device__ __forceinline__ int akz_nms_decide(const akz_nms_ctx &c, int i, int *
 
 __device__ __forceinline__ void akz_bitonic2048(int *v)
 {
-  const int t = threadIdx.x; /* 1024 threads */
   for (int k = 2; k <= 2048; k <<= 1) {
     for (int j = k >> 1; j > 0; j >>= 1) {
-      const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
-      const int l = i | j;
-      const bool up = (i & k) == 0;
-      const int a = v[i], b = v[l];
-      if ((a > b) == up) {
-        v[i] = b;
-        v[l] = a;
+      for (int t = threadIdx.x; t < 1024; t += blockDim.x) { /* 1024 compare-exchanges per step */
+        const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+        const int l = i | j;
+        const bool up = (i & k) == 0;
+        const int a = v[i], b = v[l];
+        if ((a > b) == up) {
+          v[i] = b;
+          v[l] = a;
+        }
       }
       __syncthreads();
     }
   }
 }
 
-__global__ void __launch_bounds__(AKZ_NMS_THREADS) k_nms(akz_nms_params p)
+/* Suppression of one image per cluster of AKZ_NMS_CL CTAs (a point per
+ * thread of the cluster, strided): the reference's rounds (cuda_akaze.cu:
+ * 1005-1224) with a cluster barrier between their phases, so the image with
+ * the most raw extrema no longer runs on one SM while the others idle.
+ * Points' states live in global memory; they are read through L2
+ * (__ldcg) after each barrier's release/acquire, since another SM of the
+ * cluster may have written them.  Emission: every chunk of 2048 slots is
+ * counted first (any CTA), the counts are prefixed, then each CTA sorts its
+ * own chunks and writes them at their offsets (cuda_akaze.cu:1227-1316). */
+__global__ void __cluster_dims__(AKZ_NMS_CL, 1, 1) __launch_bounds__(AKZ_NMS_THREADS) k_nms(akz_nms_params p)
 {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
   __shared__ int sv[2048];
-  const int img = blockIdx.x;
+  __shared__ int sflag[2];
+  const int rank = (int)cl.block_rank();
+  const int img = blockIdx.x / AKZ_NMS_CL;
   const int tid = threadIdx.x;
+  const int gt = rank * AKZ_NMS_THREADS + tid, GT = AKZ_NMS_CL * AKZ_NMS_THREADS;
   const akz_image_desc I = p.t.im[img];
   akz_image_stats *stats = &p.t.stats[img];
-  if (stats->overflow) {
-    if (tid == 0) stats->nkp = 0;
+  if (__ldcg(&stats->overflow)) { /* the same for every CTA of the cluster */
+    if (rank == 0 && tid == 0) stats->nkp = 0;
     return;
   }
-  const int n = stats->nraw;
+  const int n = __ldcg(&stats->nraw);
   const akz_raw *R = p.raw + I.raw_base;
   int *state = p.state + I.raw_base;
   int *minc = p.aux + I.raw_base;
   signed char *dec = p.decision + I.raw_base;
-  for (int i = tid; i < n; i += AKZ_NMS_THREADS) {
+  if (tid < 2) sflag[tid] = 0;
+  for (int i = gt; i < n; i += GT) {
     state[i] = -1;
     minc[i] = INT_MAX;
   }
-  __syncthreads();
+  cl.sync();
   const akz_nms_ctx c{R, state, p.rowscan + I.rows_base, p.t.lv, I.first_level, I.rows_base};
   /* neighbour sets, found once (the rounds then cost O(neighbours) each);
-   * a point with more than AKZ_NMS_NB neighbours is decided by scanning */
+   * a point with more than AKZ_NMS_NB neighbours is decided by scanning;
+   * point i is always handled by the same thread */
   int *nbr = p.nbr + (long long)I.raw_base * AKZ_NMS_NB;
   unsigned char *nbc = p.nbc + I.raw_base;
-  for (int i = tid; i < n; i += AKZ_NMS_THREADS) {
+  for (int i = gt; i < n; i += GT) {
     int cnt = 0;
     int *li = nbr + (long long)i * AKZ_NMS_NB;
     const bool all = akz_nms_visit(c, i, [&](int j) {
@@ -644,12 +662,12 @@ __global__ void __launch_bounds__(AKZ_NMS_THREADS) k_nms(akz_nms_params p)
     });
     nbc[i] = (unsigned char)(all ? cnt : AKZ_NMS_NB + 1);
   }
-  __syncthreads();
+  int *flag0 = cl.map_shared_rank(sflag, 0);
   int rounds = 0;
   for (;;) {
     int any = 0;
-    for (int i = tid; i < n; i += AKZ_NMS_THREADS) {
-      if (state[i] != -1) continue;
+    for (int i = gt; i < n; i += GT) {
+      if (__ldcg(state + i) != -1) continue;
       any = 1;
       int target = -1, d;
       const int cnt = nbc[i];
@@ -666,46 +684,74 @@ __global__ void __launch_bounds__(AKZ_NMS_THREADS) k_nms(akz_nms_params p)
       dec[i] = (signed char)d;
       if (d == 2) atomicMin(&minc[target], i);
     }
-    if (!__syncthreads_or(any)) break;
-    for (int i = tid; i < n; i += AKZ_NMS_THREADS)
-      if (state[i] == -1 && dec[i] == 1) state[i] = i;
-    __syncthreads();
-    for (int s = tid; s < n; s += AKZ_NMS_THREADS) {
-      const int ch = minc[s];
+    /* cluster-wide "any point unsettled": an OR into rank 0's flag of this
+     * round's parity; rank 0 clears the other parity, last read a round ago */
+    if (__syncthreads_or(any) && tid == 0) atomicOr(flag0 + (rounds & 1), 1);
+    cl.sync();
+    const int anyc = *(volatile int *)(flag0 + (rounds & 1));
+    if (rank == 0 && tid == 0) sflag[(rounds + 1) & 1] = 0;
+    if (!anyc) break;
+    for (int i = gt; i < n; i += GT)
+      if (__ldcg(state + i) == -1 && dec[i] == 1) state[i] = i;
+    cl.sync();
+    for (int s2 = gt; s2 < n; s2 += GT) {
+      const int ch = __ldcg(minc + s2);
       if (ch != INT_MAX) {
-        minc[s] = INT_MAX;
-        if (R[ch].response > R[s].response) {
-          state[ch] = s;
-          state[s] = -2;
+        minc[s2] = INT_MAX;
+        if (R[ch].response > R[s2].response) {
+          state[ch] = s2;
+          state[s2] = -2;
         } else {
           state[ch] = -2;
         }
       }
     }
-    __syncthreads();
+    cl.sync();
     if (++rounds > p.max_rounds) {
-      if (tid == 0) stats->status = 5; /* AKZ_ERR_TIMEOUT */
+      if (rank == 0 && tid == 0) stats->status = 5; /* AKZ_ERR_TIMEOUT */
       break;
     }
   }
-  /* emission in chunks of 2048 slots, each chunk's slot values ascending */
-  akz_kp *kp = p.kp + I.kp_base;
-  int out = 0;
-  for (int cs = 0; cs < n; cs += 2048) {
+  /* emission in chunks of 2048 slots, each chunk's slot values ascending:
+   * counts of every chunk (into minc[chunk], free again), then offsets */
+  const int nchunks = (n + 2047) / 2048;
+  __shared__ int scnt;
+  for (int ck = rank; ck < nchunks; ck += AKZ_NMS_CL) {
+    if (tid == 0) scnt = 0;
+    __syncthreads();
+    int cnt = 0;
     for (int k = tid; k < 2048; k += AKZ_NMS_THREADS) {
-      const int s = cs + k;
+      const int s2 = ck * 2048 + k;
+      if (s2 < n) {
+        const int st = __ldcg(state + s2);
+        cnt += st >= 0 && R[st].size >= 0.0f;
+      }
+    }
+    if (cnt) atomicAdd(&scnt, cnt);
+    __syncthreads();
+    if (tid == 0) minc[ck] = scnt;
+    __syncthreads();
+  }
+  cl.sync();
+  akz_kp *kp = p.kp + I.kp_base;
+  int total = 0;
+  for (int ck = 0; ck < nchunks; ck++) total += __ldcg(minc + ck);
+  for (int ck = rank; ck < nchunks; ck += AKZ_NMS_CL) {
+    int out = 0;
+    for (int q = 0; q < ck; q++) out += __ldcg(minc + q);
+    for (int k = tid; k < 2048; k += AKZ_NMS_THREADS) {
+      const int s2 = ck * 2048 + k;
       int v = INT_MAX;
-      if (s < n) {
-        const int st = state[s];
+      if (s2 < n) {
+        const int st = __ldcg(state + s2);
         if (st >= 0 && R[st].size >= 0.0f) v = st;
       }
       sv[k] = v;
     }
     __syncthreads();
     akz_bitonic2048(sv);
-    const int c0 = __syncthreads_count(sv[tid] != INT_MAX);
-    const int c1 = __syncthreads_count(sv[tid + 1024] != INT_MAX);
-    for (int k = tid; k < c0 + c1; k += AKZ_NMS_THREADS) {
+    const int cnt = __ldcg(minc + ck);
+    for (int k = tid; k < cnt; k += AKZ_NMS_THREADS) {
       const akz_raw e = R[sv[k]];
       const float octsub = fabsf(e.octsub);
       const int octave = (int)octsub;
@@ -723,13 +769,13 @@ __global__ void __launch_bounds__(AKZ_NMS_THREADS) k_nms(akz_nms_params p)
       o.angle = 0.0f;
       kp[out + k] = o;
     }
-    out += c0 + c1;
     __syncthreads();
   }
-  if (tid == 0) {
-    stats->nkp = out;
+  if (rank == 0 && tid == 0) {
+    stats->nkp = total;
     stats->nms_rounds = rounds;
   }
+  cl.sync(); /* no CTA leaves while another may still read rank 0's flags */
 }
 
 /* ------------------------------------------------------------------------ */
@@ -763,6 +809,6 @@ cudaError_t akz_launch_extract(const akz_extract_params &p, int nrows, cudaStrea
 
 cudaError_t akz_launch_nms(const akz_nms_params &p, cudaStream_t s)
 {
-  k_nms<<<p.t.nimg, AKZ_NMS_THREADS, 0, s>>>(p);
+  k_nms<<<p.t.nimg * AKZ_NMS_CL, AKZ_NMS_THREADS, 0, s>>>(p);
   return cudaGetLastError();
 }

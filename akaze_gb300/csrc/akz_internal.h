@@ -21,7 +21,8 @@
 
 #define AKZ_MAX_LEVELS 64
 #define AKZ_MAX_NBINS 4096
-#define AKZ_NMS_THREADS 1024
+#define AKZ_NMS_THREADS 512
+#define AKZ_NMS_CL 8 /* CTAs per image in the suppression kernel (a thread-block cluster) */
 #define AKZ_NMS_NB 8 /* neighbour list capacity per raw extremum */
 
 /* One (image, level). */
