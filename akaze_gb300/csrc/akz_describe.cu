@@ -45,7 +45,70 @@ struct akz_warp_smem {
   float v[87];
   float bx[42], by[42];
   float wx[42], wy[42];
+  float acc[16 * 2 * 32]; /* cell partials of one grid and channel: [cell][thread parity][lane] */
 };
+
+/* One grid (C cells) of the M-LDB cell sums, all three channels, in the
+ * reference's order (ExtractDescriptors, cuda_akaze.cu:1456-1523): its 64
+ * threads each sum the samples i = t, t + 64, ... of a cell in increasing
+ * i; then for every cell, lane j (j < 32) adds the partials of threads j and
+ * j + 32 and a __shfl_down tree (offsets 1, 2, 4, 8, 16) sums the 32 lanes.
+ * Here lane l holds the samples i = l + 32 m: even m belong to thread l,
+ * odd m to thread l + 32, so each lane keeps both partials of every cell
+ * (lane-private columns of acc; the sample's column offset is decoded once
+ * per grid) and forms its tree leaf.  The leaves of a small grid go through
+ * the shuffle tree itself; those of a larger one are transposed through acc
+ * (row stride 33: conflict-free both ways) so that lane c sums cell c's 32
+ * leaves in the tree's association. */
+template <int C, int SHIFT, int MASK, int BASE>
+__device__ __forceinline__ void akz_mldb_cells(float *acc, const float (*src)[441], const unsigned short *cells, int lane,
+                                               int nsmp, float *vout)
+{
+  int off[AKZ_DESC_ITERS]; /* acc column offset of each sample of this lane, -1 outside the grid */
+#pragma unroll
+  for (int m = 0; m < AKZ_DESC_ITERS; m++) {
+    const int i = lane + 32 * m;
+    const int c = i < nsmp ? (cells[i] >> SHIFT) & MASK : MASK;
+    off[m] = c < C ? (2 * c + (m & 1)) * 32 + lane : -1;
+  }
+#pragma unroll 1
+  for (int ch = 0; ch < 3; ch++) {
+    const float *sc = src[ch];
+#pragma unroll
+    for (int r = 0; r < 2 * C; r++) acc[r * 32 + lane] = 0.0f;
+#pragma unroll
+    for (int m = 0; m < AKZ_DESC_ITERS; m++)
+      if (off[m] >= 0) acc[off[m]] += sc[lane + 32 * m];
+    float a[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) a[c] = acc[(2 * c) * 32 + lane] + acc[(2 * c + 1) * 32 + lane];
+    if (C <= 4) {
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        float v = a[c];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+        if (lane == 0) vout[3 * (BASE + c) + ch] = v;
+      }
+    } else {
+      __syncwarp();
+#pragma unroll
+      for (int c = 0; c < C; c++) acc[c * 33 + lane] = a[c];
+      __syncwarp();
+      if (lane < C) {
+        float t[32];
+#pragma unroll
+        for (int k = 0; k < 32; k++) t[k] = acc[lane * 33 + k];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1)
+#pragma unroll
+          for (int j = 0; j < 32; j += 2 * d) t[j] = t[j] + t[j + d];
+        vout[3 * (BASE + lane) + ch] = t[0];
+      }
+    }
+    __syncwarp();
+  }
+}
 
 __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_params p)
 {
@@ -92,6 +155,24 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
   const int ps = p.pattern_size;
   const int size2 = ps, size3 = (int)ceilf(2.0f * (float)ps / 3.0f), size4 = (int)ceilf(0.5f * (float)ps);
   const int win = max(3 * size3, 4 * size4);
+  /* each window sample's cell in the 2x2, 3x3 and 4x4 grids (7, 15, 31:
+   * outside that grid's range), the rules of cuda_akaze.cu:1470-1497 */
+  __shared__ unsigned short sCell[32 * AKZ_DESC_ITERS];
+  for (int i = threadIdx.x; i < 32 * AKZ_DESC_ITERS; i += blockDim.x) {
+    int c = 0xffff;
+    if (i < win * win) {
+      const int y = i / win, x = i - y * win, m = max(x, y);
+      const int c2 = m < 2 * size2 ? (x < size2 ? 0 : 1) + 2 * (y < size2 ? 0 : 1) : 7;
+      const int x3 = x < size3 ? 0 : (x < 2 * size3 ? 1 : 2), y3 = y < size3 ? 0 : (y < 2 * size3 ? 1 : 2);
+      const int c3 = m < 3 * size3 ? x3 + 3 * y3 : 15;
+      const int x4 = x < 2 * size4 ? (x < size4 ? 0 : 1) : (x < 3 * size4 ? 2 : 3);
+      const int y4 = y < 2 * size4 ? (y < size4 ? 0 : 1) : (y < 3 * size4 ? 2 : 3);
+      const int c4 = m < 4 * size4 ? x4 + 4 * y4 : 31;
+      c = c2 | (c3 << 3) | (c4 << 7);
+    }
+    sCell[i] = (unsigned short)c;
+  }
+  __syncthreads();
   for (int g = blockIdx.x * AKZ_DESC_WARPS + wib; g < total; g += nwarps) {
     int img = 0, k = g;
     if (table) {
@@ -278,28 +359,9 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
       S.s[2][s] = dx * co + dy * si;
     }
     __syncwarp();
-    for (int q = lane; q < 87; q += 32) {
-      const int cell = q / 3, ch = q - 3 * cell;
-      int sz, cx, cy;
-      if (cell < 4) {
-        sz = size2;
-        cx = cell & 1;
-        cy = cell >> 1;
-      } else if (cell < 13) {
-        sz = size3;
-        cx = (cell - 4) % 3;
-        cy = (cell - 4) / 3;
-      } else {
-        sz = size4;
-        cx = (cell - 13) & 3;
-        cy = (cell - 13) >> 2;
-      }
-      const float *src = S.s[ch];
-      float acc = 0.0f;
-      for (int yy = cy * sz; yy < (cy + 1) * sz; yy++)
-        for (int xx = cx * sz; xx < (cx + 1) * sz; xx++) acc += src[yy * win + xx];
-      S.v[q] = acc;
-    }
+    akz_mldb_cells<4, 0, 7, 0>(S.acc, S.s, sCell, lane, nsmp, S.v);
+    akz_mldb_cells<9, 3, 15, 4>(S.acc, S.s, sCell, lane, nsmp, S.v);
+    akz_mldb_cells<16, 7, 31, 13>(S.acc, S.s, sCell, lane, nsmp, S.v);
     __syncwarp();
     /* word w holds bits 32w .. 32w+31, LSB first: one ballot per word */
     uint32_t myword = 0;

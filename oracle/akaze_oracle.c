@@ -786,8 +786,11 @@ int ako_get_keypoints(const ako_ctx *c, ako_keypoint *out, int cap)
 
 /* ------------------------------------------------------------------------ */
 /* M-LDB: cuda_akaze.cu:1420-1533 (samples and cell sums), :1786-1807 (bits)
- * and :2034-2111 (comparison order).  Cell sums accumulate in raster order of
- * the sampling window. */
+ * and :2034-2111 (comparison order).  Cell sums in the reference's order
+ * (ExtractDescriptors, cuda_akaze.cu:1456-1523): 64 threads, thread t sums
+ * the window samples i = t, t + 64, ... of each cell in increasing i; per
+ * cell, lane j < 32 adds the partials of threads j and j + 32, and a
+ * __shfl_down tree with offsets 1, 2, 4, 8, 16 sums the 32 lanes. */
 
 static int ako_cmp_pairs(int *i1, int *i2)
 {
@@ -830,9 +833,11 @@ int ako_describe(ako_ctx *c)
     float co = 1.0f, si = 0.0f;
     if (!upright) akz_sincosf(k->angle, &si, &co);
     float vals[87];
-    for (int q = 0; q < 87; q++) vals[q] = 0.0f;
+    float part[64][87];
+    memset(part, 0, sizeof(part));
     for (int y = 0; y < win; y++) {
       for (int x = 0; x < win; x++) {
+        float *pv = part[(y * win + x) & 63];
         const int m = x > y ? x : y;
         const int l = x - size2, kk = y - size2;
         int xp = (int)(xf + (float)scale * ((float)kk * co - (float)l * si) + 0.5f);
@@ -846,26 +851,33 @@ int ako_describe(ako_ctx *c)
         if (m < 2 * size2) {
           const int x2 = x < size2 ? 0 : 1, y2 = y < size2 ? 0 : 1;
           const int cell = y2 * 2 + x2;
-          vals[3 * cell] += im;
-          vals[3 * cell + 1] += rx;
-          vals[3 * cell + 2] += ry;
+          pv[3 * cell] += im;
+          pv[3 * cell + 1] += rx;
+          pv[3 * cell + 2] += ry;
         }
         if (m < 3 * size3) {
           const int x3 = x < size3 ? 0 : (x < 2 * size3 ? 1 : 2), y3 = y < size3 ? 0 : (y < 2 * size3 ? 1 : 2);
           const int cell = 4 + y3 * 3 + x3;
-          vals[3 * cell] += im;
-          vals[3 * cell + 1] += rx;
-          vals[3 * cell + 2] += ry;
+          pv[3 * cell] += im;
+          pv[3 * cell + 1] += rx;
+          pv[3 * cell + 2] += ry;
         }
         if (m < 4 * size4) {
           const int x4 = x < 2 * size4 ? (x < size4 ? 0 : 1) : (x < 3 * size4 ? 2 : 3);
           const int y4 = y < 2 * size4 ? (y < size4 ? 0 : 1) : (y < 3 * size4 ? 2 : 3);
           const int cell = 13 + y4 * 4 + x4;
-          vals[3 * cell] += im;
-          vals[3 * cell + 1] += rx;
-          vals[3 * cell + 2] += ry;
+          pv[3 * cell] += im;
+          pv[3 * cell + 1] += rx;
+          pv[3 * cell + 2] += ry;
         }
       }
+    }
+    for (int q = 0; q < 87; q++) {
+      float a[32];
+      for (int j = 0; j < 32; j++) a[j] = part[j][q] + part[j + 32][q];
+      for (int d = 1; d < 32; d <<= 1)
+        for (int j = 0; j < 32; j += 2 * d) a[j] = a[j] + a[j + d];
+      vals[q] = a[0];
     }
     uint8_t *d = c->desc + (size_t)p * 61;
     for (int b = 0; b < 486; b++)
