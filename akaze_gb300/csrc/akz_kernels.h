@@ -58,7 +58,7 @@ struct akz_gauss_params {
   float taps[AKZ_MAX_TAPS];
 };
 
-/* k_fed geometry: a 128 x 40 region R0 = tile +- d per CTA (d = FED steps of
+/* k_fed geometry: a 128 x 48 region R0 = tile +- d per CTA (d = FED steps of
  * the launch).  The region's left edge tx0 - d - delta sits on a multiple of
  * 4 columns (delta = (-d) mod 4, tile origins are multiples of 4), so every
  * column pair is 8-byte aligned in shared and global memory and the TMA box
@@ -66,9 +66,9 @@ struct akz_gauss_params {
  * width is what remains, rounded down to a multiple of 4. */
 static inline __host__ __device__ int akz_fed_delta(int d) { return (4 - (d & 3)) & 3; }
 static inline __host__ __device__ int akz_fed_tile_w(int d) { return (128 - 2 * d - akz_fed_delta(d)) & ~3; }
-static inline __host__ __device__ int akz_fed_tile_h(int d) { return 40 - 2 * d; }
+static inline __host__ __device__ int akz_fed_tile_h(int d) { return 48 - 2 * d; }
 #define AKZ_FED_BOX_W 136 /* input box: region +- 4 columns */
-#define AKZ_FED_BOX_H 46  /* region +- 3 rows */
+#define AKZ_FED_BOX_H 54  /* region +- 3 rows */
 
 struct akz_fed_params {
   akz_tables t;

@@ -455,38 +455,42 @@ __global__ void __launch_bounds__(256) k_gauss0(akz_gauss_params p)
 
 /* FED level kernel.
  *
- * Every CTA owns a fixed 128 x 40 region R0 = tile +- d (d = FED steps of the
+ * Every CTA owns a fixed 128 x 48 region R0 = tile +- d (d = FED steps of the
  * launch; the region's left edge is rounded down to a multiple of 4 columns,
  * akz_fed_tile_w), so one thread geometry serves every chunk size: 512
- * threads, 2 column groups of 32 lanes x 2 columns, 8 bands of 5 rows; each
- * thread keeps the level values of its two columns in registers together
- * with the conductance pair sums (c_x + c_x+1) and (c_y + c_y+1) of the
- * reference's flux terms, which do not change across steps.  A step reads
- * the outer east/west neighbours (and the band's outer rows) from a
- * double-buffered shared plane and writes its two values with one 64-bit
- * store: 1.5 shared-memory operations, 3 products and 3.5 packed FP32x2
- * additions per pixel-step, one barrier per step.  Pixels outside
- * tile +- (d - s) after step s are not needed and may hold anything; image
- * borders are replicate (clamped) neighbours, whose flux is exactly zero, as
- * in the reference's border formulas (nldiffusion_functions.cpp:241-307).
- * Column pairs start at even image columns everywhere, so global loads and
- * stores of a pair are single 64-bit accesses.
+ * threads, each with 4 columns x 3 rows of R0 (a warp spans the region's
+ * 128 columns, 16 warps its 48 rows).  A thread keeps its level values and
+ * the conductance pair sums (c_x + c_x+1), (c_y + c_y+1) of the reference's
+ * flux terms in registers for the whole launch.  A step takes the west and
+ * east neighbours from the adjacent lanes (shuffles) and the rows above and
+ * below the warp's band from a double-buffered shared exchange of every
+ * warp's first and last row: one barrier per step, 6 shuffles and 2 128-bit
+ * shared loads and stores per thread and step.  Pixels outside
+ * tile +- (d - s) after step s are not needed and may hold anything (the
+ * region's outer columns and rows take their own values as stand-ins);
+ * image borders are replicate (clamped) neighbours, whose flux is exactly
+ * zero, as in the reference's border formulas (nldiffusion_functions.cpp:
+ * 241-307).  Column groups start at multiples of 4 image columns, so every
+ * global load or store of a thread's row is one 128-bit access.
  */
 #define AKZ_FED_RW 128
-#define AKZ_FED_RH 40
-#define AKZ_FED_RB 5
+#define AKZ_FED_RH 48
+#define AKZ_FED_RB 3
 #define AKZ_FED_THREADS 512
 #define AKZ_FED_PS (AKZ_FED_RW + 8) /* input plane: columns R0 - 4 .. R0 + 131 */
 #define AKZ_FED_SS (AKZ_FED_RW + 4) /* Gaussian planes: columns R0 - 2 .. R0 + 129 */
+#define AKZ_FED_XB (2 * 2 * 16 * AKZ_FED_RW) /* exchange rows: [step parity][first, last row][warp][column] */
 #define AKZ_FED_TMA_SPIN (1 << 22)  /* bounded wait for the input box */
 static_assert(AKZ_FED_PS == AKZ_FED_BOX_W && AKZ_FED_RH + 6 == AKZ_FED_BOX_H, "k_fed input box");
+static_assert(AKZ_FED_RB * 16 == AKZ_FED_RH && AKZ_FED_THREADS == 512, "k_fed thread geometry");
 
 size_t akz_fed_smem_bytes(int, int, int, int first)
 {
-  if (!first) return 2 * AKZ_FED_RW * AKZ_FED_RH * sizeof(float) + 128; /* the kernel aligns its base to 128 bytes */
+  if (!first) return AKZ_FED_XB * sizeof(float) + 128; /* the kernel aligns its base to 128 bytes */
   const size_t P = (size_t)(AKZ_FED_RH + 6) * AKZ_FED_PS;
   const size_t T = (size_t)(AKZ_FED_RH + 6) * AKZ_FED_SS;
   const size_t S = (size_t)(AKZ_FED_RH + 2) * AKZ_FED_SS;
+  static_assert((size_t)AKZ_FED_XB <= (size_t)(AKZ_FED_RH + 6) * (AKZ_FED_PS + AKZ_FED_SS), "exchange rows fit sP + sT");
   return (P + T + S) * sizeof(float) + 128 + 16; /* 128-byte alignment of the TMA box, the mbarrier */
 }
 
@@ -558,7 +562,8 @@ __device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
  * conductance pair sums are zero.
  *
  * Leaves the level values of R0 in sP (stride AKZ_FED_PS, R0 at row 3,
- * column 4) and the conductance in sT (stride RW).  Filter passes work on
+ * column 4), the conductance in sT (stride RW) and this thread's 3 x 4
+ * conductances in g.  Filter passes work on
  * column pairs with packed FP32x2 additions and scalar products, in the
  * reference's operation order:
  *   Gaussian  k0*(v[-2] + v[+2]) + k1*(v[-1] + v[+1]) + k2*v[0], rows then columns;
@@ -569,12 +574,12 @@ __device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
 template <int SRCK>
 __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const akz_level_desc &L,
                                                  const akz_image_desc &I, int level_desc, float *sm, int ox, int oy,
-                                                 int tx0, int ty0, int tx1, int ty1, int lx0, int ly0)
+                                                 int tx0, int ty0, int tx1, int ty1, int lx0, int ly0, float (&g)[3][4])
 {
-  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB, NT = AKZ_FED_THREADS;
+  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, NT = AKZ_FED_THREADS;
   constexpr int PS = AKZ_FED_PS, SS = AKZ_FED_SS, PH = RH + 6, SH = RH + 2;
   constexpr int NP = SS / 2;          /* column pairs of the smoothing regions */
-  constexpr int VR = 6, VG = SH / VR; /* rows per thread and row groups of the vertical pass */
+  constexpr int VR = 10, VG = SH / VR; /* rows per thread and row groups of the vertical pass */
   static_assert(SH % VR == 0 && NP * VG <= NT && NP == 66 && NT == 512, "k_fed prologue geometry");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int W = L.width, H = L.height;
@@ -640,7 +645,7 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
     /* replicate border: columns first (each row from its own clamped
      * column), then whole rows; the box always contains column and row 0
      * or W-1 / H-1 where it crosses the image edge */
-    if (ox - 4 < 0 || ox + 132 > W || oy - 3 < 0 || oy + 43 > H) {
+    if (ox - 4 < 0 || ox + 132 > W || oy - 3 < 0 || oy - 3 + PH > H) {
       if (ox - 4 < 0 || ox + 132 > W) {
         for (int i = tid; i < PH * PS; i += NT) {
           const int r = i / PS, c = i - r * PS, x = ox - 4 + c, xc = akz_clampi(x, 0, W - 1);
@@ -648,7 +653,7 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
         }
         __syncthreads();
       }
-      if (oy - 3 < 0 || oy + 43 > H) {
+      if (oy - 3 < 0 || oy - 3 + PH > H) {
         for (int i = tid; i < PH * PS; i += NT) {
           const int r = i / PS, c = i - r * PS, y = oy - 3 + r, yc = akz_clampi(y, 0, H - 1);
           if (yc != y) sP[i] = sP[(yc - (oy - 3)) * PS + c];
@@ -734,142 +739,159 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
   }
 
   /* 5. Scharr gradient of Lsmooth and the conductance on R0, in this
-   *    thread's k_fed geometry: columns lx0, lx0+1 (x0 = ox + lx0, sS
-   *    column lx0 + 2), rows ly0 .. ly0+RB-1; the conductance goes to sT
-   *    (free since pass 3), the level values stay in sP */
+   *    thread's k_fed geometry: columns x0 .. x0+3 (x0 = ox + lx0, sS
+   *    columns lx0 + 2 ..), rows ly0 .. ly0+2; kept in g, stored to sT
+   *    (free since pass 3; neighbours read it after the barrier) and, for
+   *    later chunks, to HBM */
   float *sG = sT;
   const float inv_k = p.kc[L.image * 16 + L.octave].y;
-  float2 dh[RB + 2], sh[RB + 2];
+  const int x0 = ox + lx0; /* a multiple of 4 */
 #pragma unroll
-  for (int j = 0; j < RB + 2; j++) {
-    const float *row = sS + (ly0 + j) * SS + lx0; /* x0 - 2 .. x0 + 3 */
-    const float2 A = ld2(row), B = ld2(row + 2), C = ld2(row + 4);
-    const float2 P = make_float2(A.y, B.x), Q = make_float2(B.y, C.x); /* (x0-1, x0), (x0+1, x0+2) */
-    dh[j] = f2sub(Q, P);
-    const float2 t = f2add(P, Q);
-    sh[j] = f2add(make_float2(3.0f * t.x, 3.0f * t.y), make_float2(10.0f * P.y, 10.0f * Q.x));
+  for (int h = 0; h < 2; h++) { /* column pairs (x0, x0+1), (x0+2, x0+3) */
+    float2 dh[5], sh[5];
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+      const float *row = sS + (ly0 + j) * SS + lx0 + 2 * h; /* x0 + 2h - 2 .. x0 + 2h + 3 */
+      const float2 A = ld2(row), B = ld2(row + 2), C = ld2(row + 4);
+      const float2 P = make_float2(A.y, B.x), Q = make_float2(B.y, C.x);
+      dh[j] = f2sub(Q, P);
+      const float2 t = f2add(P, Q);
+      sh[j] = f2add(make_float2(3.0f * t.x, 3.0f * t.y), make_float2(10.0f * P.y, 10.0f * Q.x));
+    }
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const float2 u = f2add(dh[r], dh[r + 2]);
+      const float2 gx = f2add(make_float2(3.0f * u.x, 3.0f * u.y), make_float2(10.0f * dh[r + 1].x, 10.0f * dh[r + 1].y));
+      const float2 gy = f2sub(sh[r + 2], sh[r]);
+      const float2 m = f2add(make_float2(gx.x * gx.x, gx.y * gx.y), make_float2(gy.x * gy.x, gy.y * gy.y));
+      const float2 gv = p.diffusivity == 1 ? akz_pm_g2_pair(m, inv_k)
+                                           : make_float2(akz_conductance_m(m.x, inv_k, p.diffusivity),
+                                                         akz_conductance_m(m.y, inv_k, p.diffusivity));
+      g[r][2 * h] = gv.x;
+      g[r][2 * h + 1] = gv.y;
+    }
   }
-  const int x0 = ox + lx0; /* even */
-  const bool w0 = p.write_g && x0 >= tx0 && x0 < tx1, w1 = x0 + 1 < tx1;
-  float *gp = p.t.planes + I.g + x0;
 #pragma unroll
-  for (int r = 0; r < RB; r++) {
-    const float2 u = f2add(dh[r], dh[r + 2]);
-    const float2 gx = f2add(make_float2(3.0f * u.x, 3.0f * u.y), make_float2(10.0f * dh[r + 1].x, 10.0f * dh[r + 1].y));
-    const float2 gy = f2sub(sh[r + 2], sh[r]);
-    const float2 m = f2add(make_float2(gx.x * gx.x, gx.y * gx.y), make_float2(gy.x * gy.x, gy.y * gy.y));
-    const float2 gv = p.diffusivity == 1 ? akz_pm_g2_pair(m, inv_k)
-                                         : make_float2(akz_conductance_m(m.x, inv_k, p.diffusivity),
-                                                       akz_conductance_m(m.y, inv_k, p.diffusivity));
-    st2(sG + (ly0 + r) * RW + lx0, gv);
+  for (int r = 0; r < 3; r++) {
+    *reinterpret_cast<float4 *>(sG + (ly0 + r) * RW + lx0) = make_float4(g[r][0], g[r][1], g[r][2], g[r][3]);
     const int y = oy + ly0 + r;
-    if (w0 && y >= ty0 && y < ty1) {
-      float *o = gp + (long long)y * L.pitch;
-      if (w1)
-        st2(o, gv);
-      else
-        o[0] = gv.x;
+    if (p.write_g && y >= ty0 && y < ty1) {
+      float *o = p.t.planes + I.g + (long long)y * L.pitch + x0;
+      if (x0 >= tx0 && x0 + 4 <= tx1) {
+        *reinterpret_cast<float4 *>(o) = make_float4(g[r][0], g[r][1], g[r][2], g[r][3]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          if (x0 + k >= tx0 && x0 + k < tx1) o[k] = g[r][k];
+      }
     }
   }
   __syncthreads();
   return true;
 }
 
-/* Registers of one k_fed thread (columns x0, x0+1 of R0, RB rows) from the
- * level values (sL, row stride LS, at R0's origin, pairs 8-byte aligned) and
- * the conductance on R0 (sG, row stride RW) in shared memory:
- *   Lp[r]   the two level values;
- *   gw[r]   c(x0-1) + c(x0)   the west flux pair of column x0;
- *   gm[r]   c(x0) + c(x0+1)   the flux pair between the two columns;
- *   ge[r]   c(x0+1) + c(x0+2) the east flux pair of column x0+1;
- *   gs[r]   c(x, y) + c(x, y+1) of both columns; gn0 the pair above row 0.
+/* The flux pair sums of one thread (columns x0 .. x0+3, rows ytop ..
+ * ytop+2) from its conductances g, the rows above (ga) and below (gb) its
+ * band and the lanes' neighbours (shuffles):
+ *   gh[r][e]  c(x0+e-1) + c(x0+e) for e = 0..4, the fluxes west of column e
+ *             (e = 4: east of column 3);
+ *   gs[r][k]  c(x, y) + c(x, y+1);   gn[k] the pair above row 0.
  * A pair that crosses the image border is zero: the reference omits that
  * flux term (nldiffusion_functions.cpp:241-307), and zero times any finite
- * difference adds nothing.  INTERIOR: R0 +- 1 lies inside the image, so no
- * pair crosses the border. */
-template <bool INTERIOR, int LS>
-__device__ __forceinline__ void akz_fed_gather_smem(const float *sL, const float *sG, int lx0, int ly0, int x0, int ytop,
-                                                    int W, int H, float2 *Lp, float *gw, float *gm, float *ge,
-                                                    float2 *gs, float2 &gn0)
+ * difference adds nothing. */
+template <bool INTERIOR>
+__device__ __forceinline__ void akz_fed_pairs(const float (&g)[3][4], const float4 ga, const float4 gb, int x0, int ytop,
+                                              int W, int H, float (&gh)[3][5], float (&gs)[3][4], float (&gn)[4])
 {
-  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
-  const int lxw = max(lx0 - 1, 0), lxe = min(lx0 + 2, RW - 1);
-  float2 c[RB + 2]; /* conductance pairs of rows ly0 - 1 .. ly0 + RB (clamped to R0) */
+  const float ra[4] = {ga.x, ga.y, ga.z, ga.w}, rb[4] = {gb.x, gb.y, gb.z, gb.w};
 #pragma unroll
-  for (int r = 0; r < RB + 2; r++) c[r] = ld2(sG + akz_clampi(ly0 - 1 + r, 0, RH - 1) * RW + lx0);
+  for (int r = 0; r < 3; r++) {
+    const float gw = __shfl_up_sync(0xffffffffu, g[r][3], 1), ge = __shfl_down_sync(0xffffffffu, g[r][0], 1);
+    const int y = ytop + r;
+    const bool yin = y >= 0 && y < H, ys = y >= 0 && y + 1 < H;
 #pragma unroll
-  for (int r = 0; r < RB; r++) {
-    const int ly = ly0 + r;
-    Lp[r] = ld2(sL + ly * LS + lx0);
-    const float cw = sG[ly * RW + lxw], ce = sG[ly * RW + lxe];
-    const float2 cc = c[r + 1], cs = c[r + 2];
-    if (INTERIOR) {
-      gw[r] = cw + cc.x;
-      gm[r] = cc.x + cc.y;
-      ge[r] = cc.y + ce;
-      gs[r] = f2add(cc, cs);
-    } else {
-      const int y = ytop + r;
-      const bool yin = y >= 0 && y < H, x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
-      gw[r] = (yin && x0in && x0 >= 1) ? cw + cc.x : 0.0f;
-      gm[r] = (yin && x0 >= 0 && x0 + 1 < W) ? cc.x + cc.y : 0.0f;
-      ge[r] = (yin && x1in && x0 + 2 < W) ? cc.y + ce : 0.0f;
-      gs[r].x = (x0in && y >= 0 && y + 1 < H) ? cc.x + cs.x : 0.0f;
-      gs[r].y = (x1in && y >= 0 && y + 1 < H) ? cc.y + cs.y : 0.0f;
+    for (int e = 0; e < 5; e++) {
+      const float a = e == 0 ? gw : g[r][e - 1], b = e == 4 ? ge : g[r][e];
+      const int xl = x0 + e - 1; /* the pair (xl, xl + 1) */
+      gh[r][e] = (INTERIOR || (yin && xl >= 0 && xl + 1 < W)) ? a + b : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float b = r < 2 ? g[r + 1][k] : rb[k];
+      gs[r][k] = (INTERIOR || (ys && x0 + k >= 0 && x0 + k < W)) ? g[r][k] + b : 0.0f;
     }
   }
-  if (INTERIOR) {
-    gn0 = f2add(c[0], c[1]);
-  } else {
-    const bool nin = ytop >= 1 && ytop < H, x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
-    gn0.x = (x0in && nin) ? c[0].x + c[1].x : 0.0f;
-    gn0.y = (x1in && nin) ? c[0].y + c[1].y : 0.0f;
-  }
+  const bool nin = ytop >= 1 && ytop < H;
+#pragma unroll
+  for (int k = 0; k < 4; k++) gn[k] = (INTERIOR || (nin && x0 + k >= 0 && x0 + k < W)) ? ra[k] + g[0][k] : 0.0f;
 }
 
-/* One FED step of this thread's RB x 2 pixels (nld_step_scalar,
+/* One FED step of this thread's 3 x 4 pixels (nld_step_scalar,
  * nldiffusion_functions.cpp:232-237, :309-316):
  *   L += h * (((xpos - xneg) + ypos) - yneg)
  * Each flux product is formed once and used twice, which is exact: the
  * reference's xneg at x+1 is (c(x) + c(x+1)) * (L(x+1) - L(x)), the same
  * operands in the same order as xpos at x, and likewise yneg at y+1 and ypos
- * at y.  Additions run as packed FP32x2 pairs of the two columns; products
- * stay scalar.  cur: level values (row stride CS, at R0's origin, pairs
- * 8-byte aligned); nxt: the new values (row stride RW). */
-template <int CS>
-__device__ __forceinline__ void akz_fed_step(const float *cur, float *nxt, float h, int lx0, int ly0, float2 *Lp,
-                                             const float *gw, const float *gm, const float *ge, const float2 *gs,
-                                             float2 gn0)
+ * at y.  Additions run as packed FP32x2 pairs; products stay scalar.  above
+ * and below are the rows next to the band (old values). */
+__device__ __forceinline__ void akz_fed_step4(float (&Lp)[3][4], float4 above, float4 below, float h,
+                                              const float (&gh)[3][5], const float (&gs)[3][4], const float (&gn)[4])
 {
-  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB;
-  const int lyn = max(ly0 - 1, 0), lys = min(ly0 + RB, RH - 1);
-  const int lxw = max(lx0 - 1, 0), lxe = min(lx0 + 2, RW - 1);
-  const float2 above = ld2(cur + lyn * CS + lx0), below = ld2(cur + lys * CS + lx0);
-  const float2 dn = f2sub(Lp[0], above);
-  float2 Fn = make_float2(gn0.x * dn.x, gn0.y * dn.y);
+  float Lw[3], Le[3];
 #pragma unroll
-  for (int r = 0; r < RB; r++) {
-    const int ly = ly0 + r;
-    const float2 Lc = Lp[r];
-    const float Lw = cur[ly * CS + lxw], Le = cur[ly * CS + lxe];
-    const float2 dwm = f2sub(Lc, make_float2(Lw, Lc.x)); /* L(x0)-L(x0-1), L(x0+1)-L(x0) */
-    const float de = Le - Lc.y;                          /* L(x0+2)-L(x0+1) */
-    const float Fw = gw[r] * dwm.x, Fm = gm[r] * dwm.y, Fe = ge[r] * de;
-    const float2 xs = f2sub(make_float2(Fm, Fe), make_float2(Fw, Fm)); /* xpos - xneg */
-    const float2 ds = f2sub(r < RB - 1 ? Lp[r + 1] : below, Lc);
-    const float2 Fs = make_float2(gs[r].x * ds.x, gs[r].y * ds.y); /* ypos */
-    const float2 t = f2sub(f2add(xs, Fs), Fn);
-    const float2 nv = f2add(Lc, make_float2(h * t.x, h * t.y));
-    st2(nxt + ly * RW + lx0, nv);
-    Lp[r] = nv;
-    Fn = Fs;
+  for (int r = 0; r < 3; r++) {
+    Lw[r] = __shfl_up_sync(0xffffffffu, Lp[r][3], 1);
+    Le[r] = __shfl_down_sync(0xffffffffu, Lp[r][0], 1);
   }
+  const float ab[4] = {above.x, above.y, above.z, above.w}, bl[4] = {below.x, below.y, below.z, below.w};
+  float Fn[4];
+  {
+    const float2 d0 = f2sub(make_float2(Lp[0][0], Lp[0][1]), make_float2(ab[0], ab[1]));
+    const float2 d1 = f2sub(make_float2(Lp[0][2], Lp[0][3]), make_float2(ab[2], ab[3]));
+    Fn[0] = gn[0] * d0.x;
+    Fn[1] = gn[1] * d0.y;
+    Fn[2] = gn[2] * d1.x;
+    Fn[3] = gn[3] * d1.y;
+  }
+  float nv[3][4];
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    const float *L = Lp[r];
+    /* horizontal differences L(x) - L(x-1) at the 5 edges */
+    const float2 e01 = f2sub(make_float2(L[0], L[1]), make_float2(Lw[r], L[0]));
+    const float2 e23 = f2sub(make_float2(L[2], L[3]), make_float2(L[1], L[2]));
+    const float e4 = Le[r] - L[3];
+    const float F0 = gh[r][0] * e01.x, F1 = gh[r][1] * e01.y, F2 = gh[r][2] * e23.x, F3 = gh[r][3] * e23.y,
+                F4 = gh[r][4] * e4;
+    const float2 xs01 = f2sub(make_float2(F1, F2), make_float2(F0, F1)); /* xpos - xneg */
+    const float2 xs23 = f2sub(make_float2(F3, F4), make_float2(F2, F3));
+    float nb[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) nb[k] = r < 2 ? Lp[r + 1][k] : bl[k];
+    const float2 ds01 = f2sub(make_float2(nb[0], nb[1]), make_float2(L[0], L[1]));
+    const float2 ds23 = f2sub(make_float2(nb[2], nb[3]), make_float2(L[2], L[3]));
+    const float Fs[4] = {gs[r][0] * ds01.x, gs[r][1] * ds01.y, gs[r][2] * ds23.x, gs[r][3] * ds23.y}; /* ypos */
+    const float2 t01 = f2sub(f2add(xs01, make_float2(Fs[0], Fs[1])), make_float2(Fn[0], Fn[1]));
+    const float2 t23 = f2sub(f2add(xs23, make_float2(Fs[2], Fs[3])), make_float2(Fn[2], Fn[3]));
+    const float2 n01 = f2add(make_float2(L[0], L[1]), make_float2(h * t01.x, h * t01.y));
+    const float2 n23 = f2add(make_float2(L[2], L[3]), make_float2(h * t23.x, h * t23.y));
+    nv[r][0] = n01.x;
+    nv[r][1] = n01.y;
+    nv[r][2] = n23.x;
+    nv[r][3] = n23.y;
+#pragma unroll
+    for (int k = 0; k < 4; k++) Fn[k] = Fs[k];
+  }
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int k = 0; k < 4; k++) Lp[r][k] = nv[r][k];
 }
 
 __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
 {
   extern __shared__ __align__(128) float sm_raw[];
-  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, RB = AKZ_FED_RB, PS = AKZ_FED_PS;
+  constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, PS = AKZ_FED_PS;
   if (p.gate && *p.gate <= p.gate_tol) return; /* a gated fallback that is not needed */
   /* the TMA box wants a 128-byte aligned destination */
   float *sm = sm_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(sm_raw) & 127u)) & 127u) / 4;
@@ -888,113 +910,106 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   const int srck = p.first ? sg.aux : p.src;
   float *planes = p.t.planes;
 
-  /* this thread: columns lx0, lx0+1 of R0, rows ly0 .. ly0+RB-1 */
-  const int lx0 = 2 * ((warp & 1) * 32 + lane);
-  const int ly0 = (warp >> 1) * RB;
-  const int x0 = ox + lx0; /* even */
+  /* this thread: columns lx0 .. lx0+3 of R0, rows ly0 .. ly0+2 */
+  const int lx0 = 4 * lane, ly0 = 3 * warp;
+  const int x0 = ox + lx0; /* a multiple of 4 */
   const int ytop = oy + ly0;
+  const bool interior = ox >= 1 && oy >= 1 && ox + RW + 1 <= W && oy + RH + 1 <= H;
 
-  float2 Lp[RB], gs[RB], gn0;
-  float gw[RB], gm[RB], ge[RB];
-  float *cur, *nxt;
-
+  float Lp[3][4], g[3][4];
+  float4 ga, gb; /* conductances of the rows above and below the band */
   if (p.first) {
-    float *sP = sm, *sT = sm + (RH + 6) * PS, *sS = sT + (RH + 6) * AKZ_FED_SS;
+    float *sP = sm, *sT = sm + (RH + 6) * PS;
     bool ok;
     if (srck == 1)
-      ok = akz_fed_prologue<1>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
+      ok = akz_fed_prologue<1>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0, g);
     else if (srck == 0)
-      ok = akz_fed_prologue<0>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
+      ok = akz_fed_prologue<0>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0, g);
     else
-      ok = akz_fed_prologue<2>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0);
+      ok = akz_fed_prologue<2>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0, g);
     if (!ok) return; /* uniform: every thread saw the same barrier state */
     const float *sL = sP + 3 * PS + 4; /* level values of R0 */
-    const bool interior = ox >= 1 && oy >= 1 && ox + RW + 1 <= W && oy + RH + 1 <= H;
-    if (interior)
-      akz_fed_gather_smem<true, PS>(sL, sT, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
-    else
-      akz_fed_gather_smem<false, PS>(sL, sT, lx0, ly0, x0, ytop, W, H, Lp, gw, gm, ge, gs, gn0);
-    if (d > 0) { /* the first step reads the level values where the prologue left them */
-      akz_fed_step<PS>(sL, sS, p.h[0], lx0, ly0, Lp, gw, gm, ge, gs, gn0);
-      __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      const float4 v = *reinterpret_cast<const float4 *>(sL + (ly0 + r) * PS + lx0);
+      Lp[r][0] = v.x;
+      Lp[r][1] = v.y;
+      Lp[r][2] = v.z;
+      Lp[r][3] = v.w;
     }
-    cur = sS;
-    nxt = sT; /* the conductance plane, read into registers before the barrier above */
+    ga = *reinterpret_cast<const float4 *>(sT + max(ly0 - 1, 0) * RW + lx0);
+    gb = *reinterpret_cast<const float4 *>(sT + min(ly0 + 3, RH - 1) * RW + lx0);
+    __syncthreads(); /* sP and sT are the exchange rows from here */
   } else {
-    cur = sm;
-    nxt = sm + RW * RH;
     const float *lp = planes + (p.src == 1 ? I.t1 : I.t2);
     const float *gp = planes + I.g;
     const long long pitch = L.pitch;
-    const bool both = x0 >= 0 && x0 + 1 < W, x0in = x0 >= 0 && x0 < W, x1in = x0 + 1 >= 0 && x0 + 1 < W;
+    const bool full = x0 >= 0 && x0 + 4 <= W;
+    auto row4 = [&](const float *base, int y) -> float4 { /* 4 values of row y from column x0, 0 outside */
+      if (y < 0 || y >= H) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const float *q = base + (long long)y * pitch + x0;
+      if (full) return __ldg(reinterpret_cast<const float4 *>(q));
+      float v[4];
 #pragma unroll
-    for (int r = 0; r < RB; r++) {
-      const int y = ytop + r;
-      Lp[r] = make_float2(0.0f, 0.0f);
-      gs[r] = make_float2(0.0f, 0.0f);
-      gw[r] = gm[r] = ge[r] = 0.0f;
-      if (y >= 0 && y < H) {
-        const float *gr = gp + (long long)y * pitch, *lr = lp + (long long)y * pitch;
-        float2 c = make_float2(0.0f, 0.0f), cb = make_float2(0.0f, 0.0f);
-        const bool below = y + 1 < H;
-        if (both) {
-          c = __ldg((const float2 *)(gr + x0));
-          Lp[r] = __ldg((const float2 *)(lr + x0));
-          if (below) cb = __ldg((const float2 *)(gr + pitch + x0));
-        } else if (x0in) {
-          c.x = __ldg(gr + x0);
-          Lp[r].x = __ldg(lr + x0);
-          if (below) cb.x = __ldg(gr + pitch + x0);
-        } else if (x1in) {
-          c.y = __ldg(gr + x0 + 1);
-          Lp[r].y = __ldg(lr + x0 + 1);
-          if (below) cb.y = __ldg(gr + pitch + x0 + 1);
-        }
-        if (x0in && x0 >= 1) gw[r] = __ldg(gr + x0 - 1) + c.x;
-        if (both) gm[r] = c.x + c.y;
-        if (x1in && x0 + 2 < W) ge[r] = c.y + __ldg(gr + x0 + 2);
-        if (below) {
-          if (x0in) gs[r].x = c.x + cb.x;
-          if (x1in) gs[r].y = c.y + cb.y;
-        }
-      }
-    }
-    gn0 = make_float2(0.0f, 0.0f);
-    if (ytop >= 1 && ytop < H) {
-      const float *ga = gp + (long long)(ytop - 1) * pitch, *gb = gp + (long long)ytop * pitch;
-      if (both) {
-        gn0 = f2add(__ldg((const float2 *)(ga + x0)), __ldg((const float2 *)(gb + x0)));
-      } else {
-        if (x0in) gn0.x = __ldg(ga + x0) + __ldg(gb + x0);
-        if (x1in) gn0.y = __ldg(ga + x0 + 1) + __ldg(gb + x0 + 1);
-      }
-    }
+      for (int k = 0; k < 4; k++) v[k] = (x0 + k >= 0 && x0 + k < W) ? __ldg(q + k) : 0.0f;
+      return make_float4(v[0], v[1], v[2], v[3]);
+    };
 #pragma unroll
-    for (int r = 0; r < RB; r++) st2(cur + (ly0 + r) * RW + lx0, Lp[r]);
-    __syncthreads();
+    for (int r = 0; r < 3; r++) {
+      const float4 l4 = row4(lp, ytop + r), g4 = row4(gp, ytop + r);
+      Lp[r][0] = l4.x;
+      Lp[r][1] = l4.y;
+      Lp[r][2] = l4.z;
+      Lp[r][3] = l4.w;
+      g[r][0] = g4.x;
+      g[r][1] = g4.y;
+      g[r][2] = g4.z;
+      g[r][3] = g4.w;
+    }
+    ga = row4(gp, ytop - 1);
+    gb = row4(gp, ytop + 3);
   }
+  float gh[3][5], gs[3][4], gn[4];
+  if (interior)
+    akz_fed_pairs<true>(g, ga, gb, x0, ytop, W, H, gh, gs, gn);
+  else
+    akz_fed_pairs<false>(g, ga, gb, x0, ytop, W, H, gh, gs, gn);
 
-  for (int s = p.first ? 1 : 0; s < d; s++) {
-    akz_fed_step<RW>(cur, nxt, p.h[s], lx0, ly0, Lp, gw, gm, ge, gs, gn0);
+  /* exchange rows: xb[((par * 2 + last) * 16 + warp) * RW + column] */
+  float *xb = sm;
+  auto put = [&](int par) {
+    *reinterpret_cast<float4 *>(xb + ((par * 2 + 0) * 16 + warp) * RW + lx0) = make_float4(Lp[0][0], Lp[0][1], Lp[0][2], Lp[0][3]);
+    *reinterpret_cast<float4 *>(xb + ((par * 2 + 1) * 16 + warp) * RW + lx0) = make_float4(Lp[2][0], Lp[2][1], Lp[2][2], Lp[2][3]);
+  };
+  if (d > 0) {
+    put(0);
     __syncthreads();
-    float *t = cur;
-    cur = nxt;
-    nxt = t;
   }
-  /* tile interior from registers, one 64-bit store per pair */
+  for (int s = 0; s < d; s++) {
+    const int par = s & 1;
+    const float4 above = warp > 0 ? *reinterpret_cast<const float4 *>(xb + ((par * 2 + 1) * 16 + warp - 1) * RW + lx0)
+                                  : make_float4(Lp[0][0], Lp[0][1], Lp[0][2], Lp[0][3]);
+    const float4 below = warp < 15 ? *reinterpret_cast<const float4 *>(xb + ((par * 2 + 0) * 16 + warp + 1) * RW + lx0)
+                                   : make_float4(Lp[2][0], Lp[2][1], Lp[2][2], Lp[2][3]);
+    akz_fed_step4(Lp, above, below, p.h[s], gh, gs, gn);
+    if (s + 1 < d) {
+      put(par ^ 1);
+      __syncthreads();
+    }
+  }
+  /* tile interior from registers, one 128-bit store per row */
   float *out = p.dst == 3 ? p.chk : planes + (p.dst == 0 ? L.lt : (p.dst == 1 ? I.t1 : I.t2));
-  const bool w0 = x0 >= tx0 && x0 < tx1, w1 = x0 + 1 < tx1;
-  if (w0) {
 #pragma unroll
-    for (int r = 0; r < RB; r++) {
-      const int y = ytop + r;
-      if (y >= ty0 && y < ty1) {
-        float *o = out + (long long)y * L.pitch + x0;
-        if (w1)
-          st2(o, Lp[r]);
-        else
-          o[0] = Lp[r].x;
-      }
+  for (int r = 0; r < 3; r++) {
+    const int y = ytop + r;
+    if (y < ty0 || y >= ty1) continue;
+    float *o = out + (long long)y * L.pitch + x0;
+    if (x0 >= tx0 && x0 + 4 <= tx1) {
+      *reinterpret_cast<float4 *>(o) = make_float4(Lp[r][0], Lp[r][1], Lp[r][2], Lp[r][3]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if (x0 + k >= tx0 && x0 + k < tx1) o[k] = Lp[r][k];
     }
   }
 }
