@@ -14,8 +14,11 @@
  *              extrema come out in (level, y, x) order, which is the order
  *              the reference's per-level bitonic sort gives (:884-939),
  *              with no per-level cap.
- *   k_extract  one warp per row: subpixel fit and record (:744-769), the
- *              determinant recomputed from Lx, Ly at the 3x3 neighbourhood.
+ *   k_extract  one warp per row: the raw extrema's positions in (level, y, x)
+ *              order at their scanned indices.
+ *   k_extract_fit  one thread per raw extremum of the batch: subpixel fit and
+ *              record (:744-769), the determinant recomputed from Lx, Ly at
+ *              the 3x3 neighbourhood.
  *   k_nms      one CTA per image: the reference's round-based suppression
  *              (:1005-1224) with an exact per-slot minimum (atomicMin), then
  *              the 2048-slot chunked emission and subpixel restore
@@ -439,13 +442,10 @@ __global__ void __launch_bounds__(256) k_extract(akz_extract_params p, int nrows
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const akz_image_desc I = p.t.im[L.image];
   const int y = r - sg.tile_begin;
-  const int W = L.width, H = L.height, st = L.deriv_step;
   const int words = L.bitmap_pitch;
   const uint32_t *row = p.bitmap + L.bitmap + (long long)y * words;
   const int rank0 = p.rowscan[L.rows + y];
   akz_raw *out = p.raw + I.raw_base;
-  const akz_plane_acc X{p.t.planes + L.lx, L.pitch}, Y{p.t.planes + L.ly, L.pitch};
-  const int ratio = 1 << L.octave;
   int running = 0;
   for (int w0 = 0; w0 < words; w0 += 32) {
     const int w = w0 + lane;
@@ -461,38 +461,78 @@ __global__ void __launch_bounds__(256) k_extract(akz_extract_params p, int nrows
     while (bits) {
       const int b = __ffs(bits) - 1;
       bits &= bits - 1;
-      const int x = w * 32 + b;
       const int idx = rank0 + k++;
       if (idx >= I.raw_cap) continue;
-      float D[3][3];
-      for (int j = -1; j <= 1; j++)
-        for (int i = -1; i <= 1; i++) D[j + 1][i + 1] = akz_det_at(X, Y, W, H, st, x + i, y + j, p.fac1, p.fac2);
-      const float v = D[1][1];
-      const float dx = 0.5f * (D[1][2] - D[1][0]);
-      const float dy = 0.5f * (D[2][1] - D[0][1]);
-      const float dxx = D[1][2] + D[1][0] - 2.0f * v;
-      const float dyy = D[2][1] + D[0][1] - 2.0f * v;
-      const float dxy = 0.25f * (D[2][2] + D[0][0] - D[2][0] - D[0][2]);
-      const float det = dxx * dyy - dxy * dxy;
-      const float idet = (det != 0.0f ? 1.0f / det : 0.0f);
-      const float dst0 = idet * (dxy * dy - dyy * dx);
-      const float dst1 = idet * (dxy * dx - dxx * dy);
-      const bool weak = !(dst0 >= -1.0f && dst0 <= 1.0f && dst1 >= -1.0f && dst1 <= 1.0f);
-      akz_raw e;
-      e.x = x;
-      e.y = y;
-      e.level = L.level;
-      e.octave = L.octave;
-      e.response = v;
-      e.size = (float)((weak ? -1 : 1) * 2.0 * (double)L.size);
-      const float octsub = (float)(dst0 < 0 ? -1 : 1) * ((float)L.octave + fabsf(dst0));
-      e.octsub = weak ? (float)L.octave : octsub;
-      e.dst1 = dst1;
-      out[idx] = e;
+      /* position only; k_extract_fit completes the record */
+      out[idx].x = w * 32 + b;
+      out[idx].y = y;
+      out[idx].level = L.level;
     }
     running += total;
   }
-  (void)ratio;
+}
+
+/* Subpixel fit of every raw extremum (cuda_akaze.cu:744-769), one thread
+ * each over the whole batch: the determinant recomputed from Lx, Ly at the
+ * 3x3 neighbourhood, its gradient and Hessian, the offset (dst0, dst1) and
+ * the record. */
+__global__ void __launch_bounds__(256) k_extract_fit(akz_extract_params p)
+{
+  __shared__ int sOff[AKZ_FIT_MAXIMG + 1]; /* raw extrema before each image (capped at each image's capacity) */
+  const int nimg = p.t.nimg;
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int i = 0; i < nimg; i++) {
+      sOff[i] = acc;
+      acc += min(p.t.stats[i].nraw, p.t.im[i].raw_cap);
+    }
+    sOff[nimg] = acc;
+  }
+  __syncthreads();
+  const int total = sOff[nimg];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    int lo = 0, hi = nimg - 1; /* last image with sOff <= g */
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sOff[mid] <= g)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const akz_image_desc I = p.t.im[lo];
+    akz_raw *rec = p.raw + I.raw_base + (g - sOff[lo]);
+    const int x = rec->x, y = rec->y;
+    const akz_level_desc L = p.t.lv[I.first_level + rec->level];
+    const int W = L.width, H = L.height, st = L.deriv_step;
+    const akz_plane_acc X{p.t.planes + L.lx, L.pitch}, Y{p.t.planes + L.ly, L.pitch};
+    float D[3][3];
+#pragma unroll
+    for (int j = -1; j <= 1; j++)
+#pragma unroll
+      for (int i = -1; i <= 1; i++) D[j + 1][i + 1] = akz_det_at(X, Y, W, H, st, x + i, y + j, p.fac1, p.fac2);
+    const float v = D[1][1];
+    const float dx = 0.5f * (D[1][2] - D[1][0]);
+    const float dy = 0.5f * (D[2][1] - D[0][1]);
+    const float dxx = D[1][2] + D[1][0] - 2.0f * v;
+    const float dyy = D[2][1] + D[0][1] - 2.0f * v;
+    const float dxy = 0.25f * (D[2][2] + D[0][0] - D[2][0] - D[0][2]);
+    const float det = dxx * dyy - dxy * dxy;
+    const float idet = (det != 0.0f ? 1.0f / det : 0.0f);
+    const float dst0 = idet * (dxy * dy - dyy * dx);
+    const float dst1 = idet * (dxy * dx - dxx * dy);
+    const bool weak = !(dst0 >= -1.0f && dst0 <= 1.0f && dst1 >= -1.0f && dst1 <= 1.0f);
+    akz_raw e;
+    e.x = x;
+    e.y = y;
+    e.level = L.level;
+    e.octave = L.octave;
+    e.response = v;
+    e.size = (float)((weak ? -1 : 1) * 2.0 * (double)L.size);
+    const float octsub = (float)(dst0 < 0 ? -1 : 1) * ((float)L.octave + fabsf(dst0));
+    e.octsub = weak ? (float)L.octave : octsub;
+    e.dst1 = dst1;
+    *rec = e;
+  }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -804,6 +844,13 @@ cudaError_t akz_launch_extract(const akz_extract_params &p, int nrows, cudaStrea
   if (nrows <= 0) return cudaSuccess;
   const int warps_per_block = 8;
   k_extract<<<(nrows + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, s>>>(p, nrows);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (p.t.nimg > AKZ_FIT_MAXIMG) return cudaErrorInvalidValue;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  k_extract_fit<<<8 * std::max(nsm, 1), 256, 0, s>>>(p);
   return cudaGetLastError();
 }
 

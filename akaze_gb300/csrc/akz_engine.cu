@@ -408,6 +408,7 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
   akz_status st = akz_validate(opt);
   if (st != AKZ_OK) return st;
   if (n < 1 || !Ws || !Hs || !out) return akz_fail(AKZ_ERR_INVALID_ARG, "batch needs at least one image and size arrays");
+  if (n > AKZ_FIT_MAXIMG) return akz_fail(AKZ_ERR_INVALID_ARG, "a batch holds at most %d images", AKZ_FIT_MAXIMG);
   akz_batch *b = new (std::nothrow) akz_batch();
   if (!b) return akz_fail(AKZ_ERR_OOM, "host allocation failed");
   b->opt = *opt;

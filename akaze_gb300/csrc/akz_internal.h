@@ -22,7 +22,8 @@
 #define AKZ_MAX_LEVELS 64
 #define AKZ_MAX_NBINS 4096
 #define AKZ_NMS_THREADS 512
-#define AKZ_NMS_CL 8 /* CTAs per image in the suppression kernel (a thread-block cluster) */
+#define AKZ_NMS_CL 8
+#define AKZ_FIT_MAXIMG 4096 /* images of one batch the fit kernel indexes */ /* CTAs per image in the suppression kernel (a thread-block cluster) */
 #define AKZ_NMS_NB 8 /* neighbour list capacity per raw extremum */
 
 /* One (image, level). */

@@ -156,8 +156,8 @@ AKZ_API akz_status akz_get_extrema(akz_context *ctx, akz_extremum *out, int capa
 
 /* ---- many images per launch (persistent, graph-replayed stages) -------- */
 
-/* A batch of nimages images of the given sizes (each >= 8x8), processed by
- * one launch per stage. */
+/* A batch of nimages images (1 .. 4096) of the given sizes (each >= 8x8),
+ * processed by one launch per stage. */
 AKZ_API akz_status akz_batch_create(const akz_options *opt, int nimages, const int *widths, const int *heights, akz_batch **out);
 AKZ_API akz_status akz_batch_destroy(akz_batch *b);
 AKZ_API akz_status akz_batch_set_stream(akz_batch *b, void *stream);
