@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
     const akz_kp kp = *kpp;
     const akz_level_desc L = p.t.lv[I.first_level + kp.class_id];
     const int W = L.width, H = L.height, pitch = L.pitch;
-    const float *lxp = p.t.planes + L.lx, *lyp = p.t.planes + L.ly, *ltp = p.t.planes + L.lt;
+    const float *lxyp = p.t.planes + L.lx, *ltp = p.t.planes + L.lt; /* (Lx, Ly) interleaved, row pitch 2 * pitch */
     float angle = 0.0f;
     if (!p.upright) {
       const int octave = kp.octave;
@@ -213,9 +213,9 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
           const int ij = sOrIJ[s];
           const int sx = akz_clampi(x + step * (int)(short)(ij & 0xffff), 0, W - 1);
           const int sy = akz_clampi(y + step * (ij >> 16), 0, H - 1);
-          const long long pos = (long long)sy * pitch + sx;
-          gxv[it] = __ldg(lxp + pos);
-          gyv[it] = __ldg(lyp + pos);
+          const float2 g2 = __ldg(reinterpret_cast<const float2 *>(lxyp + (long long)sy * (2 * pitch) + 2 * sx));
+          gxv[it] = g2.x;
+          gyv[it] = g2.y;
         }
       }
       /* per bin, a 109-bit mask of its samples (4 words in the third
@@ -329,10 +329,10 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
           int yp = (int)(yf + fs * ((float)kk * si + (float)l * co) + 0.5f);
           xp = akz_clampi(xp, 0, W - 1);
           yp = akz_clampi(yp, 0, H - 1);
-          const long long pos = (long long)yp * pitch + xp;
-          vi[it] = __ldg(ltp + pos);
-          vx[it] = __ldg(lxp + pos);
-          vy[it] = __ldg(lyp + pos);
+          vi[it] = __ldg(ltp + (long long)yp * pitch + xp);
+          const float2 g2 = __ldg(reinterpret_cast<const float2 *>(lxyp + (long long)yp * (2 * pitch) + 2 * xp));
+          vx[it] = g2.x;
+          vy[it] = g2.y;
         }
       }
 #pragma unroll
@@ -352,9 +352,9 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
       const int l = xx - size2, kk = yy - size2;
       const int xp = akz_clampi((int)(xf + fs * ((float)kk * co - (float)l * si) + 0.5f), 0, W - 1);
       const int yp = akz_clampi((int)(yf + fs * ((float)kk * si + (float)l * co) + 0.5f), 0, H - 1);
-      const long long pos = (long long)yp * pitch + xp;
-      const float dx = __ldg(lxp + pos), dy = __ldg(lyp + pos);
-      S.s[0][s] = __ldg(ltp + pos);
+      const float2 g2 = __ldg(reinterpret_cast<const float2 *>(lxyp + (long long)yp * (2 * pitch) + 2 * xp));
+      const float dx = g2.x, dy = g2.y;
+      S.s[0][s] = __ldg(ltp + (long long)yp * pitch + xp);
       S.s[1][s] = -dx * si + dy * co;
       S.s[2][s] = dx * co + dy * si;
     }

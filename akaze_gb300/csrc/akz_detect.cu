@@ -135,7 +135,7 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
   float *sS = sm, *sX = sS + NS * SW, *sY = sX + ND * 128, *sE = sY + ND * 128;
   const float fac1 = p.fac1, fac2 = p.fac2;
   const float *ls = p.t.planes + L.ls;
-  float *lxp = p.t.planes + L.lx, *lyp = p.t.planes + L.ly;
+  float *lxyp = p.t.planes + L.lx; /* interleaved (Lx, Ly), row pitch 2 * pitch */
   const long long pitch = L.pitch;
 
   int xs[SJ]; /* source column of this lane's S columns lane + 32 j */
@@ -171,14 +171,11 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
       st2(oy + d, b);
       const int x = tx0 - A + d; /* even */
       if (wrow && d >= A && d < A + TW && x < W) {
-        float *gx = lxp + (long long)r * pitch + x, *gy = lyp + (long long)r * pitch + x;
-        if (x + 1 < W) {
-          st2(gx, a);
-          st2(gy, b);
-        } else {
-          gx[0] = a.x;
-          gy[0] = b.x;
-        }
+        float *o = lxyp + (long long)r * (2 * pitch) + 2 * x; /* x even: 16-byte aligned */
+        if (x + 1 < W)
+          *reinterpret_cast<float4 *>(o) = make_float4(a.x, b.x, a.y, b.y);
+        else
+          st2(o, make_float2(a.x, b.x));
       }
     }
   };
@@ -315,7 +312,7 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   for (int y = sy0 + warp; y < sy1; y += 8)
     for (int x = sx0 + lane; x < sx1; x += 32) sS[(y - sy0) * sw + (x - sx0)] = __ldg(ls + (long long)y * L.pitch + x);
   __syncthreads();
-  float *lxp = p.t.planes + L.lx, *lyp = p.t.planes + L.ly;
+  float *lxyp = p.t.planes + L.lx; /* interleaved (Lx, Ly), row pitch 2 * pitch */
   const float fac1 = p.fac1, fac2 = p.fac2;
   /* Lx, Ly on the tile +- (step+1): scaled Scharr with step sigma_size and
    * reflect-101 offsets (cuda_akaze.cu:651-671) */
@@ -334,10 +331,7 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
       const float b = fac1 * (lr + ll - ur - ul) + fac2 * (lc - uc);
       ox[x] = a;
       oy[x] = b;
-      if (yt && x >= tx0 && x < tx1) {
-        lxp[(long long)y * L.pitch + x] = a;
-        lyp[(long long)y * L.pitch + x] = b;
-      }
+      if (yt && x >= tx0 && x < tx1) st2(lxyp + (long long)y * (2 * L.pitch) + 2 * x, make_float2(a, b));
     }
   }
   __syncthreads();
@@ -504,12 +498,13 @@ __global__ void __launch_bounds__(256) k_extract_fit(akz_extract_params p)
     const int x = rec->x, y = rec->y;
     const akz_level_desc L = p.t.lv[I.first_level + rec->level];
     const int W = L.width, H = L.height, st = L.deriv_step;
-    const akz_plane_acc X{p.t.planes + L.lx, L.pitch}, Y{p.t.planes + L.ly, L.pitch};
+    const float *lxy = p.t.planes + L.lx;
+    const long long pitch2 = 2LL * L.pitch;
     float D[3][3];
 #pragma unroll
     for (int j = -1; j <= 1; j++)
 #pragma unroll
-      for (int i = -1; i <= 1; i++) D[j + 1][i + 1] = akz_det_at(X, Y, W, H, st, x + i, y + j, p.fac1, p.fac2);
+      for (int i = -1; i <= 1; i++) D[j + 1][i + 1] = akz_det_at2(lxy, pitch2, W, H, st, x + i, y + j, p.fac1, p.fac2);
     const float v = D[1][1];
     const float dx = 0.5f * (D[1][2] - D[1][0]);
     const float dy = 0.5f * (D[2][1] - D[0][1]);

@@ -89,6 +89,25 @@ __device__ __forceinline__ float akz_det_at(const A &lx, const A &ly, int W, int
   return lxx * lyy - lyx * lyx;
 }
 
+/* Hessian determinant at (x, y) from the interleaved (Lx, Ly) plane lxy
+ * (row pitch pitch2 floats): the expressions of akz_det_at, each tap's pair
+ * read with one 64-bit load. */
+__device__ __forceinline__ float akz_det_at2(const float *lxy, long long pitch2, int W, int H, int step, int x, int y,
+                                             float fac1, float fac2)
+{
+  const int xl = x < step ? step - x : x - step;
+  const int xh = x >= W - step ? 2 * W - x - step - 2 : x + step;
+  const int yl = y < step ? step - y : y - step;
+  const int yh = y >= H - step ? 2 * H - y - step - 2 : y + step;
+  auto at = [&](int xx, int yy) { return __ldg(reinterpret_cast<const float2 *>(lxy + yy * pitch2 + 2 * xx)); };
+  const float2 ul = at(xl, yl), ur = at(xh, yl), ll = at(xl, yh), lr = at(xh, yh);
+  const float2 cl = at(xl, y), cr = at(xh, y), uc = at(x, yl), lc = at(x, yh);
+  const float lxx = fac1 * (ur.x + lr.x - ul.x - ll.x) + fac2 * (cr.x - cl.x);
+  const float lyx = fac1 * (lr.x + ll.x - ur.x - ul.x) + fac2 * (lc.x - uc.x);
+  const float lyy = fac1 * (lr.y + ll.y - ur.y - ul.y) + fac2 * (lc.y - uc.y);
+  return lxx * lyy - lyx * lyx;
+}
+
 /* Packed FP32x2 additions (sm_100+ add/sub .f32x2): two independent IEEE
  * float additions per instruction, each rounded exactly like the scalar one.
  * There is deliberately no packed multiply: the assembler of CUDA 13.0

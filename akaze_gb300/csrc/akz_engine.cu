@@ -493,10 +493,9 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
         L.ls = (long long)plane_floats;
         plane_floats += pf;
       }
-      L.lx = (long long)plane_floats;
-      plane_floats += pf;
-      L.ly = (long long)plane_floats;
-      plane_floats += pf;
+      L.lx = (long long)plane_floats; /* Lx, Ly interleaved: (Lx, Ly) pairs, row pitch 2 * pitch */
+      L.ly = L.lx + 1;
+      plane_floats += 2 * pf;
       L.rows = rows + rt;
       rt += g.h;
       L.bitmap_pitch = (g.w + 31) / 32;
@@ -1211,8 +1210,17 @@ static akz_status akz_plane_out(akz_batch *b, int i, int level, int plane, float
   switch (plane) {
     case AKZ_PLANE_LT: off = L.lt; break;
     case AKZ_PLANE_LSMOOTH: off = L.ls; break;
-    case AKZ_PLANE_LX: off = L.lx; break;
-    case AKZ_PLANE_LY: off = L.ly; break;
+    case AKZ_PLANE_LX:
+    case AKZ_PLANE_LY: {
+      /* the interleaved (Lx, Ly) plane, split on the host */
+      std::vector<float> tmp((size_t)2 * L.width * L.height);
+      CK(cudaMemcpy2DAsync(tmp.data(), (size_t)L.width * 8, b->planes + L.lx, (size_t)L.pitch * 8, (size_t)L.width * 8,
+                           L.height, cudaMemcpyDeviceToHost, b->stream));
+      CK(cudaStreamSynchronize(b->stream));
+      const int k = plane == AKZ_PLANE_LY ? 1 : 0;
+      for (size_t q = 0; q < (size_t)L.width * L.height; q++) out[q] = tmp[2 * q + k];
+      return AKZ_OK;
+    }
     default: return akz_fail(AKZ_ERR_INVALID_ARG, "unknown plane %d", plane);
   }
   CK(cudaMemcpy2DAsync(out, (size_t)L.width * 4, b->planes + off, (size_t)L.pitch * 4, (size_t)L.width * 4, L.height,

@@ -33,7 +33,8 @@ struct akz_level_desc {
   int deriv_step;           /* detector step sigma_size */
   float border;             /* extrema border */
   float size;               /* esigma * derivative_factor */
-  long long lt, ls, lx, ly; /* float offsets into the plane arena */
+  long long lt, ls, lx, ly; /* float offsets into the plane arena; Lx and Ly are one interleaved
+                             * plane of (Lx, Ly) pairs with row pitch 2 * pitch (ly = lx + 1) */
   long long rows;           /* offset of this level's rows in the row-count arrays */
   long long bitmap;         /* word offset of the bitmap */
   int bitmap_pitch;         /* 32-bit words per row */
