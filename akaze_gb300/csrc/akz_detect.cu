@@ -130,8 +130,10 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
   constexpr int SJ = (SW + 31) / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int W = L.width, H = L.height;
+  constexpr int BH = ST == 3 ? 6 : 8; /* rows per block: pairs (o, o + ST) tile it */
+  static_assert(BH % (2 * ST) == 0, "row pairs tile the block");
   const int ch = min(AKZ_STRIP_CH, H - ty0); /* rows of this CTA */
-  const int iters = (ch + 7) >> 3;
+  const int iters = (ch + BH - 1) / BH;
   float *sS = sm, *sX = sS + NS * SW, *sY = sX + ND * 128, *sE = sY + ND * 128;
   const float fac1 = p.fac1, fac2 = p.fac2;
   const float *ls = p.t.planes + L.ls;
@@ -205,6 +207,72 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
       st2(o + e, f2sub(make_float2(lxx.x * lyy.x, lxx.y * lyy.y), make_float2(lyx.x * lyx.x, lyx.y * lyx.y)));
     }
   };
+  /* a centre tap of a ring row: a pair, or two floats for odd ST */
+  auto tap = [&](const float *row, int c) -> float2 { return (ST & 1) ? make_float2(row[c], row[c + 1]) : ld2(row + c); };
+  /* Lx, Ly rows rA and rA + ST for column pair d: the two share their
+   * middle Lsmooth rows, 12 pair loads instead of 16 */
+  auto comp_d2 = [&](int rA, int d) {
+    const float *s0 = sS + ((rA - ST) & (NS - 1)) * SW, *s1 = sS + (rA & (NS - 1)) * SW,
+                *s2 = sS + ((rA + ST) & (NS - 1)) * SW, *s3 = sS + ((rA + 2 * ST) & (NS - 1)) * SW;
+    const float2 L0 = ld2(s0 + d), C0 = tap(s0, d + ST), R0 = ld2(s0 + d + 2 * ST);
+    const float2 L1 = ld2(s1 + d), C1 = tap(s1, d + ST), R1 = ld2(s1 + d + 2 * ST);
+    const float2 L2 = ld2(s2 + d), C2 = tap(s2, d + ST), R2 = ld2(s2 + d + 2 * ST);
+    const float2 L3 = ld2(s3 + d), C3 = tap(s3, d + ST), R3 = ld2(s3 + d + 2 * ST);
+    const int x = tx0 - A + d; /* even */
+    const bool wcol = d >= A && d < A + TW && x < W;
+#pragma unroll
+    for (int t = 0; t < 2; t++) { /* row rA (u, c, d = rows 0, 1, 2), row rA + ST (rows 1, 2, 3) */
+      const float2 ul = t ? L1 : L0, uc = t ? C1 : C0, ur = t ? R1 : R0;
+      const float2 cl = t ? L2 : L1, cr = t ? R2 : R1;
+      const float2 ll = t ? L3 : L2, lc = t ? C3 : C2, lr = t ? R3 : R2;
+      const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
+      const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(lc, uc);
+      const float2 a = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
+      const float2 b = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+      const int r = rA + t * ST;
+      st2(sX + (r & (ND - 1)) * 128 + d, a);
+      st2(sY + (r & (ND - 1)) * 128 + d, b);
+      if (wcol && r >= ty0 && r < ty0 + ch) {
+        float *o = lxyp + (long long)r * (2 * pitch) + 2 * x; /* x even: 16-byte aligned */
+        if (x + 1 < W)
+          *reinterpret_cast<float4 *>(o) = make_float4(a.x, b.x, a.y, b.y);
+        else
+          st2(o, make_float2(a.x, b.x));
+      }
+    }
+  };
+  /* determinant rows rA and rA + ST for E pair q: they share two Lx rows */
+  auto comp_e2 = [&](int rA, int q) {
+    if (q >= NEP) return;
+    const int e = 2 * q, d = e + EO + A; /* centre D column */
+    const float *x0 = sX + ((rA - ST) & (ND - 1)) * 128, *x1 = sX + (rA & (ND - 1)) * 128,
+                *x2 = sX + ((rA + ST) & (ND - 1)) * 128, *x3 = sX + ((rA + 2 * ST) & (ND - 1)) * 128;
+    const float *y0 = sY + ((rA - ST) & (ND - 1)) * 128, *y1 = sY + (rA & (ND - 1)) * 128,
+                *y2 = sY + ((rA + ST) & (ND - 1)) * 128, *y3 = sY + ((rA + 2 * ST) & (ND - 1)) * 128;
+    const float2 XL0 = ld2(x0 + d - ST), XC0 = tap(x0, d), XR0 = ld2(x0 + d + ST);
+    const float2 XL1 = ld2(x1 + d - ST), XC1 = tap(x1, d), XR1 = ld2(x1 + d + ST);
+    const float2 XL2 = ld2(x2 + d - ST), XC2 = tap(x2, d), XR2 = ld2(x2 + d + ST);
+    const float2 XL3 = ld2(x3 + d - ST), XC3 = tap(x3, d), XR3 = ld2(x3 + d + ST);
+    const float2 YL0 = ld2(y0 + d - ST), YC0 = tap(y0, d), YR0 = ld2(y0 + d + ST);
+    const float2 YL1 = ld2(y1 + d - ST), YC1 = tap(y1, d), YR1 = ld2(y1 + d + ST);
+    const float2 YL2 = ld2(y2 + d - ST), YC2 = tap(y2, d), YR2 = ld2(y2 + d + ST);
+    const float2 YL3 = ld2(y3 + d - ST), YC3 = tap(y3, d), YR3 = ld2(y3 + d + ST);
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      const float2 ul = t ? XL1 : XL0, ur = t ? XR1 : XR0, ll = t ? XL3 : XL2, lr = t ? XR3 : XR2;
+      const float2 cl = t ? XL2 : XL1, cr = t ? XR2 : XR1, xuc = t ? XC1 : XC0, xdc = t ? XC3 : XC2;
+      const float2 vul = t ? YL1 : YL0, vur = t ? YR1 : YR0, vll = t ? YL3 : YL2, vlr = t ? YR3 : YR2;
+      const float2 yuc = t ? YC1 : YC0, ydc = t ? YC3 : YC2;
+      const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
+      const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(xdc, xuc);
+      const float2 lxx = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
+      const float2 lyx = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+      const float2 cy = f2sub(f2sub(f2add(vlr, vll), vur), vul), dy = f2sub(ydc, yuc);
+      const float2 lyy = f2add(make_float2(fac1 * cy.x, fac1 * cy.y), make_float2(fac2 * dy.x, fac2 * dy.y));
+      st2(sE + ((rA + t * ST) & (NE - 1)) * EW + e,
+          f2sub(make_float2(lxx.x * lyy.x, lxx.y * lyy.y), make_float2(lyx.x * lyx.x, lyx.y * lyx.y)));
+    }
+  };
   const int xlo = max(akz_border_lo(L.border), tx0), xhi = min(akz_border_hi(L.border, W), tx0 + TW - 1);
   const int ylo = max(akz_border_lo(L.border), ty0), yhi = min(akz_border_hi(L.border, H), ty0 + ch - 1);
   auto maxima = [&](int y) {
@@ -232,22 +300,25 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
   akz_cp_async_commit();
   akz_cp_async_wait_all();
   __syncthreads();
-  for (int r = ty0 + 2 * ST + 1 + warp; r <= ty0 + 2 * ST + 8; r += 8) load_s(r);
+  if (warp < BH) load_s(ty0 + 2 * ST + 1 + warp);
   akz_cp_async_commit();
   for (int r = ty0 - 1 - ST + warp; r <= ty0 + ST; r += 8) comp_d(r);
   __syncthreads();
   if (warp < 2) comp_e(ty0 - 1 + warp);
+  /* blocks of BH rows; warp w < BH takes row pair (o, o + ST) of the block,
+   * o = (q / ST) 2 ST + q % ST with q = w / 2, and column half w % 2 */
+  const int q = warp >> 1, half = warp & 1, o = (q / ST) * 2 * ST + q % ST;
   for (int k = 0; k < iters; k++) {
-    const int r = ty0 + 8 * k;
+    const int r = ty0 + BH * k;
     akz_cp_async_wait_all();
-    __syncthreads(); /* S rows up to r+8+2ST landed; E rows up to r visible */
-    if (k + 1 < iters) load_s(r + 2 * ST + 9 + warp);
+    __syncthreads(); /* S rows up to r+BH+2ST landed; E rows up to r visible */
+    if (k + 1 < iters && warp < BH) load_s(r + 2 * ST + BH + 1 + warp);
     akz_cp_async_commit();
-    comp_d(r + ST + 1 + warp);
+    if (warp < BH) comp_d2(r + ST + 1 + o, 2 * (32 * half + lane));
     __syncthreads();
-    comp_e(r + 1 + warp);
+    if (warp < BH) comp_e2(r + 1 + o, 32 * half + lane);
     __syncthreads();
-    maxima(r + warp);
+    if (warp < BH) maxima(r + warp);
   }
   akz_cp_async_wait_all();
 }
