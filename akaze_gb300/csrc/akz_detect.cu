@@ -326,7 +326,7 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
 __global__ void __launch_bounds__(256) k_detect_strip(akz_detect_params p)
 {
   extern __shared__ float sm[];
-  const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
+  const int si = akz_find_seg_warp(p.segs, p.nsegs, blockIdx.x);
   const akz_tile_seg sg = p.segs[si];
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const int st = L.deriv_step;
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
   constexpr int TW = AKZ_DETECT_TW, TH = AKZ_DETECT_TH;
   extern __shared__ float sm[];
   const int tid = threadIdx.x;
-  const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
+  const int si = akz_find_seg_warp(p.segs, p.nsegs, blockIdx.x);
   const akz_tile_seg sg = p.segs[si];
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const int W = L.width, H = L.height, st = L.deriv_step;
@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(256) k_extract(akz_extract_params p, int nrows
   const int lane = threadIdx.x & 31;
   const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (r >= nrows) return;
-  const int si = akz_find_seg(p.segs, p.nsegs, r);
+  const int si = akz_find_seg_warp(p.segs, p.nsegs, r);
   const akz_tile_seg sg = p.segs[si];
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const akz_image_desc I = p.t.im[L.image];

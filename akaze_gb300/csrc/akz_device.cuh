@@ -39,6 +39,24 @@ __device__ __forceinline__ int akz_find_seg(const akz_tile_seg *segs, int nsegs,
   return lo;
 }
 
+/* akz_find_seg as a 32-way search by the (full) warp: each round every lane
+ * reads one segment start, so up to 32 segments cost one load round trip and
+ * up to 1024 two, instead of a chain of log2(nsegs) dependent loads. */
+__device__ __forceinline__ int akz_find_seg_warp(const akz_tile_seg *segs, int nsegs, int t)
+{
+  const int lane = threadIdx.x & 31;
+  int lo = 0, n = nsegs; /* the answer lies in [lo, lo + n); segs[lo] starts at or before t */
+  while (n > 32) {
+    const int stride = (n + 31) >> 5, i = lo + lane * stride;
+    const int c = __popc(__ballot_sync(0xffffffffu, i < lo + n && __ldg(&segs[i].tile_begin) <= t));
+    const int nlo = lo + (c - 1) * stride; /* starts are sorted: the lanes at or below t form a prefix */
+    n = min(stride, lo + n - nlo);
+    lo = nlo;
+  }
+  const int i = lo + lane;
+  return lo + __popc(__ballot_sync(0xffffffffu, i < lo + n && __ldg(&segs[i].tile_begin) <= t)) - 1;
+}
+
 /* Input pixel of image img as float in [0,1]: u8 * (float)(1/255) or f32.
  * Both staging arrays use the same element offsets and pitches. */
 __device__ __forceinline__ float akz_fetch_input(const akz_tables &t, const akz_image_desc &I, int x, int y, float inv255)

@@ -1448,10 +1448,11 @@ AKZ_API akz_status akz_batch_level_plane(akz_batch *b, int i, int level, int pla
 /* Number of kernels one akz_batch_run launches. */
 static int akz_batch_nkernels(const akz_batch *b)
 {
-  /* level 0 + contrast: k_level0, k_contrast_hist, k_contrast_final (radius <= 4),
-   * else k_contrast x2, k_contrast_final, k_gauss0; then the detector
-   * (strip and/or tile kernel), scan, extract, nms, describe */
-  int n = (b->R0 <= 4 ? 3 : 4) + 4 + (b->strip_tiles > 0) + (b->detect_tiles > 0);
+  /* level 0 + contrast: k_level0, k_contrast_hist, k_contrast_final
+   * (radius <= 4), else k_contrast x2, k_contrast_final, k_gauss0; then the
+   * detector (strip and/or tile kernel), k_rowscan, k_extract, k_extract_fit,
+   * k_nms, k_describe */
+  int n = (b->R0 <= 4 ? 3 : 4) + 5 + (b->strip_tiles > 0) + (b->detect_tiles > 0);
   for (int l = 1; l < b->maxlev; l++) {
     n += b->area[l].nsegs > 0 ? 1 : 0;
     if (b->sg_on && l / b->opt.nsublevels >= b->sg_first_octave) {

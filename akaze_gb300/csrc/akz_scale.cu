@@ -172,13 +172,11 @@ __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
   constexpr int TW = AKZ_L0_TW, TH = AKZ_L0_TH;
   constexpr int PW = TW + 8, PH = TH + 8;  /* input: tile +- 4 */
   constexpr int BW = TW + 2, BH = TH + 6;  /* sigma-1 rows pass: cols tile +- 1, rows tile +- 3 */
-  constexpr int CH = TH + 2;               /* sigma-1 columns pass: rows tile +- 1 */
   extern __shared__ __align__(16) float l0sm[];
   float *sP = l0sm, *sA = sP + PH * PW, *sB = sA + PH * TW;
-  float *sC = sP; /* the input region is dead after both rows passes */
   __shared__ float sRed[8];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
+  const int si = akz_find_seg_warp(p.segs, p.nsegs, blockIdx.x);
   const akz_tile_seg sg = p.segs[si];
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const akz_image_desc I = p.t.im[L.image];
@@ -213,8 +211,9 @@ __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
     }
   }
   __syncthreads();
-  /* rows passes: soffset Gaussian on tile columns (all PH rows), sigma-1 on
-   * columns tile +- 1, rows tile +- 3 */
+  /* rows passes from one window per column pair: soffset Gaussian on tile
+   * columns (all PH rows), sigma-1 on the same columns for rows tile +- 3
+   * (sB column d is x = tx0 - 1 + d, sB row r is sP row r + 1) */
   const float t0 = p.taps0[0], t1 = p.taps0[1], t2 = p.taps0[2], t3 = p.taps0[3], t4 = p.taps0[4];
   const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
   for (int i = tid; i < PH * (TW / 2); i += 256) {
@@ -231,82 +230,110 @@ __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
     acc = f2add(acc, make_float2(t3 * s35.x, t3 * s35.y));
     acc = f2add(acc, make_float2(t4 * A2.x, t4 * A2.y));
     st2(sA + r * TW + c, acc);
+    if (r >= 1 && r <= BH) { /* sigma 1 at x = tx0 + c, c + 1: taps sP columns c + 2 .. c + 7 */
+      const float2 s15 = s26, s24 = s35;
+      float2 g = make_float2(k0 * s15.x, k0 * s15.y);
+      g = f2add(g, make_float2(k1 * s24.x, k1 * s24.y));
+      g = f2add(g, make_float2(k2 * A2.x, k2 * A2.y));
+      float *o = sB + (r - 1) * BW + c + 1;
+      o[0] = g.x;
+      o[1] = g.y;
+    }
   }
-  for (int i = tid; i < BH * (BW / 2); i += 256) {
-    const int r = i / (BW / 2), d = 2 * (i - r * (BW / 2));
-    const float *q = sP + (r + 1) * PW + d; /* sB column d is x = tx0 - 1 + d, sP column d + 3 */
-    const float2 B0 = ld2(q), B1 = ld2(q + 2), B2 = ld2(q + 4), B3 = ld2(q + 6);
-    const float2 s15 = f2add(make_float2(B0.y, B1.x), make_float2(B2.y, B3.x));
-    const float2 s24 = f2add(B1, B2);
-    float2 acc = make_float2(k0 * s15.x, k0 * s15.y);
-    acc = f2add(acc, make_float2(k1 * s24.x, k1 * s24.y));
-    acc = f2add(acc, make_float2(k2 * B1.y, k2 * B2.x));
-    st2(sB + r * BW + d, acc);
+  if (tid < 2 * BH) { /* sigma 1 at the two columns outside the tile, x = tx0 - 1 and tx0 + TW */
+    const int r = tid >> 1, d = (tid & 1) ? BW - 1 : 0;
+    const float *q = sP + (r + 1) * PW + d + 3; /* centre */
+    float g = k0 * (q[-2] + q[2]);
+    g = g + k1 * (q[-1] + q[1]);
+    g = g + k2 * q[0];
+    sB[r * BW + d] = g;
   }
   __syncthreads();
-  /* columns passes: Lt0 for the tile (to HBM), sigma-1 rows tile +- 1 */
+  /* columns passes, 8 rows x one column pair per thread: Lt0 for the tile
+   * (to HBM); the sigma-1 image of rows y - 1 .. y + 8 on columns x - 1 ..
+   * x + 2 from sB rows y - 3 .. y + 10, and from it the Scharr gradient
+   * magnitude^2 at interior pixels */
+  float mx = 0.0f;
   {
     const int c = 2 * (tid & 63), g = tid >> 6; /* 64 column pairs x 4 groups of 8 rows */
     const int x = tx0 + c;
     float *out = p.t.planes + L.lt;
-    float2 v[16];
+    {
+      float2 v[16];
 #pragma unroll
-    for (int j = 0; j < 16; j++) v[j] = ld2(sA + (g * 8 + j) * TW + c);
+      for (int j = 0; j < 16; j++) v[j] = ld2(sA + (g * 8 + j) * TW + c);
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const float2 s08 = f2add(v[j], v[j + 8]), s17 = f2add(v[j + 1], v[j + 7]);
-      const float2 s26 = f2add(v[j + 2], v[j + 6]), s35 = f2add(v[j + 3], v[j + 5]);
-      float2 acc = make_float2(t0 * s08.x, t0 * s08.y);
-      acc = f2add(acc, make_float2(t1 * s17.x, t1 * s17.y));
-      acc = f2add(acc, make_float2(t2 * s26.x, t2 * s26.y));
-      acc = f2add(acc, make_float2(t3 * s35.x, t3 * s35.y));
-      acc = f2add(acc, make_float2(t4 * v[j + 4].x, t4 * v[j + 4].y));
-      const int y = ty0 + g * 8 + j;
-      if (y < H) {
-        float *o = out + (long long)y * L.pitch + x;
-        if (x + 1 < W)
-          st2(o, acc);
-        else if (x < W)
-          o[0] = acc.x;
+      for (int j = 0; j < 8; j++) {
+        const float2 s08 = f2add(v[j], v[j + 8]), s17 = f2add(v[j + 1], v[j + 7]);
+        const float2 s26 = f2add(v[j + 2], v[j + 6]), s35 = f2add(v[j + 3], v[j + 5]);
+        float2 acc = make_float2(t0 * s08.x, t0 * s08.y);
+        acc = f2add(acc, make_float2(t1 * s17.x, t1 * s17.y));
+        acc = f2add(acc, make_float2(t2 * s26.x, t2 * s26.y));
+        acc = f2add(acc, make_float2(t3 * s35.x, t3 * s35.y));
+        acc = f2add(acc, make_float2(t4 * v[j + 4].x, t4 * v[j + 4].y));
+        const int y = ty0 + g * 8 + j;
+        if (y < H) {
+          float *o = out + (long long)y * L.pitch + x;
+          if (x + 1 < W)
+            st2(o, acc);
+          else if (x < W)
+            o[0] = acc.x;
+        }
       }
     }
-  }
-  for (int i = tid; i < CH * (BW / 2); i += 256) {
-    const int r = i / (BW / 2), d = 2 * (i - r * (BW / 2));
-    const float *q = sB + r * BW + d; /* sC row r is y = ty0 - 1 + r, sB rows r .. r + 4 */
-    const float2 a = ld2(q), b = ld2(q + BW), c = ld2(q + 2 * BW), e = ld2(q + 3 * BW), f = ld2(q + 4 * BW);
-    const float2 s04 = f2add(a, f), s13 = f2add(b, e);
-    float2 acc = make_float2(k0 * s04.x, k0 * s04.y);
-    acc = f2add(acc, make_float2(k1 * s13.x, k1 * s13.y));
-    acc = f2add(acc, make_float2(k2 * c.x, k2 * c.y));
-    st2(sC + r * BW + d, acc);
-  }
-  __syncthreads();
-  /* Scharr gradient magnitude^2 at interior pixels of the tile */
-  float mx = 0.0f;
-  float *mp = p.t.planes + I.t1;
-  for (int i = tid; i < TH * (TW / 2); i += 256) {
-    const int r = i / (TW / 2), c = 2 * (i - r * (TW / 2));
-    const float *rm = sC + r * BW + c, *r0 = rm + BW, *rp = r0 + BW; /* sC columns c .. c + 3 are x - 1 .. x + 2 */
-    const float2 m0 = ld2(rm), m1 = ld2(rm + 2), c0 = ld2(r0), c1 = ld2(r0 + 2), p0 = ld2(rp), p1 = ld2(rp + 2);
-    const float2 hm = f2sub(m1, m0), h0 = f2sub(c1, c0), hp = f2sub(p1, p0); /* v[x+1] - v[x-1] */
-    const float2 u = f2add(hm, hp);
-    const float2 lx = f2add(make_float2(3.0f * u.x, 3.0f * u.y), make_float2(10.0f * h0.x, 10.0f * h0.y));
-    const float2 sp = f2add(p0, p1), sm = f2add(m0, m1); /* (v[x-1] + v[x+1]) */
-    const float2 syp = f2add(make_float2(3.0f * sp.x, 3.0f * sp.y), make_float2(10.0f * p0.y, 10.0f * p1.x));
-    const float2 sym = f2add(make_float2(3.0f * sm.x, 3.0f * sm.y), make_float2(10.0f * m0.y, 10.0f * m1.x));
-    const float2 ly = f2sub(syp, sym);
-    const float2 m = f2add(make_float2(lx.x * lx.x, lx.y * lx.y), make_float2(ly.x * ly.x, ly.y * ly.y));
-    const int y = ty0 + r, x = tx0 + c;
-    if (y < 1 || y >= H - 1) continue;
-    float *o = mp + (long long)y * L.pitch + x;
-    if (x >= 1 && x < W - 1) {
-      o[0] = m.x;
-      mx = fmaxf(mx, m.x);
-    }
-    if (x + 1 >= 1 && x + 1 < W - 1) {
-      o[1] = m.y;
-      mx = fmaxf(mx, m.y);
+    float *mp = p.t.planes + I.t1;
+    const bool mx0 = x >= 1 && x < W - 1, mx1 = x + 1 >= 1 && x + 1 < W - 1;
+    float2 ba[5], bb[5], ga[3], gb[3]; /* sB rows and sigma-1 rows; a: x - 1, x; b: x + 1, x + 2 */
+#pragma unroll
+    for (int k = 0; k < 14; k++) { /* sB row 8 g + k */
+      const float *q = sB + (g * 8 + k) * BW + c;
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        ba[i] = ba[i + 1];
+        bb[i] = bb[i + 1];
+      }
+      ba[4] = ld2(q);
+      bb[4] = ld2(q + 2);
+      if (k < 4) continue;
+      { /* sigma-1 row y - 1 + (k - 4), y = ty0 + 8 g */
+        const float2 sa04 = f2add(ba[0], ba[4]), sa13 = f2add(ba[1], ba[3]);
+        const float2 sb04 = f2add(bb[0], bb[4]), sb13 = f2add(bb[1], bb[3]);
+        float2 a = make_float2(k0 * sa04.x, k0 * sa04.y), b = make_float2(k0 * sb04.x, k0 * sb04.y);
+        a = f2add(a, make_float2(k1 * sa13.x, k1 * sa13.y));
+        b = f2add(b, make_float2(k1 * sb13.x, k1 * sb13.y));
+        a = f2add(a, make_float2(k2 * ba[2].x, k2 * ba[2].y));
+        b = f2add(b, make_float2(k2 * bb[2].x, k2 * bb[2].y));
+        ga[0] = ga[1];
+        ga[1] = ga[2];
+        ga[2] = a;
+        gb[0] = gb[1];
+        gb[1] = gb[2];
+        gb[2] = b;
+      }
+      if (k < 6) continue;
+      /* Scharr at row y = ty0 + 8 g + k - 6 */
+      const float2 m0 = ga[0], m1 = gb[0], c0 = ga[1], c1 = gb[1], p0 = ga[2], p1 = gb[2];
+      const float2 hm = f2sub(m1, m0), h0 = f2sub(c1, c0), hp = f2sub(p1, p0); /* v[x+1] - v[x-1] */
+      const float2 u = f2add(hm, hp);
+      const float2 lx = f2add(make_float2(3.0f * u.x, 3.0f * u.y), make_float2(10.0f * h0.x, 10.0f * h0.y));
+      const float2 sp = f2add(p0, p1), sm = f2add(m0, m1); /* (v[x-1] + v[x+1]) */
+      const float2 syp = f2add(make_float2(3.0f * sp.x, 3.0f * sp.y), make_float2(10.0f * p0.y, 10.0f * p1.x));
+      const float2 sym = f2add(make_float2(3.0f * sm.x, 3.0f * sm.y), make_float2(10.0f * m0.y, 10.0f * m1.x));
+      const float2 ly = f2sub(syp, sym);
+      const float2 m = f2add(make_float2(lx.x * lx.x, lx.y * lx.y), make_float2(ly.x * ly.x, ly.y * ly.y));
+      const int y = ty0 + g * 8 + k - 6;
+      if (y < 1 || y >= H - 1) continue;
+      float *o = mp + (long long)y * L.pitch + x;
+      if (mx0 && mx1) {
+        st2(o, m);
+        mx = fmaxf(fmaxf(mx, m.x), m.y);
+      } else if (mx0) {
+        o[0] = m.x;
+        mx = fmaxf(mx, m.x);
+      } else if (mx1) {
+        o[1] = m.y;
+        mx = fmaxf(mx, m.y);
+      }
     }
   }
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -324,7 +351,7 @@ __global__ void __launch_bounds__(256) k_contrast_hist(akz_level0_params p)
   constexpr int TW = AKZ_L0_TW, TH = AKZ_L0_TH;
   __shared__ unsigned int sHist[AKZ_MAX_NBINS];
   const int tid = threadIdx.x;
-  const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
+  const int si = akz_find_seg_warp(p.segs, p.nsegs, blockIdx.x);
   const akz_tile_seg sg = p.segs[si];
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const akz_image_desc I = p.t.im[L.image];
@@ -896,7 +923,7 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   /* the TMA box wants a 128-byte aligned destination */
   float *sm = sm_raw + ((128u - ((uint32_t)__cvta_generic_to_shared(sm_raw) & 127u)) & 127u) / 4;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int si = akz_find_seg(p.segs, p.nsegs, blockIdx.x);
+  const int si = akz_find_seg_warp(p.segs, p.nsegs, blockIdx.x);
   const akz_tile_seg sg = p.segs[si];
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const akz_image_desc I = p.t.im[L.image];
