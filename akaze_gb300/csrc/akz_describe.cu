@@ -25,6 +25,9 @@
 #define AKZ_DESC_WARPS 4
 #define AKZ_DESC_ITERS 14 /* 14 x 32 = 448 >= 21 x 21 window samples */
 #define AKZ_DESC_MAXIMG 1024 /* images whose keypoint offsets a CTA keeps in shared memory */
+#ifndef AKZ_DESC_CTAS
+#define AKZ_DESC_CTAS 5 /* resident CTAs per SM: at most 96 registers, ~34 KB of shared memory each */
+#endif
 #define AKZ_CV_PI 3.1415926535897932384626433832795
 
 /* orientation samples in the reference's thread order: tx = 16*(j+6) + (i+6) */
@@ -43,9 +46,13 @@ __device__ unsigned short g_smp_order[AKZ_DESC_MAXWIN + 1][32 * AKZ_DESC_ITERS];
 struct akz_warp_smem {
   float s[3][441];
   float v[87];
-  float bx[42], by[42];
-  float wx[42], wy[42];
-  float acc[16 * 2 * 32]; /* cell partials of one grid and channel: [cell][thread parity][lane] */
+  union {
+    struct {
+      float bx[42], by[42];
+      float wx[42], wy[42];
+    } o;                /* orientation bins */
+    float acc[16 * 33]; /* cell partials of one grid, channel and thread parity: [cell][lane] */
+  } u;
 };
 
 /* One grid (C cells) of the M-LDB cell sums, all three channels, in the
@@ -69,19 +76,22 @@ __device__ __forceinline__ void akz_mldb_cells(float *acc, const float (*src)[44
   for (int m = 0; m < AKZ_DESC_ITERS; m++) {
     const int i = lane + 32 * m;
     const int c = i < nsmp ? (cells[i] >> SHIFT) & MASK : MASK;
-    off[m] = c < C ? (2 * c + (m & 1)) * 32 + lane : -1;
+    off[m] = c < C ? c * 32 + lane : -1;
   }
 #pragma unroll 1
   for (int ch = 0; ch < 3; ch++) {
     const float *sc = src[ch];
-#pragma unroll
-    for (int r = 0; r < 2 * C; r++) acc[r * 32 + lane] = 0.0f;
-#pragma unroll
-    for (int m = 0; m < AKZ_DESC_ITERS; m++)
-      if (off[m] >= 0) acc[off[m]] += sc[lane + 32 * m];
     float a[C];
 #pragma unroll
-    for (int c = 0; c < C; c++) a[c] = acc[(2 * c) * 32 + lane] + acc[(2 * c + 1) * 32 + lane];
+    for (int par = 0; par < 2; par++) { /* thread l (even m), then thread l + 32 (odd m) */
+#pragma unroll
+      for (int r = 0; r < C; r++) acc[r * 32 + lane] = 0.0f;
+#pragma unroll
+      for (int m = par; m < AKZ_DESC_ITERS; m += 2)
+        if (off[m] >= 0) acc[off[m]] += sc[lane + 32 * m];
+#pragma unroll
+      for (int c = 0; c < C; c++) a[c] = par ? a[c] + acc[c * 32 + lane] : acc[c * 32 + lane];
+    }
     if (C <= 4) {
 #pragma unroll
       for (int c = 0; c < C; c++) {
@@ -95,29 +105,34 @@ __device__ __forceinline__ void akz_mldb_cells(float *acc, const float (*src)[44
 #pragma unroll
       for (int c = 0; c < C; c++) acc[c * 33 + lane] = a[c];
       __syncwarp();
-      if (lane < C) {
-        float t[32];
+      if (lane < C) { /* the tree's two halves of 16 leaves, then their sum (its last level) */
+        float h[2];
 #pragma unroll
-        for (int k = 0; k < 32; k++) t[k] = acc[lane * 33 + k];
+        for (int q = 0; q < 2; q++) {
+          float t[16];
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1)
+          for (int k = 0; k < 16; k++) t[k] = acc[lane * 33 + 16 * q + k];
 #pragma unroll
-          for (int j = 0; j < 32; j += 2 * d) t[j] = t[j] + t[j + d];
-        vout[3 * (BASE + lane) + ch] = t[0];
+          for (int d = 1; d < 16; d <<= 1)
+#pragma unroll
+            for (int j = 0; j < 16; j += 2 * d) t[j] = t[j] + t[j + d];
+          h[q] = t[0];
+        }
+        vout[3 * (BASE + lane) + ch] = h[0] + h[1];
       }
     }
     __syncwarp();
   }
 }
 
-__global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_params p)
+__global__ void __launch_bounds__(32 * AKZ_DESC_WARPS, AKZ_DESC_CTAS) k_describe(akz_describe_params p)
 {
   __shared__ akz_warp_smem sm_all[AKZ_DESC_WARPS];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   akz_warp_smem &S = sm_all[wib];
   const int nwarps = gridDim.x * AKZ_DESC_WARPS;
   /* keypoint offsets of the images, once per CTA: sOff[i] = sum_{j<i} nkp_j */
-  __shared__ int sOff[AKZ_DESC_MAXIMG + 1];
+  extern __shared__ int sOff[]; /* nimg + 1 entries when nimg <= AKZ_DESC_MAXIMG */
   const bool table = p.t.nimg <= AKZ_DESC_MAXIMG;
   if (table) {
     if (threadIdx.x == 0) {
@@ -266,24 +281,24 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
             ry1 += S.s[1][s];
           }
         }
-        S.bx[lane] = rx0;
-        S.by[lane] = ry0;
+        S.u.o.bx[lane] = rx0;
+        S.u.o.by[lane] = ry0;
         if (b1 < 42) {
-          S.bx[b1] = rx1;
-          S.by[b1] = ry1;
+          S.u.o.bx[b1] = rx1;
+          S.u.o.by[b1] = ry1;
         }
       }
       __syncwarp();
       float best = -1.0f;
       int bk = 0;
       for (int t = lane; t < 42; t += 32) {
-        float ex = S.bx[t], ey = S.by[t];
+        float ex = S.u.o.bx[t], ey = S.u.o.by[t];
         for (int q = t + 1; q < t + 7; q++) {
-          ex += S.bx[q < 42 ? q : q - 42];
-          ey += S.by[q < 42 ? q : q - 42];
+          ex += S.u.o.bx[q < 42 ? q : q - 42];
+          ey += S.u.o.by[q < 42 ? q : q - 42];
         }
-        S.wx[t] = ex;
-        S.wy[t] = ey;
+        S.u.o.wx[t] = ex;
+        S.u.o.wy[t] = ey;
         const float r = ex * ex + ey * ey;
         if (r > best) {
           best = r;
@@ -301,7 +316,7 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
       }
       if (!(best > 0.0f)) bk = 0;
       __syncwarp();
-      const float a = akz_atan2f(S.wy[bk], S.wx[bk]);
+      const float a = akz_atan2f(S.u.o.wy[bk], S.u.o.wx[bk]);
       angle = a < 0.0f ? (float)((double)a + 2.0 * AKZ_CV_PI) : a;
       if (lane == 0) kpp->angle = angle;
       __syncwarp();
@@ -359,9 +374,9 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS) k_describe(akz_describe_p
       S.s[2][s] = dx * co + dy * si;
     }
     __syncwarp();
-    akz_mldb_cells<4, 0, 7, 0>(S.acc, S.s, sCell, lane, nsmp, S.v);
-    akz_mldb_cells<9, 3, 15, 4>(S.acc, S.s, sCell, lane, nsmp, S.v);
-    akz_mldb_cells<16, 7, 31, 13>(S.acc, S.s, sCell, lane, nsmp, S.v);
+    akz_mldb_cells<4, 0, 7, 0>(S.u.acc, S.s, sCell, lane, nsmp, S.v);
+    akz_mldb_cells<9, 3, 15, 4>(S.u.acc, S.s, sCell, lane, nsmp, S.v);
+    akz_mldb_cells<16, 7, 31, 13>(S.u.acc, S.s, sCell, lane, nsmp, S.v);
     __syncwarp();
     /* word w holds bits 32w .. 32w+31, LSB first: one ballot per word */
     uint32_t myword = 0;
@@ -437,7 +452,14 @@ cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaS
     }
   }
   if (nblocks <= 0) return cudaSuccess;
-  k_describe<<<nblocks, 32 * AKZ_DESC_WARPS, 0, s>>>(p);
+  const size_t dyn = p.t.nimg <= AKZ_DESC_MAXIMG ? (size_t)(p.t.nimg + 1) * sizeof(int) : 0;
+  /* a grid-stride loop over the keypoints: one wave of resident CTAs */
+  int per_sm = 0, nsm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_describe, 32 * AKZ_DESC_WARPS, dyn) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return cudaErrorInvalidValue;
+  const int grid = std::min(nblocks, std::max(1, per_sm) * nsm);
+  k_describe<<<grid, 32 * AKZ_DESC_WARPS, dyn, s>>>(p);
   return cudaGetLastError();
 }
 
