@@ -295,7 +295,10 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
   };
 
   /* pre-roll: S rows ty0-1-2ST .. ty0+2ST, D rows ty0-1-ST .. ty0+ST,
-   * E rows ty0-1, ty0; then iteration 0's S rows in flight */
+   * E rows ty0-1, ty0; then block 0's Lx, Ly and determinant rows.
+   * Blocks of BH rows; warp w < BH takes row pair (o, o + ST) of a block,
+   * o = (q / ST) 2 ST + q % ST with q = w / 2, and column half w % 2 */
+  const int q = warp >> 1, half = warp & 1, o = (q / ST) * 2 * ST + q % ST;
   for (int r = ty0 - 1 - 2 * ST + warp; r <= ty0 + 2 * ST; r += 8) load_s(r);
   akz_cp_async_commit();
   akz_cp_async_wait_all();
@@ -305,20 +308,25 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
   for (int r = ty0 - 1 - ST + warp; r <= ty0 + ST; r += 8) comp_d(r);
   __syncthreads();
   if (warp < 2) comp_e(ty0 - 1 + warp);
-  /* blocks of BH rows; warp w < BH takes row pair (o, o + ST) of the block,
-   * o = (q / ST) 2 ST + q % ST with q = w / 2, and column half w % 2 */
-  const int q = warp >> 1, half = warp & 1, o = (q / ST) * 2 * ST + q % ST;
+  akz_cp_async_wait_all();
+  __syncthreads(); /* block 0's S rows landed */
+  if (iters > 1 && warp < BH) load_s(ty0 + 2 * ST + BH + 1 + warp);
+  akz_cp_async_commit();
+  if (warp < BH) comp_d2(ty0 + ST + 1 + o, 2 * (32 * half + lane));
+  __syncthreads();
+  if (warp < BH) comp_e2(ty0 + 1 + o, 32 * half + lane);
+  /* iteration k: block k + 1's Lx, Ly next to block k's maxima, then block
+   * k + 1's determinant; block k + 2's S rows in flight */
   for (int k = 0; k < iters; k++) {
     const int r = ty0 + BH * k;
     akz_cp_async_wait_all();
-    __syncthreads(); /* S rows up to r+BH+2ST landed; E rows up to r visible */
-    if (k + 1 < iters && warp < BH) load_s(r + 2 * ST + BH + 1 + warp);
+    __syncthreads(); /* S rows up to r+2BH+2ST landed; E rows up to r+BH visible */
+    if (k + 2 < iters && warp < BH) load_s(r + 2 * ST + 2 * BH + 1 + warp);
     akz_cp_async_commit();
-    if (warp < BH) comp_d2(r + ST + 1 + o, 2 * (32 * half + lane));
-    __syncthreads();
-    if (warp < BH) comp_e2(r + 1 + o, 32 * half + lane);
-    __syncthreads();
+    if (k + 1 < iters && warp < BH) comp_d2(r + BH + ST + 1 + o, 2 * (32 * half + lane));
     if (warp < BH) maxima(r + warp);
+    __syncthreads();
+    if (k + 1 < iters && warp < BH) comp_e2(r + BH + 1 + o, 32 * half + lane);
   }
   akz_cp_async_wait_all();
 }
