@@ -10,7 +10,10 @@
  *              L_end = L_start + s_out * (net output).
  * Every 3x3 layer extends its input by replicate padding at the image border.
  *
- * GEMM kernel: a CTA computes a 32 x 4 pixel block (4 warps, one pixel row
+ * The 3 x 3 layers 2-4 run on tcgen05 (k_sg_conv_tcp below, the default);
+ * layers 1 and 5, and layers 2-4 when tcgen05 is switched off, on mma.sync.
+ *
+ * mma.sync kernel: a CTA computes a 32 x 4 pixel block (4 warps, one pixel row
  * each, two m16 tiles per warp) for all outputs.  Its input region (with a
  * one-pixel halo for 3x3) is staged in shared memory as 64-byte pixel rows
  * whose four 16-byte channel chunks are XOR-swizzled by (pixel >> 1) & 3, so
@@ -183,18 +186,10 @@ __global__ void __launch_bounds__(128) k_sg_conv_mma(const __nv_bfloat16 *__rest
 }
 
 /* ------------------------------------------------------------------------ */
-/* tcgen05 path for the 32 -> 32 layers (layer 1 as 1 x 1, layers 2-4 as
- * 3 x 3): a CTA of 4 warps computes 128 consecutive pixels of one row,
- * D[128 x 32] (FP32, in TMEM) += A[128 x K] * B[K x 32] in K steps of 16.
- *
- * Shared-memory operands use the canonical K-major layout without swizzle:
- * 8-row x 16-byte core matrices, row r of a core matrix at r * 16 bytes;
- * core matrices adjacent in K are LBO = 128 bytes apart, adjacent in M / N
- * SBO bytes apart.  A: per tap a [16 row groups][4 K groups] block (SBO =
- * 512, 8 KB per tap); B: [4 row groups][K / 8 K groups] (SBO = K * 16).
- * One elected thread issues the MMAs and commits them to an mbarrier; the
- * wait is bounded (AKZ_SG_TC_SPIN polls), after which the CTA records an
- * error and still frees its TMEM. */
+/* tcgen05 helpers.  Shared-memory operands use the canonical K-major layout
+ * without swizzle: 8-row x 16-byte core matrices, row r of a core matrix at
+ * r * 16 bytes; LBO is the byte distance of core matrices adjacent in K,
+ * SBO of those adjacent in M / N. */
 
 #define AKZ_SG_TC_SPIN (1 << 24)
 
@@ -215,110 +210,213 @@ __host__ __device__ constexpr uint32_t sg_idesc(int M, int N)
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-template <int NTAPS>
-__global__ void __launch_bounds__(128) k_sg_conv_tc(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ wt,
-                                                    const float *__restrict__ bias, __nv_bfloat16 *__restrict__ out,
-                                                    akz_sg_level lv, int *err)
+/* ------------------------------------------------------------------------ */
+/* Persistent, pipelined tcgen05 kernel for the 3 x 3 layers (32 -> 32).
+ *
+ * Work item: a 128-pixel column block and rc consecutive rows.  The CTA
+ * walks the rows downwards; each input row (the block's 128 pixels plus one
+ * on each side, replicate-clamped) is staged once, by cp.async, into a ring
+ * of SG_TP_R rows laid out as [channel group][pixel] 16-byte cells.  In that
+ * layout the K-major core matrices of a row are SBO = 128 bytes apart along
+ * M (8 pixels) and LBO = SG_TP_NPIX * 16 bytes apart along K, so the three
+ * horizontal taps of a row are the same row at start offsets 0, 16 and 32
+ * bytes: no im2col copy.  Row y's 18 MMAs (9 taps x 2 K-steps of 16) read
+ * ring rows y - 1 .. y + 1 and accumulate into one of two 32-column TMEM
+ * buffers; while they run, the threads wait for row y - 1's MMAs, load row
+ * y + 4 into the slot row y - 2 left (rows y + 2 and y + 3 are on their
+ * way), and write row y - 1 from TMEM (bias, ReLU, bf16).  rc is chosen by
+ * the host so that every CTA gets at most one item.  Every mbarrier wait is bounded; a timeout records the error
+ * flag, ends the CTA's loop, and TMEM is freed after one more bounded wait. */
+
+#define SG_TP_R 6                      /* ring rows */
+#define SG_TP_NPIX 130                 /* staged pixels per row */
+#define SG_TP_SLOT (4 * SG_TP_NPIX * 16) /* bytes per ring row */
+#define SG_TP_SMEM (32 * 288 * 2 + SG_TP_R * SG_TP_SLOT)
+
+__device__ __forceinline__ void sg_cp_async16(void *dst, const void *src)
 {
-  constexpr int K = NTAPS * 32;
-  constexpr int A_BYTES = NTAPS * 128 * 64, B_BYTES = 32 * K * 2;
-  extern __shared__ __align__(1024) unsigned char tcsm[];
-  unsigned char *sA = tcsm, *sB = tcsm + A_BYTES;
-  __shared__ __align__(8) unsigned long long mbar;
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ bool sg_mbar_wait(const unsigned long long *mbar, uint32_t parity)
+{
+  const uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar);
+  uint32_t done = 0;
+  for (int it = 0; it < AKZ_SG_TC_SPIN && !done; it++)
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done)
+                 : "r"(mb), "r"(parity)
+                 : "memory");
+  return done != 0;
+}
+
+__global__ void __launch_bounds__(128) k_sg_conv_tcp(const __nv_bfloat16 *__restrict__ in,
+                                                     const __nv_bfloat16 *__restrict__ wt, const float *__restrict__ bias,
+                                                     __nv_bfloat16 *__restrict__ out, akz_sg_level lv, int rc, int *err)
+{
+  constexpr int K = 288, NP = SG_TP_NPIX, R = SG_TP_R;
+  extern __shared__ __align__(1024) unsigned char tpsm[];
+  unsigned char *sB = tpsm, *sR = tpsm + 32 * K * 2;
+  __shared__ __align__(8) unsigned long long mbar[2];
   __shared__ uint32_t tbase;
   __shared__ float sBias[32];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int W = lv.W, H = lv.H;
-  const int x0 = blockIdx.x * 128, y = blockIdx.y;
+  const int nxb = (W + 127) / 128, nitems = nxb * ((H + rc - 1) / rc);
 
-  /* B: weight row n, K group kg -> core matrix (n / 8, kg), row n % 8 */
+  /* weights: row n, K group kg -> core matrix (n / 8, kg), row n % 8 */
   for (int i = tid; i < 32 * (K / 8); i += 128) {
     const int n = i / (K / 8), kg = i - n * (K / 8);
     *(uint4 *)(sB + (n >> 3) * (K * 16) + kg * 128 + (n & 7) * 16) = *(const uint4 *)(wt + n * K + kg * 8);
   }
-  /* A: tap t, pixel m (x0 + m), channel group kg -> tap block t, core (m / 8, kg), row m % 8 */
-  for (int i = tid; i < NTAPS * 128 * 4; i += 128) {
-    const int t = i / 512, r = i - t * 512, m = r >> 2, kg = r & 3;
-    const int dy = NTAPS == 9 ? t / 3 - 1 : 0, dx = NTAPS == 9 ? t % 3 - 1 : 0;
-    const int yy = sg_clamp(y + dy, 0, H - 1), xx = sg_clamp(x0 + m + dx, 0, W - 1);
-    *(uint4 *)(sA + t * 8192 + (m >> 3) * 512 + kg * 128 + (m & 7) * 16) =
-        *(const uint4 *)(in + ((long long)yy * W + xx) * 32 + kg * 8);
-  }
   if (tid < 32) sBias[tid] = bias[tid];
   if (warp == 0) {
     const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tbase);
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(dst));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(dst));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+    for (int b = 0; b < 2; b++) {
+      const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[b]);
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+    }
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
-  asm volatile("fence.proxy.async.shared::cta;"); /* generic-proxy writes -> tensor core reads */
+  asm volatile("fence.proxy.async.shared::cta;");
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tbase;
-  if (tid == 0) {
-    constexpr uint32_t idesc = sg_idesc(128, 32);
-#pragma unroll 1
-    for (int s = 0; s < K / 16; s++) {
-      const int t = s >> 1, kc = s & 1;
-      const uint64_t ad = sg_smem_desc(sA + t * 8192 + kc * 256, 128, 512);
-      const uint64_t bd = sg_smem_desc(sB + (2 * s) * 128, 128, K * 16);
-      const uint32_t acc = s > 0 ? 1u : 0u;
-      asm volatile(
-          "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-          "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+  constexpr uint32_t idesc = sg_idesc(128, 32);
+  const uint64_t adesc0 = sg_smem_desc(sR, NP * 16, 128), bdesc0 = sg_smem_desc(sB, 128, K * 16);
+
+  auto load_row = [&](int yrow, int slot, int x0) { /* 16-byte chunks, pixel-major over the threads */
+    const __nv_bfloat16 *src = in + (long long)sg_clamp(yrow, 0, H - 1) * W * 32;
+    unsigned char *dst = sR + slot * SG_TP_SLOT;
+    for (int c = tid; c < 4 * NP; c += 128) {
+      const int px = c >> 2, kg = c & 3;
+      sg_cp_async16(dst + kg * (NP * 16) + px * 16, src + (long long)sg_clamp(x0 - 1 + px, 0, W - 1) * 32 + kg * 8);
     }
-    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb));
-  }
-  /* bounded wait for the MMAs */
-  {
-    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
-    uint32_t done = 0;
-    for (int it = 0; it < AKZ_SG_TC_SPIN && !done; it++)
-      asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
-                   : "=r"(done)
-                   : "r"(mb));
-    if (!done) atomicExch(err, 1);
-  }
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  /* epilogue: warp w reads TMEM lanes 32w .. 32w+31 (its 32 pixels) x 32 columns */
-  uint32_t r[32];
-  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;");
-  const int x = x0 + warp * 32 + lane;
-  if (x < W) {
-    __align__(16) __nv_bfloat162 v[16];
+  };
+  auto sync_ring = [&](int pending) { /* landed rows -> tensor core; all threads past their TMEM reads */
+    if (pending)
+      asm volatile("cp.async.wait_group 2;" ::: "memory");
+    else
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+  };
+  auto epilogue = [&](uint32_t c, int y, int x0) { /* batch c's accumulator: warp w has pixels 32w .. 32w+31 */
+    uint32_t r[32];
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (c & 1u) * 32u;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+    const int x = x0 + warp * 32 + lane;
+    if (x < W && y < H) {
+      __align__(16) __nv_bfloat162 v[16];
 #pragma unroll
-    for (int c = 0; c < 16; c++)
-      v[c] = __floats2bfloat162_rn(fmaxf(__uint_as_float(r[2 * c]) + sBias[2 * c], 0.0f),
-                                   fmaxf(__uint_as_float(r[2 * c + 1]) + sBias[2 * c + 1], 0.0f));
-    uint4 *dst = (uint4 *)(out + ((long long)y * W + x) * 32);
-    const uint4 *src = (const uint4 *)v;
+      for (int k = 0; k < 16; k++)
+        v[k] = __floats2bfloat162_rn(fmaxf(__uint_as_float(r[2 * k]) + sBias[2 * k], 0.0f),
+                                     fmaxf(__uint_as_float(r[2 * k + 1]) + sBias[2 * k + 1], 0.0f));
+      uint4 *dst = (uint4 *)(out + ((long long)y * W + x) * 32);
+      const uint4 *src = (const uint4 *)v;
 #pragma unroll
-    for (int c = 0; c < 4; c++) dst[c] = src[c];
+      for (int k = 0; k < 4; k++) dst[k] = src[k];
+    }
+  };
+
+  uint32_t issued = 0, retired = 0; /* MMA batches issued / known complete (batch c: mbar[c & 1], its (c >> 1)-th phase) */
+  bool ok = true;
+  for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+    const int xb = item % nxb, yb = (item / nxb) * rc, n = min(rc, H - yb), x0 = xb * 128;
+    /* ring row j holds image row yb - 1 + j, slot j % R; row y's MMAs need rows up to y + 1 */
+    load_row(yb - 1, 0, x0);
+    load_row(yb, 1, x0);
+    load_row(yb + 1, 2, x0);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    if (n >= 2) load_row(yb + 2, 3, x0);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    if (n >= 3) load_row(yb + 3, 4, x0);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    sync_ring(1);
+    for (int i = 0; i < n; i++) {
+      if (tid == 0) { /* row yb + i: ring rows i .. i + 2, taps (dy, dx) at slot (i + dy) % R, offset 16 dx */
+        const uint32_t d = tmem + (issued & 1u) * 32u;
+        const uint32_t so[3] = {(uint32_t)((i % R) * SG_TP_SLOT), (uint32_t)(((i + 1) % R) * SG_TP_SLOT),
+                                (uint32_t)(((i + 2) % R) * SG_TP_SLOT)};
+#pragma unroll
+        for (int s = 0; s < 18; s++) {
+          const int t = s >> 1, kc = s & 1, dy = t / 3, dx = t - 3 * dy;
+          /* the start address field counts 16-byte units in the low bits: offsets add to it */
+          const uint64_t ad = adesc0 + ((so[dy] + (uint32_t)((2 * kc) * (NP * 16) + dx * 16)) >> 4);
+          const uint64_t bd = bdesc0 + (uint64_t)((2 * s * 128) >> 4);
+          const uint32_t acc = s > 0 ? 1u : 0u;
+          asm volatile(
+              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+        }
+        const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[issued & 1u]);
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb));
+      }
+      issued++;
+      if (i >= 1) { /* row yb + i - 1's MMAs: then its ring row yb + i - 2 is free and its accumulator ready */
+        const uint32_t c = issued - 2;
+        const bool dn = sg_mbar_wait(&mbar[c & 1u], (c >> 1) & 1u);
+        if (__syncthreads_or(!dn)) {
+          ok = false;
+          break;
+        }
+        retired = c + 1;
+      }
+      if (i + 4 <= n) load_row(yb + i + 4, (i + 5) % R, x0);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      if (i >= 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        epilogue(issued - 2, yb + i - 1, x0);
+      }
+      sync_ring(1);
+    }
+    if (!ok) break;
+    { /* the item's last row */
+      const uint32_t c = issued - 1;
+      const bool dn = sg_mbar_wait(&mbar[c & 1u], (c >> 1) & 1u);
+      if (__syncthreads_or(!dn)) {
+        ok = false;
+        break;
+      }
+      retired = c + 1;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      epilogue(c, yb + n - 1, x0);
+    }
+    sync_ring(0);
   }
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+    if (retired < issued) { /* batches complete in order: wait (bounded) for the last one */
+      const uint32_t c = issued - 1;
+      sg_mbar_wait(&mbar[c & 1u], (c >> 1) & 1u);
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
 }
 
-/* tcgen05 path switch for the 32 -> 32 layers (off: mma.sync), and the
- * flag its kernels set when an MMA wait ran out. */
-static int g_sg_tc = 0;
+/* tensor path of the 3 x 3 layers 2-4 (on: k_sg_conv_tcp, off: mma.sync),
+ * and the flag the tcgen05 kernel sets when an MMA wait ran out. */
+static int g_sg_tc = 1;
 static __device__ int g_sg_tc_err;
 
 extern "C" AKZ_API akz_status akz_sg_set_tcgen05(int on)
@@ -374,15 +472,27 @@ extern "C" AKZ_API akz_status akz_sg_infer_level(const float *l0, const float *g
   if (g_sg_tc) {
     int *err = nullptr;
     cudaError_t e = cudaGetSymbolAddress((void **)&err, g_sg_tc_err);
-    constexpr int smem1 = 1 * 128 * 64 + 32 * 32 * 2, smem9 = 9 * 128 * 64 + 32 * 288 * 2;
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sg_conv_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sg_conv_tc<9>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem9);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sg_conv_tcp, cudaFuncAttributeMaxDynamicSharedMemorySize, SG_TP_SMEM);
+    /* all of the unified L1 as shared memory, so that 3 CTAs fit an SM */
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_sg_conv_tcp, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    int dev = 0, nsm = 0, smem_sm = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
-    const dim3 gt((width + 127) / 128, height);
-    k_sg_conv_tc<1><<<gt, 128, smem1, s>>>(a0, w, biases, a1, lv, err);
-    k_sg_conv_tc<9><<<gt, 128, smem9, s>>>(a1, w + SG_W1, biases + 32, a0, lv, err);
-    k_sg_conv_tc<9><<<gt, 128, smem9, s>>>(a0, w + SG_W1 + SG_W3, biases + 64, a1, lv, err);
-    k_sg_conv_tc<9><<<gt, 128, smem9, s>>>(a1, w + SG_W1 + 2 * SG_W3, biases + 96, a0, lv, err);
+    /* resident CTAs per SM: shared memory (operands, ring, ~1 KB static and 1 KB reserved each), at most 8
+     * (8 x 64 TMEM columns = 512) */
+    const int per_sm = std::max(1, std::min(8, smem_sm / (SG_TP_SMEM + 2048)));
+    /* rows per item: every resident CTA gets at most one item, of at least 2 rows */
+    const int nxb = (width + 127) / 128, ctas = per_sm * nsm;
+    const int rc = std::max(2, (height + std::max(1, ctas / nxb) - 1) / std::max(1, ctas / nxb));
+    const int items = nxb * ((height + rc - 1) / rc);
+    const int gp = std::max(1, std::min(items, ctas));
+    k_sg_conv_mma<1, 4, false><<<grid, 128, 0, s>>>(a0, w, biases, a1, lv);
+    k_sg_conv_tcp<<<gp, 128, SG_TP_SMEM, s>>>(a1, w + SG_W1, biases + 32, a0, lv, rc, err);
+    k_sg_conv_tcp<<<gp, 128, SG_TP_SMEM, s>>>(a0, w + SG_W1 + SG_W3, biases + 64, a1, lv, rc, err);
+    k_sg_conv_tcp<<<gp, 128, SG_TP_SMEM, s>>>(a1, w + SG_W1 + 2 * SG_W3, biases + 96, a0, lv, rc, err);
   } else {
     k_sg_conv_mma<1, 4, false><<<grid, 128, 0, s>>>(a0, w, biases, a1, lv);
     k_sg_conv_mma<9, 4, false><<<grid, 128, 0, s>>>(a1, w + SG_W1, biases + 32, a0, lv);

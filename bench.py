@@ -58,7 +58,7 @@ def parse():
                     help="small case for ncu: --batch images, one graph-less run of every stage, no timing line")
     ap.add_argument("--weights", default=os.path.join(ROOT, "akaze_gb300", "surrogate_weights.npz"),
                     help="surrogate4k: trained surrogate weights (python -m akaze_gb300.surrogate train)")
-    ap.add_argument("--sg-tcgen05", type=int, default=0, choices=[0, 1],
+    ap.add_argument("--sg-tcgen05", type=int, default=1, choices=[0, 1],
                     help="surrogate4k: run the net's 32-channel layers on tcgen05 (1) or mma.sync (0)")
     ap.add_argument("--check-tol", type=float, default=2e-3,
                     help="surrogate4k: per-level tolerance of the surrogate against plain FED before it falls back")

@@ -260,10 +260,11 @@ AKZ_API akz_status akz_sg_mse_grad(const float *out, const float *target, float 
  * 2 * width * height * 64 bytes.  Weights and scratch 16-byte aligned.
  * Asynchronous on stream. */
 AKZ_API size_t akz_sg_weight_elems(void);
-/* Run the four 32 -> 32 layers of akz_sg_infer_level on tcgen05 tensor
- * cores (TMEM accumulators, one elected thread issuing the MMAs) instead of
- * mma.sync; process-wide, off by default.  akz_sg_tcgen05_status reports (and
- * clears) whether any of those kernels gave up waiting for its MMAs. */
+/* Run the three 3 x 3 32 -> 32 layers of akz_sg_infer_level on tcgen05
+ * tensor cores (persistent CTAs, a ring of input rows, TMEM accumulators,
+ * one elected thread issuing the MMAs; on by default) or on mma.sync (0);
+ * process-wide.  akz_sg_tcgen05_status reports (and clears) whether any of
+ * those kernels gave up waiting for its MMAs. */
 AKZ_API akz_status akz_sg_set_tcgen05(int on);
 AKZ_API akz_status akz_sg_tcgen05_status(int *timed_out);
 

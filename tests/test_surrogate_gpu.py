@@ -42,13 +42,17 @@ def test_training_kernels_match_numpy(gpu_lib):
         assert _close(net.gb[i].cpu().numpy(), db, 1e-3), f"db {i}"
 
 
-@pytest.mark.parametrize("tcgen05", [False, True])
-def test_inference_kernel_matches_bf16_emulation(gpu_lib, tcgen05):
+@pytest.mark.parametrize("tcgen05,W,H", [(False, 100, 70), (True, 100, 70), (True, 300, 77), (True, 640, 400)])
+def test_inference_kernel_matches_bf16_emulation(gpu_lib, tcgen05, W, H):
+    """The persistent tcgen05 kernel gives each CTA at most one item of
+    ceil(H / (CTAs per 128-pixel column block)) rows: (300, 77) has a
+    partial column block and one-row items; (640, 400) has items of 5 rows
+    on 152 SMs, so rows are prefetched inside the loop."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(5)
     params = [(rng.normal(0, np.sqrt(2.0 / (ci * 9)), (co, ci, 3, 3)).astype(np.float32),
                rng.normal(0, 0.05, co).astype(np.float32)) for ci, co in sg.LAYERS]
-    H, W, pitch = 70, 100, 112
+    pitch = (W + 31) // 32 * 32
     l0 = rng.uniform(0, 1, (H, W)).astype(np.float32)
     g = rng.uniform(0, 1, (H, W)).astype(np.float32)
     dtf, s_out = 0.7, sg.S_OUT
@@ -70,7 +74,7 @@ def test_inference_kernel_matches_bf16_emulation(gpu_lib, tcgen05):
                                 ctypes.c_void_p(dout.data_ptr()), None)
     assert st == 0, lib.akz_last_error()
     torch.cuda.synchronize()
-    lib.akz_sg_set_tcgen05(0)
+    lib.akz_sg_set_tcgen05(1)  # the default
     timed_out = ctypes.c_int(-1)
     assert lib.akz_sg_tcgen05_status(ctypes.byref(timed_out)) == 0 and timed_out.value == 0
     got = (dout.cpu().numpy()[:, :W].astype(np.float64) - l0) / s_out
