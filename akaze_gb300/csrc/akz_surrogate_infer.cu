@@ -224,9 +224,11 @@ __host__ __device__ constexpr uint32_t sg_idesc(int M, int N)
  * ring rows y - 1 .. y + 1 and accumulate into one of two 32-column TMEM
  * buffers; while they run, the threads wait for row y - 1's MMAs, load row
  * y + 4 into the slot row y - 2 left (rows y + 2 and y + 3 are on their
- * way), and write row y - 1 from TMEM (bias, ReLU, bf16).  rc is chosen by
- * the host so that every CTA gets at most one item.  Every mbarrier wait is bounded; a timeout records the error
- * flag, ends the CTA's loop, and TMEM is freed after one more bounded wait. */
+ * way), and write row y - 1 from TMEM (bias, ReLU, bf16); one barrier per
+ * row.  rc is chosen by the host so that every CTA gets at most one item.
+ * Every mbarrier wait is bounded; a timeout records the error flag, ends the
+ * CTA's loop at the next barrier, and TMEM is freed after one more bounded
+ * wait. */
 
 #define SG_TP_R 6                      /* ring rows */
 #define SG_TP_NPIX 130                 /* staged pixels per row */
@@ -299,15 +301,18 @@ __global__ void __launch_bounds__(128) k_sg_conv_tcp(const __nv_bfloat16 *__rest
       sg_cp_async16(dst + kg * (NP * 16) + px * 16, src + (long long)sg_clamp(x0 - 1 + px, 0, W - 1) * 32 + kg * 8);
     }
   };
-  auto sync_ring = [&](int pending) { /* landed rows -> tensor core; all threads past their TMEM reads */
+  /* landed rows -> tensor core; all threads past their TMEM reads; returns
+   * (CTA-uniform) whether any thread saw an MMA wait run out */
+  auto sync_ring = [&](int pending, bool bad) -> bool {
     if (pending)
       asm volatile("cp.async.wait_group 2;" ::: "memory");
     else
       asm volatile("cp.async.wait_group 0;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;");
     asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
+    const bool any = __syncthreads_or(bad) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;");
+    return any;
   };
   auto epilogue = [&](uint32_t c, int y, int x0) { /* batch c's accumulator: warp w has pixels 32w .. 32w+31 */
     uint32_t r[32];
@@ -348,7 +353,7 @@ __global__ void __launch_bounds__(128) k_sg_conv_tcp(const __nv_bfloat16 *__rest
     asm volatile("cp.async.commit_group;" ::: "memory");
     if (n >= 3) load_row(yb + 3, 4, x0);
     asm volatile("cp.async.commit_group;" ::: "memory");
-    sync_ring(1);
+    sync_ring(1, false);
     for (int i = 0; i < n; i++) {
       if (tid == 0) { /* row yb + i: ring rows i .. i + 2, taps (dy, dx) at slot (i + dy) % R, offset 16 dx */
         const uint32_t d = tmem + (issued & 1u) * 32u;
@@ -370,36 +375,35 @@ __global__ void __launch_bounds__(128) k_sg_conv_tcp(const __nv_bfloat16 *__rest
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb));
       }
       issued++;
+      bool bad = false;
       if (i >= 1) { /* row yb + i - 1's MMAs: then its ring row yb + i - 2 is free and its accumulator ready */
         const uint32_t c = issued - 2;
-        const bool dn = sg_mbar_wait(&mbar[c & 1u], (c >> 1) & 1u);
-        if (__syncthreads_or(!dn)) {
-          ok = false;
-          break;
-        }
-        retired = c + 1;
+        bad = !sg_mbar_wait(&mbar[c & 1u], (c >> 1) & 1u);
+        if (!bad) retired = c + 1;
       }
-      if (i + 4 <= n) load_row(yb + i + 4, (i + 5) % R, x0);
+      if (i + 4 <= n && !bad) load_row(yb + i + 4, (i + 5) % R, x0);
       asm volatile("cp.async.commit_group;" ::: "memory");
       if (i >= 1) {
         asm volatile("tcgen05.fence::after_thread_sync;");
         epilogue(issued - 2, yb + i - 1, x0);
       }
-      sync_ring(1);
+      if (sync_ring(1, bad)) {
+        ok = false;
+        break;
+      }
     }
     if (!ok) break;
     { /* the item's last row */
       const uint32_t c = issued - 1;
-      const bool dn = sg_mbar_wait(&mbar[c & 1u], (c >> 1) & 1u);
-      if (__syncthreads_or(!dn)) {
+      const bool bad = !sg_mbar_wait(&mbar[c & 1u], (c >> 1) & 1u);
+      if (!bad) retired = c + 1;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      epilogue(c, yb + n - 1, x0);
+      if (sync_ring(0, bad)) {
         ok = false;
         break;
       }
-      retired = c + 1;
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      epilogue(c, yb + n - 1, x0);
     }
-    sync_ring(0);
   }
   if (!ok) {
     if (tid == 0) atomicExch(err, 1);
