@@ -10,9 +10,13 @@
  * cells (87 sums) and 486 pairwise comparisons, written as 64-byte rows
  * (bits 486..511 zero) that the matcher reads directly.
  *
- * Sums are formed in a fixed order (sample order for the orientation bins,
- * raster order of the window for the cells), which is the order of the CPU
- * restatement, so angles and descriptors are reproducible bit for bit.
+ * Sums are formed in a fixed order: sample order for the orientation bins,
+ * and for the cells the reference's order (64 strided per-thread partials,
+ * pairs t and t + 32, then the shuffle-down tree).  The CPU restatement uses
+ * the same orders, so angles and descriptors are reproducible bit for bit.
+ *
+ * The grid is one wave of resident CTAs (AKZ_DESC_CTAS per SM), each warp
+ * looping over keypoints.
  */
 #include <cuda_runtime.h>
 

@@ -19,7 +19,7 @@
  *   k_extract_fit  one thread per raw extremum of the batch: subpixel fit and
  *              record (:744-769), the determinant recomputed from Lx, Ly at
  *              the 3x3 neighbourhood.
- *   k_nms      one CTA per image: the reference's round-based suppression
+ *   k_nms      one cluster of 8 CTAs per image: the reference's round-based suppression
  *              (:1005-1224) with an exact per-slot minimum (atomicMin), then
  *              the 2048-slot chunked emission and subpixel restore
  *              (:1227-1316).
@@ -59,11 +59,15 @@ __device__ __forceinline__ int akz_border_hi(float border, int n)
  * options).
  *
  * A CTA owns a strip of TW output columns and AKZ_STRIP_CH rows and walks
- * down it 8 rows per iteration, one row per warp in each phase:
- *   Lsmooth rows  -> ring of 32 rows (cp.async, issued one iteration ahead)
+ * down it in blocks of BH rows (8; 6 for step 3):
+ *   Lsmooth rows  -> ring of 32 rows (cp.async, issued one block ahead)
  *   Lx, Ly rows   -> ring of 16 rows, and to HBM for the strip's own pixels
  *   determinant   -> ring of 16 rows
  *   3x3 maxima above the threshold inside the border range.
+ * Lx, Ly and the determinant are formed for row pairs (r, r + ST), which
+ * share their two middle tap rows; a warp takes one pair on half of the
+ * columns.  Block k + 1's Lx, Ly rows are formed in the same phase as block
+ * k's maxima, so a block costs two barriers.
  * Column grids (image x of column 0):
  *   D (Lx, Ly)     tx0 - A,        128 columns = 64 aligned pairs, A = ST+1 rounded up to even
  *   S (Lsmooth)    tx0 - A - ST,   128 + 2 ST columns; D column d has its taps at S d, d+ST, d+2ST
