@@ -398,6 +398,7 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS, AKZ_DESC_CTAS) k_describe
 
 #define AKZ_DESC_MAXDEV 64
 static bool akz_describe_tables_ready[AKZ_DESC_MAXDEV];
+static int akz_describe_grid[AKZ_DESC_MAXDEV]; /* resident CTAs of the device (with the largest offset table) */
 static std::mutex akz_describe_tables_mutex;
 
 static cudaError_t akz_init_describe_tables()
@@ -447,22 +448,27 @@ cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaS
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= AKZ_DESC_MAXDEV || p.pattern_size < 1 || p.pattern_size > 10) return cudaErrorInvalidValue;
+  int resident = 0;
   {
     std::lock_guard<std::mutex> lock(akz_describe_tables_mutex);
     if (!akz_describe_tables_ready[dev]) {
-      const cudaError_t e = akz_init_describe_tables();
+      cudaError_t e = akz_init_describe_tables();
       if (e != cudaSuccess) return e;
+      /* a grid-stride loop over the keypoints: one wave of resident CTAs,
+       * counted once per device with the largest keypoint-offset table */
+      int per_sm = 0, nsm = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_describe, 32 * AKZ_DESC_WARPS,
+                                                        (AKZ_DESC_MAXIMG + 1) * sizeof(int));
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      akz_describe_grid[dev] = std::max(1, per_sm) * std::max(1, nsm);
       akz_describe_tables_ready[dev] = true;
     }
+    resident = akz_describe_grid[dev];
   }
   if (nblocks <= 0) return cudaSuccess;
   const size_t dyn = p.t.nimg <= AKZ_DESC_MAXIMG ? (size_t)(p.t.nimg + 1) * sizeof(int) : 0;
-  /* a grid-stride loop over the keypoints: one wave of resident CTAs */
-  int per_sm = 0, nsm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_describe, 32 * AKZ_DESC_WARPS, dyn) != cudaSuccess ||
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    return cudaErrorInvalidValue;
-  const int grid = std::min(nblocks, std::max(1, per_sm) * nsm);
+  const int grid = std::min(nblocks, resident);
   k_describe<<<grid, 32 * AKZ_DESC_WARPS, dyn, s>>>(p);
   return cudaGetLastError();
 }
