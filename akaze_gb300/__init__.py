@@ -369,6 +369,10 @@ class Batch:
                                              ctypes.byref(rounds), ctypes.byref(kc)))
         return nraw.value, nkp.value, rounds.value, kc.value
 
+    def set_nms_round_cap(self, cap):
+        """Suppression rounds before an image reports AKZ_ERR_TIMEOUT (default 2^20)."""
+        check(self._lib.akz_batch_set_nms_round_cap(self._h, int(cap)))
+
     def submit(self, imgs):
         """First half of detect_describe_packed: enqueues the upload, the
         graph and the count read-back, and returns at once; the images must

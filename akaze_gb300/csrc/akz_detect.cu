@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <climits>
 
+#include "../../include/akaze_gb300.h"
 #include "akz_device.cuh"
 #include "akz_fmath.h"
 
@@ -826,7 +827,7 @@ __global__ void __cluster_dims__(AKZ_NMS_CL, 1, 1) __launch_bounds__(AKZ_NMS_THR
     }
     cl.sync();
     if (++rounds > p.max_rounds) {
-      if (rank == 0 && tid == 0) stats->status = 5; /* AKZ_ERR_TIMEOUT */
+      if (rank == 0 && tid == 0) stats->status = (int)AKZ_ERR_TIMEOUT;
       break;
     }
   }

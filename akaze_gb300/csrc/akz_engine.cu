@@ -321,6 +321,7 @@ struct akz_batch {
   cudaStream_t graph_stream = nullptr;
   akz_image_stats *h_stats = nullptr;
   int nsm = 152;
+  int nms_round_cap = 1 << 20; /* suppression rounds before AKZ_ERR_TIMEOUT */
   cudaEvent_t ev[9] = {}; /* 0-7 stage timing, 8 submit/collect */
 };
 
@@ -903,7 +904,7 @@ static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s, cudaEvent_t *pe
   np.aux = b->d_aux;
   np.decision = b->d_dec;
   np.kp = b->d_kp;
-  np.max_rounds = 1 << 20;
+  np.max_rounds = b->nms_round_cap;
   np.nbr = b->d_nbr;
   np.nbc = b->d_nbc;
   CK(akz_launch_nms(np, s));
@@ -1603,6 +1604,18 @@ static void akz_use_fed_depths(akz_batch *b)
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
+}
+
+AKZ_API akz_status akz_batch_set_nms_round_cap(akz_batch *b, int cap)
+{
+  AKZ_GUARD(b);
+  if (cap < 1) return akz_report(AKZ_ERR_INVALID_ARG, "akz_batch_set_nms_round_cap: cap must be >= 1");
+  b->nms_round_cap = cap;
+  if (b->graph) { /* the captured graph holds the old cap */
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  return AKZ_OK;
 }
 
 AKZ_API akz_status akz_batch_set_fed_depth(akz_batch *b, int depth)

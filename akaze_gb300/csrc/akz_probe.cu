@@ -11,6 +11,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include "../../include/akaze_gb300.h"
 
 akz_status akz_report(akz_status s, const char *msg);
@@ -64,5 +66,46 @@ extern "C" AKZ_API akz_status akz_measure_popc_rate(int iters, double *triples_p
   if (sink) cudaFree(sink);
   if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
   *triples_per_s = (double)blocks * threads * AKZ_POPC_CHAINS * (double)iters / (ms * 1e-3);
+  return AKZ_OK;
+}
+
+/* The bounded mbarrier wait of k_fed's TMA input and of the tcgen05 kernels:
+ * poll try_wait at most spin times, then record a timeout and go on. */
+__global__ void k_wait_selfcheck(int arrive, int spin, int *timed_out)
+{
+  __shared__ __align__(8) unsigned long long mbar;
+  const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  __syncthreads();
+  if (arrive && threadIdx.x == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mb) : "memory");
+  uint32_t done = 0;
+  for (int it = 0; it < spin && !done; it++)
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done)
+                 : "r"(mb)
+                 : "memory");
+  if (__syncthreads_or(!done) && threadIdx.x == 0) *timed_out = 1;
+}
+
+static __device__ int g_wait_selfcheck;
+
+extern "C" AKZ_API akz_status akz_selfcheck_bounded_wait(int arrive, int spin, int *timed_out)
+{
+  if (!timed_out || spin < 1) return akz_report(AKZ_ERR_INVALID_ARG, "akz_selfcheck_bounded_wait: bad arguments");
+  int *flag = nullptr;
+  const int zero = 0;
+  cudaError_t e = cudaGetSymbolAddress((void **)&flag, g_wait_selfcheck);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_wait_selfcheck, &zero, sizeof(int));
+  if (e == cudaSuccess) {
+    k_wait_selfcheck<<<1, 128>>>(arrive ? 1 : 0, spin, flag);
+    e = cudaGetLastError();
+  }
+  int v = 0;
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(&v, g_wait_selfcheck, sizeof(int));
+  if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
+  *timed_out = v;
   return AKZ_OK;
 }

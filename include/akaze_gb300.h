@@ -227,6 +227,14 @@ AKZ_API akz_status akz_matcher_bfmatch_noalloc(const uint8_t *query64, int nq, c
  * *triples_per_s / 16.  Synchronises stream; allocates 4 bytes. */
 AKZ_API akz_status akz_measure_popc_rate(int iters, double *triples_per_s, void *stream);
 
+/* Self-check of the bounded mbarrier wait that the level kernel uses for its
+ * TMA input and the tcgen05 kernels for their MMAs: one CTA polls an
+ * mbarrier at most spin times.  With arrive = 0 nothing completes the
+ * barrier and the wait must give up (*timed_out = 1); with arrive = 1 the
+ * CTA's first thread completes it and the wait must succeed (*timed_out =
+ * 0).  Synchronous; no fault, no hang. */
+AKZ_API akz_status akz_selfcheck_bounded_wait(int arrive, int spin, int *timed_out);
+
 /* ------------------------------------------------------------------------ */
 /* Learned FED surrogate (no counterpart in the reference; it replaces the
  * FED cycle of AKAZE.cpp:244-270 for octaves >= 1 when enabled).  A 5-layer
@@ -302,6 +310,12 @@ AKZ_API akz_status akz_batch_set_fed_depth(akz_batch *b, int depth);
  * and the contrast factor.  Any pointer may be NULL; synchronises the
  * batch's stream. */
 AKZ_API akz_status akz_batch_image_info(akz_batch *b, int i, int *nraw, int *nkp, int *rounds, float *kcontrast);
+
+/* Cap on the suppression rounds of every image (default 2^20, far above the
+ * n rounds the loop needs for n raw extrema).  An image that needs more
+ * rounds stops suppressing and its results report AKZ_ERR_TIMEOUT; the batch
+ * stays usable.  cap >= 1. */
+AKZ_API akz_status akz_batch_set_nms_round_cap(akz_batch *b, int cap);
 
 /* The two halves of akz_batch_detect_describe_packed, for overlapping
  * several batches (each on its own stream) from one host thread:

@@ -2,7 +2,12 @@
 factor 0, as compute_k_percentile gives it, so the PM-g2 conductance is
 0/0 and the levels are NaN on both sides; no keypoints), an image small
 enough to keep only octave 0, the largest benchmark size, the raw-extrema
-capacity overflow, and the matcher with an empty or one-row train set."""
+capacity overflow, and the matcher with an empty or one-row train set.
+Failure detection without a GPU fault: a bounded device wait that nothing
+completes gives up and reports it, and a suppression round cap that an image
+exceeds is reported as AKZ_ERR_TIMEOUT; the context stays usable after both."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -73,3 +78,38 @@ def test_matcher_with_empty_and_single_row_train(gpu_lib, oracle):
     empty = m.bfmatch(q, t[:0])
     assert np.all(empty["distance"] == 512) and np.all(empty["trainIdx"] == 0)
     assert empty.tobytes() == oracle.bfmatch(q, t[:0]).tobytes()
+
+
+def test_bounded_wait_gives_up_and_reports(gpu_lib):
+    lib = gpu_lib.load()
+    t = ctypes.c_int(-1)
+    assert lib.akz_selfcheck_bounded_wait(0, 1 << 14, ctypes.byref(t)) == 0
+    assert t.value == 1  # nothing completed the barrier: the wait gave up
+    assert lib.akz_selfcheck_bounded_wait(1, 1 << 24, ctypes.byref(t)) == 0
+    assert t.value == 0  # completed: the wait succeeded
+    # the context is still usable
+    img = synth.synth_image(3, 320, 240)
+    ak = _ak(gpu_lib, 320, 240)
+    ak.Create_Nonlinear_Scale_Space(img)
+    ak.Feature_Detection()
+    desc, kp = ak.Compute_Descriptors()
+    assert len(kp) > 0
+
+
+def test_suppression_round_cap_reports_timeout(gpu_lib):
+    img = synth.synth_image(7, 640, 480)
+    b = gpu_lib.Batch(gpu_lib.AKAZEOptions(), [(640, 480)])
+    b.upload([img])
+    b.run()
+    _, nkp, rounds, _ = b.image_info(0)
+    kp0, d0 = b.results(0)
+    assert rounds >= 2, rounds
+    b.set_nms_round_cap(1)
+    b.run()
+    with pytest.raises(gpu_lib.AkazeError) as e:
+        b.counts()
+    assert e.value.status == 5  # AKZ_ERR_TIMEOUT
+    b.set_nms_round_cap(1 << 20)
+    b.run()
+    kp1, d1 = b.results(0)
+    assert np.array_equal(kp0.view(np.uint8), kp1.view(np.uint8)) and np.array_equal(d0, d1)
