@@ -540,9 +540,12 @@ __device__ __forceinline__ float akz_conductance_m(float m, float inv_k, int typ
  * f = inv_k * m per lane, exactly as akz_recip1pf gives it.  The reciprocal
  * of s = fl(1 + f) starts from the hardware approximation (relative error
  * below 2^-22); one Newton step against the exact float-float sum s + lo
- * (Fast2Sum) leaves the value before the final rounding within about 2^-43
- * of 1 / (1 + f), inside the 2^-41 band of the rounding-midpoint test, so
- * every lane that could round differently takes the double evaluation. */
+ * (Fast2Sum) gives v = q + q r within about 2^-43 (relative) of 1 / (1 + f).
+ * The final rounding is taken twice, at v - q 2^-41 and v + q 2^-41 (r +- 2^-41
+ * is exact in float: |r| < 2^-21).  The true quotient lies between them, so
+ * where both round to the same float that float is its correct rounding; the
+ * lanes where they differ (a rounding midpoint within 2^-41 of v, about one
+ * in 2^17) take the double evaluation. */
 __device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
 {
   const float2 f = make_float2(inv_k * m.x, inv_k * m.y);
@@ -555,19 +558,13 @@ __device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(q.y) : "f"(s.y));
   const float2 nq = make_float2(-q.x, -q.y);
   const float2 r = f2fma(nq, lo, f2fma(nq, s, one)); /* 1 - q (s + lo) */
-  const float2 res = f2fma(q, r, q);
-  const float2 e = f2sub(make_float2(q.x * r.x, q.y * r.y), f2sub(res, q));
-  float out[2] = {res.x, res.y};
-  const float ff[2] = {f.x, f.y}, ee[2] = {e.x, e.y};
+  const float2 band = make_float2(0x1p-41f, 0x1p-41f);
+  const float2 lo_r = f2fma(q, f2sub(r, band), q), hi_r = f2fma(q, f2add(r, band), q);
+  float out[2] = {lo_r.x, lo_r.y};
+  const float ff[2] = {f.x, f.y}, hh[2] = {hi_r.x, hi_r.y};
 #pragma unroll
-  for (int k = 0; k < 2; k++) {
-    const unsigned int u = __float_as_uint(out[k]);
-    const float up = __uint_as_float((u & 0x7f800000u) - (23u << 23));
-    const float dn = (u & 0x007fffffu) ? up : up * 0.5f;
-    const float tol = up * 0x1p-18f, err = fabsf(ee[k]);
-    if (!(ff[k] <= 0x1p100f) || fabsf(err - 0.5f * up) <= tol || fabsf(err - 0.5f * dn) <= tol)
-      out[k] = (float)(1.0 / (1.0 + (double)ff[k]));
-  }
+  for (int k = 0; k < 2; k++)
+    if (!(ff[k] <= 0x1p100f) || out[k] != hh[k]) out[k] = (float)(1.0 / (1.0 + (double)ff[k]));
   return make_float2(out[0], out[1]);
 }
 
