@@ -540,7 +540,7 @@ __device__ __forceinline__ float akz_conductance_m(float m, float inv_k, int typ
  * f = inv_k * m per lane, exactly as akz_recip1pf gives it.  The reciprocal
  * of s = fl(1 + f) starts from the hardware approximation (relative error
  * below 2^-22); one Newton step against the exact float-float sum s + lo
- * (Fast2Sum) gives v = q + q r within about 2^-43 (relative) of 1 / (1 + f).
+ * (TwoSum) gives v = q + q r within about 2^-43 (relative) of 1 / (1 + f).
  * The final rounding is taken twice, at v - q 2^-41 and v + q 2^-41 (r +- 2^-41
  * is exact in float: |r| < 2^-21).  The true quotient lies between them, so
  * where both round to the same float that float is its correct rounding; the
@@ -551,8 +551,8 @@ __device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
   const float2 f = make_float2(inv_k * m.x, inv_k * m.y);
   const float2 one = make_float2(1.0f, 1.0f);
   const float2 s = f2add(one, f);
-  const float2 a = f2sub(one, f2sub(s, f)), b = f2sub(f, f2sub(s, one)); /* Fast2Sum, both orderings */
-  const float2 lo = make_float2(f.x >= 1.0f ? a.x : b.x, f.y >= 1.0f ? a.y : b.y);
+  const float2 bb = f2sub(s, one); /* TwoSum: lo = 1 + f - s exactly, for any order of magnitude */
+  const float2 lo = f2add(f2sub(one, f2sub(s, bb)), f2sub(f, bb));
   float2 q;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(q.x) : "f"(s.x));
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(q.y) : "f"(s.y));
