@@ -143,7 +143,7 @@ class Matcher {
                                   desc_query.cols, out.data()));
     dmatches.assign((size_t)desc_query.rows, std::vector<cv::DMatch>(2));
     for (int i = 0; i < desc_query.rows; i++)
-      for (int k = 0; k < 2; k++) std::memcpy(&dmatches[i][k], &out[(size_t)2 * i + k], sizeof(cv::DMatch));
+      for (int k = 0; k < 2; k++) std::memcpy(static_cast<void *>(&dmatches[i][k]), &out[(size_t)2 * i + k], sizeof(cv::DMatch));
   }
 
  private:

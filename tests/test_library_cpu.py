@@ -75,3 +75,24 @@ def test_python_api_mirrors_reference_binding(gpu_lib):
         assert callable(getattr(gpu_lib.AKAZE, name))
     assert callable(gpu_lib.Matcher.BFMatch) and callable(gpu_lib.Matcher.bfmatch)
     assert gpu_lib.KEYPOINT_DTYPE.itemsize == 28 and gpu_lib.DMATCH_DTYPE.itemsize == 16
+
+
+def test_cxx_wrapper_compiles_and_links(gpu_lib, tmp_path):
+    """Code written against the reference's libAKAZECU class API builds
+    unchanged against include/libAKAZECU/AKAZE.h and links to the library
+    (tests/cxx/wrapper_usage.cpp; not run: it needs a GPU)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    root = Path(__file__).resolve().parent.parent
+    lib_dir = root / "akaze_gb300"
+    out = tmp_path / "wrapper_usage"
+    cmd = [cxx, "-std=c++17", "-Wall", "-Wextra", "-Werror", f"-I{root / 'include'}",
+           str(root / "tests" / "cxx" / "wrapper_usage.cpp"), f"-L{lib_dir}", "-lakaze_gb300",
+           f"-Wl,-rpath,{lib_dir}", "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(out)], capture_output=True).returncode == 0  # no arguments: returns before any GPU call
