@@ -160,7 +160,9 @@ static void *g_noalloc_addr[AKZ_NOALLOC_MAX_DEVICES];
 static int g_noalloc_sms[AKZ_NOALLOC_MAX_DEVICES];
 
 /* Device address of the scratch array on the current device, resolved once
- * per device (host code cannot use the symbol itself as a device pointer). */
+ * per device (host code cannot use the symbol itself as a device pointer).
+ * The address is kept for the life of the process; a cudaDeviceReset
+ * invalidates it, so the entry point is not for use after a reset. */
 static cudaError_t akz_noalloc_setup(int *dev_out, void **addr, int *nsm)
 {
   int dev = 0;

@@ -35,7 +35,14 @@ static inline int ako_refl101(int i, int n)
 }
 
 /* Per-axis INTER_AREA weight table (pixel-area relation): for each
- * destination index the source indices and weights, in ascending order. */
+ * destination index the source indices and weights, in ascending order.
+ * The reference half-samples odd sizes with cv::resize(INTER_AREA)
+ * (nldiffusion_functions.cpp:320-324); to give its bits, the table follows
+ * the construction of OpenCV's computeResizeAreaTab (modules/imgproc/src/
+ * resize.cpp; OpenCV, Apache License 2.0 for 4.x, 3-clause BSD before):
+ * destination cell [d*scale, (d+1)*scale) clipped to the source, a leading
+ * and a trailing partial pixel kept only when their overlap exceeds 1e-3,
+ * weights = overlap / cell width. */
 typedef struct {
   int *start; /* dsize+1 */
   int *si;
@@ -336,6 +343,68 @@ void ako_u8_to_unit(const uint8_t *src, float *dst, long n)
 {
   const float s = (float)(1.0 / 255.0);
   for (long i = 0; i < n; i++) dst[i] = (float)src[i] * s;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The oracle's scale-space stages on single planes, exported so that the
+ * reference's own nldiffusion_functions.cpp, compiled by oracle/Makefile
+ * target "ref" over an OpenCV-shaped shim, can be checked against them
+ * (its GaussianBlur, Scharr and resize calls route here). */
+
+/* Gaussian of sigma with the oracle's kernel-size rule; *ksize receives the
+ * kernel size used. */
+int ako_plane_gaussian(const float *src, float *dst, int w, int h, float sigma, int *ksize)
+{
+  const int R = ako_gauss_R(sigma);
+  if (R > 64 || w < 1 || h < 1) return -1;
+  double kd[129];
+  float k[129];
+  ako_gauss_taps_d(sigma, R, kd);
+  for (int i = 0; i <= 2 * R; i++) k[i] = (float)kd[i];
+  float *tmp = (float *)malloc(sizeof(float) * (size_t)w * h);
+  if (!tmp) return -1;
+  ako_gauss_f32(src, dst, tmp, w, h, k, R);
+  free(tmp);
+  if (ksize) *ksize = 2 * R + 1;
+  return 0;
+}
+
+void ako_plane_scharr(const float *src, float *lx, float *ly, int w, int h) { ako_scharr_f32(src, lx, ly, w, h); }
+
+void ako_plane_halfsample(const float *src, int sw, int sh, float *dst, int dw, int dh)
+{
+  ako_halfsample_f32(src, sw, sh, dst, dw, dh);
+}
+
+void ako_plane_conductance(const float *lx, const float *ly, float *dst, long n, float k, int type)
+{
+  ako_conductance_f32(lx, ly, dst, (size_t)n, k, type);
+}
+
+void ako_plane_nld_step(float *Ld, const float *c, int w, int h, float stepsize)
+{
+  float *Lstep = (float *)calloc((size_t)w * h, sizeof(float));
+  if (!Lstep) return;
+  ako_nld_step_f32(Ld, c, Lstep, w, h, stepsize);
+  free(Lstep);
+}
+
+/* compute_k_percentile(img, perc, gscale, nbins, 0, 0) as the oracle
+ * evaluates it. */
+float ako_plane_k_percentile(const float *img, int w, int h, float perc, int nbins, float gscale)
+{
+  const int R = ako_gauss_R(gscale);
+  if (R > 64) return -1.0f;
+  double kd[129];
+  float k[129];
+  ako_gauss_taps_d(gscale, R, kd);
+  for (int i = 0; i <= 2 * R; i++) k[i] = (float)kd[i];
+  const size_t n = (size_t)w * h;
+  float *buf = (float *)malloc(sizeof(float) * n * 4);
+  if (!buf) return -1.0f;
+  const float r = ako_k_percentile_f32(img, w, h, perc, nbins, k, R, buf, buf + n, buf + 2 * n, buf + 3 * n);
+  free(buf);
+  return r;
 }
 
 /* AKAZE.cpp:211-276 with the reference CPU functions (the upstream CPU
@@ -917,15 +986,21 @@ int ako_run_u8(ako_ctx *c, const uint8_t *img)
 int ako_bfmatch(const uint8_t *q, int nq, const uint8_t *t, int nt, int row_bytes, ako_dmatch *out)
 {
   if (nq < 0 || nt < 0 || row_bytes < 1 || row_bytes > 64) return -1;
+  /* Rows zero-padded to 8 64-bit words: the Hamming distance is the sum of
+   * the words' xor popcounts, the same integer as the byte-wise sum. */
+  uint64_t *tw = (uint64_t *)calloc((size_t)(nt > 0 ? nt : 1) * 8, sizeof(uint64_t));
+  if (!tw) return -1;
+  for (int j = 0; j < nt; j++) memcpy(tw + (size_t)j * 8, t + (size_t)j * row_bytes, (size_t)row_bytes);
   int i;
 #pragma omp parallel for schedule(dynamic, 64)
   for (i = 0; i < nq; i++) {
+    uint64_t a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    memcpy(a, q + (size_t)i * row_bytes, (size_t)row_bytes);
     int bd = 512, bi = 0, sd = 512, si = 0;
-    const uint8_t *a = q + (size_t)i * row_bytes;
     for (int j = 0; j < nt; j++) {
-      const uint8_t *b = t + (size_t)j * row_bytes;
+      const uint64_t *b = tw + (size_t)j * 8;
       int d = 0;
-      for (int k = 0; k < row_bytes; k++) d += __builtin_popcount((unsigned)(a[k] ^ b[k]));
+      for (int k = 0; k < 8; k++) d += __builtin_popcountll(a[k] ^ b[k]);
       if (d < bd) {
         sd = bd;
         si = bi;
@@ -939,6 +1014,7 @@ int ako_bfmatch(const uint8_t *q, int nq, const uint8_t *t, int nt, int row_byte
     out[2 * i] = (ako_dmatch){i, bi, 0, (float)bd};
     out[2 * i + 1] = (ako_dmatch){i, si, 0, (float)sd};
   }
+  free(tw);
   return 0;
 }
 
