@@ -178,7 +178,13 @@ static int akz_gauss_taps(float sigma, float *taps)
   return R;
 }
 
-/* Per-axis INTER_AREA tables (same construction as the CPU restatement). */
+/* Per-axis INTER_AREA tables for odd-size half-sampling, which the reference
+ * does with cv::resize(INTER_AREA) (nldiffusion_functions.cpp:320-324).  To
+ * give OpenCV's bits, the construction follows OpenCV's computeResizeAreaTab
+ * (modules/imgproc/src/resize.cpp; OpenCV, Apache License 2.0 for 4.x,
+ * 3-clause BSD before): destination cell [d*scale, (d+1)*scale) clipped to
+ * the source, a leading and a trailing partial pixel kept only when their
+ * overlap exceeds 1e-3, weights = overlap / cell width. */
 static void akz_area_tab(int ssize, int dsize, std::vector<int> &start, std::vector<int> &si, std::vector<float> &alpha)
 {
   const double scale = (double)ssize / dsize;
@@ -218,6 +224,9 @@ static akz_status akz_validate(const akz_options *o)
     return akz_fail(AKZ_ERR_UNSUPPORTED, "descriptor %d is not implemented (MLDB and MLDB_UPRIGHT are)", o->descriptor);
   if (o->descriptor_size != 0)
     return akz_fail(AKZ_ERR_UNSUPPORTED, "descriptor_size %d: only the full 486-bit M-LDB is implemented", o->descriptor_size);
+  if (o->descriptor_channels != 3)
+    return akz_fail(AKZ_ERR_UNSUPPORTED, "descriptor_channels %d: only the 3-channel M-LDB is implemented",
+                    o->descriptor_channels);
   if (o->descriptor_pattern_size < 1 || o->descriptor_pattern_size > 10)
     return akz_fail(AKZ_ERR_INVALID_ARG, "descriptor_pattern_size must be in [1, 10]");
   if (o->kcontrast_nbins < 1 || o->kcontrast_nbins > AKZ_MAX_NBINS)

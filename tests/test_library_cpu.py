@@ -42,6 +42,8 @@ def test_defaults_mirror_akazeoptions(gpu_lib):
 @pytest.mark.parametrize("field,value,status", [
     ("descriptor", 1, 6),            # SURF: not implemented (the reference prints the same)
     ("descriptor_size", 64, 6),      # random bit subsets: not implemented
+    ("descriptor_channels", 2, 6),   # only the 3-channel row; never a silently wrong row size
+    ("descriptor_channels", 1, 6),
     ("omax", 0, 1),
     ("kcontrast_nbins", 0, 1),
     ("soffset", 0.1, 1),
@@ -77,10 +79,7 @@ def test_python_api_mirrors_reference_binding(gpu_lib):
     assert gpu_lib.KEYPOINT_DTYPE.itemsize == 28 and gpu_lib.DMATCH_DTYPE.itemsize == 16
 
 
-def test_cxx_wrapper_compiles_and_links(gpu_lib, tmp_path):
-    """Code written against the reference's libAKAZECU class API builds
-    unchanged against include/libAKAZECU/AKAZE.h and links to the library
-    (tests/cxx/wrapper_usage.cpp; not run: it needs a GPU)."""
+def _build_wrapper_usage(tmp_path, opencv_branch):
     import shutil
     import subprocess
     from pathlib import Path
@@ -89,10 +88,39 @@ def test_cxx_wrapper_compiles_and_links(gpu_lib, tmp_path):
         pytest.skip("no C++ compiler")
     root = Path(__file__).resolve().parent.parent
     lib_dir = root / "akaze_gb300"
-    out = tmp_path / "wrapper_usage"
-    cmd = [cxx, "-std=c++17", "-Wall", "-Wextra", "-Werror", f"-I{root / 'include'}",
+    out = tmp_path / ("wrapper_usage_cv" if opencv_branch else "wrapper_usage")
+    extra = ["-DAKZ_WITH_OPENCV", f"-I{root / 'tests' / 'cxx' / 'opencv_stub'}"] if opencv_branch else []
+    cmd = [cxx, "-std=c++17", "-Wall", "-Wextra", "-Werror"] + extra + [f"-I{root / 'include'}",
            str(root / "tests" / "cxx" / "wrapper_usage.cpp"), f"-L{lib_dir}", "-lakaze_gb300",
            f"-Wl,-rpath,{lib_dir}", "-o", str(out)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    assert subprocess.run([str(out)], capture_output=True).returncode == 0  # no arguments: returns before any GPU call
+    return out
+
+
+@pytest.mark.parametrize("opencv_branch", [False, True])
+def test_cxx_wrapper_compiles_and_links(gpu_lib, tmp_path, opencv_branch):
+    """Code in the reference demos' dialect (DESCRIPTOR_TYPE(atoi(..)),
+    PM_G2, unqualified CV_32F / CV_8UC1, convertTo, operator<< on the
+    options, setDefaultAKAZEOptions, Matcher, MatchDescriptors) builds
+    unchanged against include/libAKAZECU/AKAZE.h, with its own cv subset and
+    with AKZ_WITH_OPENCV against an OpenCV-shaped header, and links to the
+    library.  Run without --run it parses and prints the options only."""
+    import subprocess
+    out = _build_wrapper_usage(tmp_path, opencv_branch)
+    r = subprocess.run([str(out)], capture_output=True, text=True)
+    assert r.returncode == 0
+    lines = r.stdout.splitlines()
+    assert lines[0] == "Check AKAZE options:"
+    # AKAZEConfig.h:145-172: names left-aligned in 33 columns, then " =  value"
+    assert lines[1] == "akaze_options.omax".ljust(33) + " =  4"
+    assert "akaze_options.diffusivity".ljust(33) + " =  1" in lines
+    assert "akaze_options.descriptor".ljust(33) + " =  5" in lines
+    assert "akaze_options.descriptor_channels".ljust(33) + " =  3" in lines
+    r = subprocess.run([str(out), "--descriptor", "4", "--diffusivity", "2", "--omax", "3"], capture_output=True, text=True)
+    assert r.returncode == 0
+    assert "akaze_options.descriptor".ljust(33) + " =  4" in r.stdout.splitlines()
+    assert "akaze_options.diffusivity".ljust(33) + " =  2" in r.stdout.splitlines()
+    assert "upright, other diffusivity" in r.stdout
+    r = subprocess.run([str(out), "--descriptor", "9"], capture_output=True, text=True)  # out of range -> MLDB
+    assert "akaze_options.descriptor".ljust(33) + " =  5" in r.stdout.splitlines()
