@@ -489,10 +489,14 @@ class BatchGroup:
         return counts
 
 
-def save_keypoints(path, kpts, desc=None):
-    """save_keypoints (utils.cpp:97-152): Mikolajczyk text format."""
+def save_keypoints(path, kpts, desc=None, save_desc=None):
+    """save_keypoints (utils.cpp:97-152): Mikolajczyk text format.  save_desc
+    (default: desc given) only sets the header's descriptor length; as in
+    the reference, rows carry desc's bytes whenever desc is given."""
     kp = np.ascontiguousarray(kpts, KEYPOINT_DTYPE)
     d = None if desc is None else np.ascontiguousarray(desc, np.uint8)
+    if save_desc is None:
+        save_desc = d is not None
     check(load().akz_save_keypoints(str(path).encode(), _ptr(kp) if kp.size else None, len(kp),
                                     _ptr(d) if d is not None and d.size else None,
-                                    0 if d is None else d.shape[1], int(d is not None)))
+                                    0 if d is None else d.shape[1], int(bool(save_desc))))

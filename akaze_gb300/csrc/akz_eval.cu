@@ -71,11 +71,14 @@ extern "C" AKZ_API akz_status akz_nndr_homography_inliers(const akz_dmatch *matc
 extern "C" AKZ_API akz_status akz_save_keypoints(const char *path, const akz_keypoint *kpts, int n, const uint8_t *desc,
                                                 int desc_bytes, int save_desc)
 {
-  if (!path || n < 0 || (n > 0 && !kpts) || (save_desc && (desc_bytes < 0 || (n > 0 && desc_bytes > 0 && !desc))))
+  if (!path || n < 0 || (n > 0 && !kpts) || desc_bytes < 0 || (n > 0 && desc_bytes > 0 && !desc))
     return akz_report(AKZ_ERR_INVALID_ARG, "akz_save_keypoints: bad arguments");
   std::ofstream f(path);
   if (!f) return akz_report(AKZ_ERR_INVALID_ARG, "akz_save_keypoints: cannot open the file");
-  const int dsize = save_desc ? desc_bytes : 0;
+  /* As the reference writes it: the header says 1 without save_desc, yet
+   * every row carries the descriptor bytes it is given (utils.cpp:103,
+   * :114-118, :133-141). */
+  const int dsize = desc_bytes;
   f << (save_desc ? dsize : 1) << std::endl << n << std::endl;
   for (int i = 0; i < n; i++) {
     float sc = kpts[i].size;

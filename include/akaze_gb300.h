@@ -212,7 +212,10 @@ AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *que
  * scratch is a fixed 2 MiB device array inside the library, held by every
  * GPU that loads it until exit.  At most 131072 query rows per call (larger
  * nq returns AKZ_ERR_INVALID_ARG).  The first call on a device resolves the
- * array's address; make that first call before any stream capture.  Calls
+ * array's address and keeps it for the life of the process; make that first
+ * call before any stream capture, and do not call this entry point again
+ * after a cudaDeviceReset in the same process (the kept address would then
+ * be stale).  Calls
  * share the array, so calls that overlap on the GPU race: serialise them.
  * Runs on stream (a cudaStream_t; NULL for the legacy default stream) and
  * returns without synchronising. */
@@ -363,7 +366,10 @@ AKZ_API akz_status akz_nndr_homography_inliers(const akz_dmatch *matches, int nq
 
 /* save_keypoints (utils.cpp:97-152): the Krystian Mikolajczyk text format,
  * "x y 1/r^2 0 1/r^2 [descriptor bytes]" per keypoint with r = size, after a
- * header of the descriptor length (1 without descriptors) and the count.
+ * header of the descriptor length (1 when save_desc is 0) and the count.
+ * As in the reference, every row carries its desc_bytes descriptor bytes
+ * whatever save_desc says (desc_bytes 0: none; desc may be NULL then, or
+ * when n is 0).
  * Host memory. */
 AKZ_API akz_status akz_save_keypoints(const char *path, const akz_keypoint *kpts, int n, const uint8_t *desc,
                                       int desc_bytes, int save_desc);

@@ -45,12 +45,21 @@ EXTREMUM_DTYPE = np.dtype([("x", "<i4"), ("y", "<i4"), ("level", "<i4"), ("octav
 PLANES = {"Lt": 0, "Lsmooth": 1, "Lflow": 2, "Lx": 3, "Ly": 4, "Ldet": 5}
 
 
+def reference_dir():
+    """The reference source tree: $AKZ_REFERENCE_DIR, else a `reference`
+    directory beside the repository (absent on machines without it)."""
+    env = os.environ.get("AKZ_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.normpath(os.path.join(_HERE, "..", "..", "reference"))
+
+
 def build(quiet=True):
     """Compile the oracle (and oracle/_ref when the reference tree exists)."""
     out = subprocess.run(["make", "-C", _HERE, "all"], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
-    ref_src = os.environ.get("AKZ_REFERENCE_DIR", "/root/reference")
+    ref_src = reference_dir()
     if os.path.isfile(os.path.join(ref_src, "src", "lib", "fed.cpp")):
         out = subprocess.run(["make", "-C", _HERE, "ref", "REF=" + ref_src], capture_output=True, text=True)
         if out.returncode != 0:
@@ -133,6 +142,77 @@ def fed_tau_reference(T, M=1, tau_max=0.25, reordering=True, cap=4096):
     buf = np.zeros(cap, np.float32)
     n = R.fedref_tau_by_process_time(float(T), int(M), float(tau_max), int(bool(reordering)), buf.ctypes.data, cap)
     return buf[:n].copy()
+
+
+_NLD_REF_PATH = os.path.join(_HERE, "_ref", "libnld_ref.so")
+_nld_ref = None
+
+
+def nld_ref():
+    """The reference's own nldiffusion_functions.cpp and utils.cpp
+    (oracle/_ref/libnld_ref.so, built where the reference tree is present);
+    None if not built."""
+    global _nld_ref
+    if _nld_ref is None and os.path.exists(_NLD_REF_PATH):
+        lib()  # the shim routes its filters to the oracle library, load it first
+        R = ctypes.CDLL(_NLD_REF_PATH)
+        P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        R.nldref_pm_g2.argtypes = [P, P, P, I, I, F]
+        R.nldref_nld_step.argtypes = [P, P, I, I, F]
+        R.nldref_k_percentile.argtypes = [P, I, I, F, F, I, P]
+        R.nldref_k_percentile.restype = F
+        R.nldref_gaussian.argtypes = [P, P, I, I, F, P]
+        R.utilsref_save_keypoints.argtypes = [ctypes.c_char_p, P, I, P, I, I]
+        R.utilsref_nndr_inliers.argtypes = [P, I, P, I, P, I, P, F, F, P, P, P]
+        _nld_ref = R
+    return _nld_ref
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def plane_conductance(lx, ly, k, kind=1):
+    """The oracle's conductance (kind 1 = PM-g2) of (lx, ly) planes."""
+    lx, ly = _f32(lx), _f32(ly)
+    out = np.empty_like(lx)
+    L = lib()
+    L.ako_plane_conductance.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_long, ctypes.c_float, ctypes.c_int]
+    L.ako_plane_conductance(lx.ctypes.data, ly.ctypes.data, out.ctypes.data, lx.size, float(k), int(kind))
+    return out
+
+
+def plane_nld_step(Ld, c, stepsize):
+    """One oracle FED step of Ld (h x w) with conductance c."""
+    out, c = _f32(Ld).copy(), _f32(c)
+    L = lib()
+    L.ako_plane_nld_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float]
+    L.ako_plane_nld_step(out.ctypes.data, c.ctypes.data, out.shape[1], out.shape[0], float(stepsize))
+    return out
+
+
+def plane_k_percentile(img, perc=0.7, nbins=300, gscale=1.0):
+    img = _f32(img)
+    L = lib()
+    L.ako_plane_k_percentile.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int,
+                                         ctypes.c_float]
+    L.ako_plane_k_percentile.restype = ctypes.c_float
+    return np.float32(L.ako_plane_k_percentile(img.ctypes.data, img.shape[1], img.shape[0], float(perc), int(nbins),
+                                               float(gscale)))
+
+
+def plane_gaussian(img, sigma):
+    """The oracle's Gaussian of sigma and the kernel size it used."""
+    img = _f32(img)
+    out = np.empty_like(img)
+    ks = ctypes.c_int(0)
+    L = lib()
+    L.ako_plane_gaussian.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                     ctypes.c_void_p]
+    if L.ako_plane_gaussian(img.ctypes.data, out.ctypes.data, img.shape[1], img.shape[0], float(sigma),
+                            ctypes.byref(ks)) != 0:
+        raise ValueError(sigma)
+    return out, ks.value
 
 
 def gaussian_taps(sigma):
