@@ -73,6 +73,8 @@ def parse():
                          "uneven64: 64 images of uneven sizes, images/s and per-image latency; "
                          "matcher: 2-NN sweep N=M 1024..131072, Gmatch/s against the popc roofline; "
                          "surrogate4k: 3840x2160, 6x4 levels, plain FED vs the learned surrogate")
+    ap.add_argument("--matcher-n", type=int, nargs="*", default=None,
+                    help="matcher: the N=M sizes to run (default 1024, 2048, ..., 131072)")
     return ap.parse_args()
 
 
@@ -394,8 +396,9 @@ def workload_matcher(args):
     m = akz.Matcher()
     m.set_stream(stream.cuda_stream)
     rows = []
-    for k in range(8):
-        N = 1024 << k
+    sizes = args.matcher_n or [1024 << k for k in range(8)]
+    for N in sizes:
+        k = max(0, int(N).bit_length() - 11)
         q61, t61 = synth.matcher_rows(5000 + k, N, N)
         q64 = np.zeros((N, 64), np.uint8)
         t64 = np.zeros((N, 64), np.uint8)
