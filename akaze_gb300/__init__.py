@@ -72,6 +72,13 @@ def gaussian_taps(sigma):
     return t[: n.value].copy()
 
 
+def descriptor_bytes(options):
+    """Bytes of one descriptor row for the options (AKAZE.cpp:412-423)."""
+    b = ctypes.c_int()
+    check(load().akz_descriptor_bytes(ctypes.byref(options), ctypes.byref(b)))
+    return b.value
+
+
 class AKAZE:
     """libAKAZECU::AKAZE (AKAZE.h:58-143) over the C ABI."""
 
@@ -120,10 +127,10 @@ class AKAZE:
         return n.value
 
     def Compute_Descriptors(self):
-        """Orientation + M-LDB; returns (descriptors n x 61 uint8, keypoints)."""
+        """Orientation + M-LDB; returns (descriptors n x row bytes uint8, keypoints)."""
         n = self._n
         kp = np.zeros(n, KEYPOINT_DTYPE)
-        d = np.zeros((n, 61), np.uint8)
+        d = np.zeros((n, descriptor_bytes(self.options)), np.uint8)
         m = ctypes.c_int()
         check(self._lib.akz_compute_descriptors(self._h, _ptr(kp), _ptr(d), n, ctypes.byref(m)))
         return d[: m.value], kp[: m.value]
@@ -273,7 +280,7 @@ class Batch:
         n = ctypes.c_int()
         check(self._lib.akz_batch_results(self._h, i, None, None, 0, ctypes.byref(n)))
         kp = np.zeros(n.value, KEYPOINT_DTYPE)
-        d = np.zeros((n.value, 61), np.uint8)
+        d = np.zeros((n.value, descriptor_bytes(self.options)), np.uint8)
         check(self._lib.akz_batch_results(self._h, i, _ptr(kp), _ptr(d), n.value, ctypes.byref(n)))
         return kp, d
 
@@ -334,7 +341,7 @@ class Batch:
         cap = capacity or self.options.maxkeypoints
         if not hasattr(self, "_out") or self._out[0] != cap:
             kps = [np.zeros(cap, KEYPOINT_DTYPE) for _ in range(self.n)]
-            ds = [np.zeros((cap, 61), np.uint8) for _ in range(self.n)]
+            ds = [np.zeros((cap, descriptor_bytes(self.options)), np.uint8) for _ in range(self.n)]
             self._out = (cap, kps, ds)
         _, kps, ds = self._out
         return self.detect_describe_into(imgs, kps, ds)
@@ -351,7 +358,7 @@ class Batch:
 
     def detect_describe_packed(self, imgs, kp_out, d_out):
         """Whole job with packed output: kp_out (capacity records) and d_out
-        (capacity x 61) receive all images' results back to back; returns
+        (capacity x descriptor_bytes(options)) receive all images' results back to back; returns
         the per-image counts."""
         ptrs = (ctypes.c_void_p * self.n)(*[im.ctypes.data for im in imgs])
         strides = (ctypes.c_size_t * self.n)(*[im.strides[0] for im in imgs])

@@ -32,7 +32,7 @@ EXPORTS = [
     "akz_batch_surrogate_errors", "akz_nndr_homography_inliers", "akz_save_keypoints",
     "akz_batch_detect_describe_packed", "akz_sg_set_tcgen05", "akz_sg_tcgen05_status", "akz_selfcheck_pm_g2",
     "akz_batch_autotune", "akz_batch_set_fed_depth", "akz_batch_submit", "akz_batch_collect_packed",
-    "akz_batch_image_info", "akz_batch_set_nms_round_cap", "akz_selfcheck_bounded_wait",
+    "akz_batch_image_info", "akz_batch_set_nms_round_cap", "akz_selfcheck_bounded_wait", "akz_descriptor_bytes",
 ]
 
 
@@ -46,7 +46,7 @@ class AkzOptions(ctypes.Structure):
         ("descriptor_pattern_size", ctypes.c_int), ("kcontrast", ctypes.c_float),
         ("kcontrast_percentile", ctypes.c_float), ("kcontrast_nbins", ctypes.c_size_t),
         ("save_scale_space", ctypes.c_int), ("save_keypoints", ctypes.c_int), ("verbosity", ctypes.c_int),
-        ("ncudaimages", ctypes.c_int), ("maxkeypoints", ctypes.c_int),
+        ("ncudaimages", ctypes.c_int), ("maxkeypoints", ctypes.c_int), ("extrema_3d", ctypes.c_int),
     ]
 
 
@@ -78,6 +78,7 @@ def load():
     sig = {
         "akz_version": ([], ctypes.c_char_p), "akz_last_error": ([], ctypes.c_char_p),
         "akz_options_default": ([ctypes.POINTER(AkzOptions)], I),
+        "akz_descriptor_bytes": ([ctypes.POINTER(AkzOptions), IP], I),
         "akz_plan_info": ([ctypes.POINTER(AkzOptions), I, I, I, IP, IP, IP, IP, IP, ctypes.POINTER(ctypes.c_float), IP,
                            ctypes.POINTER(ctypes.c_float), P, I, IP], I),
         "akz_gaussian_taps": ([ctypes.c_float, P, I, IP], I),

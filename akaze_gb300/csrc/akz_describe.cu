@@ -8,7 +8,11 @@
  * samples rotated by the orientation at spacing round(size/2 / 2^octave),
  * three channels (L, rotated dx, rotated dy) summed into 2x2, 3x3 and 4x4
  * cells (87 sums) and 486 pairwise comparisons, written as 64-byte rows
- * (bits 486..511 zero) that the matcher reads directly.
+ * (bits 486..511 zero) that the matcher reads directly.  The comparisons
+ * come from a per-batch table: the full descriptor of 1, 2 or 3 channels
+ * (162 bits per channel; the second channel of a 2-channel descriptor is the
+ * gradient magnitude) or the random-bit subset of descriptor_size bits
+ * (AKAZE.cpp:412-423, :498-603).
  *
  * Sums are formed in a fixed order: sample order for the orientation bins,
  * and for the cells the reference's order (64 strided per-thread partials,
@@ -36,10 +40,6 @@
 
 /* orientation samples in the reference's thread order: tx = 16*(j+6) + (i+6) */
 __constant__ signed char c_oi[109], c_oj[109], c_or2[109];
-/* comparison pairs (cell*3 + channel) in bit order; read with one coalesced
- * load per warp and bit word (a __constant__ table would serialise the
- * lanes' different addresses) */
-__device__ unsigned char g_cmp1[512], g_cmp2[512];
 /* the M-LDB window's samples in the order the warp gathers them: 4 x 8
  * blocks of the window, so one gather instruction touches a compact patch
  * of the level (its sectors) rather than one and a half rotated rows; each
@@ -361,7 +361,8 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS, AKZ_DESC_CTAS) k_describe
           const int o = sOrd[idx], s = (o >> 8) * win + (o & 255);
           const float dx = vx[it], dy = vy[it];
           S.s[0][s] = vi[it];
-          S.s[1][s] = -dx * si + dy * co;
+          /* a 2-channel descriptor's second channel is the gradient magnitude (upstream libAKAZE's MLDB_Fill_Values) */
+          S.s[1][s] = p.channels == 2 ? __fsqrt_rn(dx * dx + dy * dy) : -dx * si + dy * co;
           S.s[2][s] = dx * co + dy * si;
         }
       }
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS, AKZ_DESC_CTAS) k_describe
       const float2 g2 = __ldg(reinterpret_cast<const float2 *>(lxyp + (long long)yp * (2 * pitch) + 2 * xp));
       const float dx = g2.x, dy = g2.y;
       S.s[0][s] = __ldg(ltp + (long long)yp * pitch + xp);
-      S.s[1][s] = -dx * si + dy * co;
+      S.s[1][s] = p.channels == 2 ? __fsqrt_rn(dx * dx + dy * dy) : -dx * si + dy * co;
       S.s[2][s] = dx * co + dy * si;
     }
     __syncwarp();
@@ -387,7 +388,7 @@ __global__ void __launch_bounds__(32 * AKZ_DESC_WARPS, AKZ_DESC_CTAS) k_describe
 #pragma unroll 4
     for (int w = 0; w < 16; w++) {
       const int bit = w * 32 + lane;
-      const bool v = bit < 486 && S.v[__ldg(&g_cmp1[bit])] > S.v[__ldg(&g_cmp2[bit])];
+      const bool v = bit < p.nbits && S.v[__ldg(&p.cmp1[bit])] > S.v[__ldg(&p.cmp2[bit])];
       const uint32_t word = __ballot_sync(0xffffffffu, v);
       if (lane == w) myword = word;
     }
@@ -423,24 +424,11 @@ static cudaError_t akz_init_describe_tables()
       n++;
     }
   }
-  unsigned char c1[512] = {0}, c2[512] = {0};
-  int m = 0;
-  const int g0[3] = {0, 4, 13}, g1[3] = {4, 13, 29};
-  for (int grid = 0; grid < 3; grid++)
-    for (int ch = 0; ch < 3; ch++)
-      for (int j = g0[grid]; j < g1[grid] - 1; j++)
-        for (int i = j + 1; i < g1[grid]; i++) {
-          c1[m] = (unsigned char)(3 * j + ch);
-          c2[m] = (unsigned char)(3 * i + ch);
-          m++;
-        }
   cudaError_t e;
   if ((e = cudaMemcpyToSymbol(c_oi, oi, sizeof(oi))) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_oj, oj, sizeof(oj))) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_or2, orr, sizeof(orr))) != cudaSuccess) return e;
-  if ((e = cudaMemcpyToSymbol(g_smp_order, ord, sizeof(ord))) != cudaSuccess) return e;
-  if ((e = cudaMemcpyToSymbol(g_cmp1, c1, sizeof(c1))) != cudaSuccess) return e;
-  return cudaMemcpyToSymbol(g_cmp2, c2, sizeof(c2));
+  return cudaMemcpyToSymbol(g_smp_order, ord, sizeof(ord));
 }
 
 cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaStream_t s)
@@ -473,10 +461,11 @@ cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaS
   return cudaGetLastError();
 }
 
-/* Packs every image's keypoints and 61-byte descriptor rows contiguously
- * (image i at offset sum_{j<i} nkp_j): blockIdx.x is the image, blockIdx.y
- * a slice of its rows; a thread copies whole rows. */
-__global__ void k_pack_results(akz_tables t, const akz_kp *kp, const uint32_t *desc, akz_kp *kp_out, uint8_t *desc_out)
+/* Packs every image's keypoints and descriptor rows (rb <= 64 bytes each)
+ * contiguously (image i at offset sum_{j<i} nkp_j): blockIdx.x is the image,
+ * blockIdx.y a slice of its rows; a thread copies whole rows. */
+__global__ void k_pack_results(akz_tables t, const akz_kp *kp, const uint32_t *desc, akz_kp *kp_out, uint8_t *desc_out,
+                               int rb)
 {
   const int img = blockIdx.x;
   int off = 0;
@@ -490,15 +479,20 @@ __global__ void k_pack_results(akz_tables t, const akz_kp *kp, const uint32_t *d
     uint4 *rw = (uint4 *)row;
 #pragma unroll
     for (int c = 0; c < 4; c++) rw[c] = src[c];
-    uint8_t *dst = desc_out + (long long)(off + k) * 61;
+    uint8_t *dst = desc_out + (long long)(off + k) * rb;
+    if (rb == 61) {
 #pragma unroll
-    for (int c = 0; c < 61; c++) dst[c] = row[c];
+      for (int c = 0; c < 61; c++) dst[c] = row[c];
+    } else {
+      for (int c = 0; c < rb; c++) dst[c] = row[c];
+    }
   }
 }
 
 cudaError_t akz_launch_pack_results(const akz_tables &t, const akz_kp *kp, const uint32_t *desc, akz_kp *kp_out,
-                                    uint8_t *desc_out, cudaStream_t s)
+                                    uint8_t *desc_out, int row_bytes, cudaStream_t s)
 {
-  k_pack_results<<<dim3(t.nimg, 8), 256, 0, s>>>(t, kp, desc, kp_out, desc_out);
+  if (row_bytes < 1 || row_bytes > 64) return cudaErrorInvalidValue;
+  k_pack_results<<<dim3(t.nimg, 8), 256, 0, s>>>(t, kp, desc, kp_out, desc_out, row_bytes);
   return cudaGetLastError();
 }

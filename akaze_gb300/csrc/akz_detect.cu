@@ -281,6 +281,15 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
   const int xlo = max(akz_border_lo(L.border), tx0), xhi = min(akz_border_hi(L.border, W), tx0 + TW - 1);
   const int ylo = max(akz_border_lo(L.border), ty0), yhi = min(akz_border_hi(L.border, H), ty0 + ch - 1);
   auto maxima = [&](int y) {
+    if (p.store_det && y >= ty0 && y < ty0 + ch) { /* the strip's own determinants, for the 3 x 3 x 3 rule */
+      const float *ec = sE + (y & (NE - 1)) * EW;
+      float *o = p.t.planes + L.ldet + (long long)y * pitch;
+#pragma unroll
+      for (int j = 0; j < (TW + 31) / 32; j++) {
+        const int x = tx0 + lane + 32 * j;
+        if (lane + 32 * j < TW && x < W) o[x] = ec[x - tx0 - EO];
+      }
+    }
     if (y < ylo || y > yhi) return;
     const float *eu = sE + ((y - 1) & (NE - 1)) * EW, *ec = sE + (y & (NE - 1)) * EW, *ed = sE + ((y + 1) & (NE - 1)) * EW;
 #pragma unroll
@@ -441,6 +450,10 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
     }
   }
   __syncthreads();
+  if (p.store_det) /* the tile's determinants, for the 3 x 3 x 3 rule */
+    for (int y = ty0 + warp; y < ty1; y += 8)
+      for (int x = tx0 + lane; x < tx1; x += 32)
+        p.t.planes[L.ldet + (long long)y * L.pitch + x] = sD[(y - ey0) * ew + (x - ex0)];
   const float border = L.border;
   for (int y = ty0 + warp; y < ty1; y += 8)
     for (int x = tx0 + lane; x < tx1; x += 32) {
@@ -457,6 +470,70 @@ __global__ void __launch_bounds__(256) k_detect(akz_detect_params p, int max_ste
       atomicAdd(&p.rowcnt[L.rows + y], 1);
     }
   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* The 3 x 3 x 3 extrema rule (akz_options.extrema_3d): a candidate of the
+ * 3 x 3 rule stays only if it also exceeds the 3 x 3 blocks of the
+ * determinant at its position in the previous and the next level of its
+ * octave (where those exist); AKAZE.cpp:340-367 hands FindExtrema those
+ * planes, cuda_akaze.cu:727-774 does not read them.  One warp per bitmap
+ * row (grid: x = level descriptor, y = groups of 8 rows), one lane per
+ * 32-bit word; the warp's removals leave the row count in one add.  The
+ * candidates lie inside the level's border range (>= 10 sqrt(2) pixels
+ * from every edge), so their neighbours' blocks are inside the image. */
+__global__ void __launch_bounds__(256) k_extrema3d(akz_detect_params p, int nlev_total)
+{
+  const int ld = blockIdx.x;
+  const akz_level_desc L = p.t.lv[ld];
+  const int lane = threadIdx.x & 31, y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (y >= L.height) return;
+  const float *adj[2] = {nullptr, nullptr};
+  if (ld > 0) {
+    const akz_level_desc P = p.t.lv[ld - 1];
+    if (P.image == L.image && P.octave == L.octave) adj[0] = p.t.planes + P.ldet;
+  }
+  if (ld + 1 < nlev_total) {
+    const akz_level_desc N = p.t.lv[ld + 1];
+    if (N.image == L.image && N.octave == L.octave) adj[1] = p.t.planes + N.ldet;
+  }
+  const long long pitch = L.pitch;
+  const float *det = p.t.planes + L.ldet;
+  uint32_t *row = p.bitmap + L.bitmap + (long long)y * L.bitmap_pitch;
+  int removed = 0;
+  for (int wd = lane; wd < L.bitmap_pitch; wd += 32) {
+    uint32_t bits = row[wd], keep = bits;
+    while (bits) {
+      const int b = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const int x = 32 * wd + b;
+      const float v = det[(long long)y * pitch + x];
+      bool ok = true;
+#pragma unroll
+      for (int a = 0; a < 2; a++) {
+        if (!adj[a]) continue;
+#pragma unroll
+        for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+          for (int dx = -1; dx <= 1; dx++) ok = ok && v > adj[a][(long long)(y + dy) * pitch + x + dx];
+      }
+      if (!ok) {
+        keep &= ~(1u << b);
+        removed++;
+      }
+    }
+    if (keep != row[wd]) row[wd] = keep;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) removed += __shfl_down_sync(0xffffffffu, removed, o);
+  if (lane == 0 && removed) p.rowcnt[L.rows + y] -= removed;
+}
+
+cudaError_t akz_launch_extrema3d(const akz_detect_params &p, int nlevels_total, int max_level_h, cudaStream_t s)
+{
+  if (nlevels_total <= 0) return cudaSuccess;
+  k_extrema3d<<<dim3(nlevels_total, (max_level_h + 7) / 8), 256, 0, s>>>(p, nlevels_total);
+  return cudaGetLastError();
 }
 
 /* ------------------------------------------------------------------------ */

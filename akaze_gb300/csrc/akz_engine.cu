@@ -29,7 +29,7 @@
 cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit, cudaStream_t s);
 cudaError_t akz_sg_maxdiff(const float *a, const float *b, int pitch, int width, int height, float *slot, cudaStream_t s);
 cudaError_t akz_launch_pack_results(const akz_tables &t, const akz_kp *kp, const uint32_t *desc, akz_kp *kp_out,
-                                    uint8_t *desc_out, cudaStream_t s);
+                                    uint8_t *desc_out, int row_bytes, cudaStream_t s);
 extern "C" akz_status akz_sg_infer_level(const float *l0, const float *g, size_t pitch, int width, int height,
                                          float dt_feature, float s_out, const void *weights_bf16, const float *biases,
                                          void *scratch, float *out, void *stream);
@@ -212,6 +212,116 @@ static void akz_area_tab(int ssize, int dsize, std::vector<int> &start, std::vec
   start.push_back((int)si.size());
 }
 
+/* The GNU C library's rand() after srand(seed): its TYPE_3 additive
+ * feedback generator, r[i] = r[i-31] + r[i-3] over a table seeded by
+ * r[i] = 16807 r[i-1] mod (2^31 - 1), the first 310 sums discarded, outputs
+ * r >> 1.  The reference draws its descriptor subsample with it
+ * (srand(1024), AKAZE.cpp:535); restated so that the table does not depend
+ * on, or disturb, the process's own rand() state. */
+struct akz_libc_rand {
+  uint32_t r[34];
+  int i = 0;
+  explicit akz_libc_rand(uint32_t seed)
+  {
+    uint32_t u[344];
+    int64_t v = seed ? seed : 1;
+    u[0] = (uint32_t)v;
+    for (int k = 1; k < 31; k++) {
+      v = (16807 * v) % 2147483647;
+      u[k] = (uint32_t)v;
+    }
+    for (int k = 31; k < 34; k++) u[k] = u[k - 31];
+    for (int k = 34; k < 344; k++) u[k] = u[k - 31] + u[k - 3];
+    for (int k = 0; k < 34; k++) r[k] = u[310 + k];
+  }
+  int next()
+  {
+    const uint32_t v = r[(i + 3) % 34] + r[(i + 31) % 34];
+    r[i] = v;
+    i = (i + 1) % 34;
+    return (int)(v >> 1);
+  }
+};
+
+/* The M-LDB bit table: bit b compares cell sum c1[b] with c2[b] (index
+ * 3 * cell + channel; cells 0-3 the 2x2 grid, 4-12 the 3x3, 13-28 the 4x4,
+ * row-major with rows along the keypoint direction).  descriptor_size 0:
+ * every pair of each grid per channel, (6 + 36 + 120) x channels bits
+ * (AKAZE.cpp:412-418).  descriptor_size n: the random comparisons of
+ * generateDescriptorSubsample (AKAZE.cpp:498-603), restated: picks from the
+ * 162 grid pairs (forced to the first 6, then rand() % remaining, the picked
+ * row replaced by the last live one), each pick's cells listed once as
+ * samples and compared channel by channel, the first n comparisons kept; a
+ * listed cell j of a g x g grid sits at row j % g, column j / g, as
+ * upstream libAKAZE's Get_MLDB_Descriptor_Subset samples it.  Returns the
+ * bit count. */
+static int akz_mldb_table(int channels, int subset, unsigned char *c1, unsigned char *c2)
+{
+  static const int g0[3] = {0, 4, 13};
+  int n = 0;
+  if (subset <= 0) {
+    for (int grid = 0; grid < 3; grid++) {
+      const int gs = (grid + 2) * (grid + 2);
+      for (int ch = 0; ch < channels; ch++)
+        for (int j = 0; j < gs - 1; j++)
+          for (int i = j + 1; i < gs; i++) {
+            c1[n] = (unsigned char)(3 * (g0[grid] + j) + ch);
+            c2[n] = (unsigned char)(3 * (g0[grid] + i) + ch);
+            n++;
+          }
+    }
+    return n;
+  }
+  struct pair3 {
+    int grid, a, b;
+  };
+  std::vector<pair3> pairs;
+  for (int grid = 0; grid < 3; grid++) {
+    const int gs = (grid + 2) * (grid + 2);
+    for (int a = 0; a < gs; a++)
+      for (int b2 = a + 1; b2 < gs; b2++) pairs.push_back({grid, a, b2});
+  }
+  const int nf = (int)pairs.size();
+  std::vector<std::pair<int, int>> listed; /* (grid, cell in the subset's order) */
+  std::vector<int> cmp_a, cmp_b;          /* listed sample index, per comparison */
+  std::vector<int> cmp_ch;
+  akz_libc_rand rng(1024);
+  const int picks = (subset + channels - 1) / channels;
+  for (int i = 0; i < picks; i++) {
+    int k = rng.next() % (nf - i);
+    if (i < 6) k = i;
+    int idx[2];
+    for (int e = 0; e < 2; e++) {
+      const std::pair<int, int> s(pairs[k].grid, e ? pairs[k].b : pairs[k].a);
+      int j = 0;
+      while (j < (int)listed.size() && listed[j] != s) j++;
+      if (j == (int)listed.size()) listed.push_back(s);
+      idx[e] = j;
+    }
+    for (int ch = 0; ch < channels; ch++) {
+      cmp_a.push_back(idx[0]);
+      cmp_b.push_back(idx[1]);
+      cmp_ch.push_back(ch);
+    }
+    pairs[k] = pairs[nf - i - 1];
+  }
+  auto cell = [&](int s) {
+    const int grid = listed[s].first, j = listed[s].second, g = grid + 2;
+    return g0[grid] + (j % g) * g + j / g;
+  };
+  for (n = 0; n < subset; n++) {
+    c1[n] = (unsigned char)(3 * cell(cmp_a[n]) + cmp_ch[n]);
+    c2[n] = (unsigned char)(3 * cell(cmp_b[n]) + cmp_ch[n]);
+  }
+  return n;
+}
+
+static int akz_row_bytes(const akz_options *o)
+{
+  const int bits = o->descriptor_size > 0 ? o->descriptor_size : 162 * o->descriptor_channels;
+  return (bits + 7) / 8;
+}
+
 static akz_status akz_validate(const akz_options *o)
 {
   if (!o) return akz_fail(AKZ_ERR_INVALID_ARG, "options are NULL");
@@ -222,11 +332,11 @@ static akz_status akz_validate(const akz_options *o)
   if (o->diffusivity < 0 || o->diffusivity > 3) return akz_fail(AKZ_ERR_INVALID_ARG, "unknown diffusivity %d", o->diffusivity);
   if (o->descriptor != AKZ_MLDB && o->descriptor != AKZ_MLDB_UPRIGHT)
     return akz_fail(AKZ_ERR_UNSUPPORTED, "descriptor %d is not implemented (MLDB and MLDB_UPRIGHT are)", o->descriptor);
-  if (o->descriptor_size != 0)
-    return akz_fail(AKZ_ERR_UNSUPPORTED, "descriptor_size %d: only the full 486-bit M-LDB is implemented", o->descriptor_size);
-  if (o->descriptor_channels != 3)
-    return akz_fail(AKZ_ERR_UNSUPPORTED, "descriptor_channels %d: only the 3-channel M-LDB is implemented",
-                    o->descriptor_channels);
+  if (o->descriptor_channels < 1 || o->descriptor_channels > 3)
+    return akz_fail(AKZ_ERR_INVALID_ARG, "descriptor_channels %d: must be 1, 2 or 3", o->descriptor_channels);
+  if (o->descriptor_size < 0 || o->descriptor_size > 162 * o->descriptor_channels)
+    return akz_fail(AKZ_ERR_INVALID_ARG, "descriptor_size %d: must be 0 (full) or at most %d bits for %d channel(s)",
+                    o->descriptor_size, 162 * o->descriptor_channels, o->descriptor_channels);
   if (o->descriptor_pattern_size < 1 || o->descriptor_pattern_size > 10)
     return akz_fail(AKZ_ERR_INVALID_ARG, "descriptor_pattern_size must be in [1, 10]");
   if (o->kcontrast_nbins < 1 || o->kcontrast_nbins > AKZ_MAX_NBINS)
@@ -234,6 +344,7 @@ static akz_status akz_validate(const akz_options *o)
   if (!(o->kcontrast_percentile >= 0.0f && o->kcontrast_percentile <= 1.0f))
     return akz_fail(AKZ_ERR_INVALID_ARG, "kcontrast_percentile must be in [0, 1]");
   if (o->maxkeypoints < 1) return akz_fail(AKZ_ERR_INVALID_ARG, "maxkeypoints must be positive");
+  if (o->extrema_3d != 0 && o->extrema_3d != 1) return akz_fail(AKZ_ERR_INVALID_ARG, "extrema_3d must be 0 or 1");
   return AKZ_OK;
 }
 
@@ -260,7 +371,7 @@ struct akz_batch {
   std::vector<akz_level_desc> lv;
   std::vector<std::vector<akz_geo>> geo;
   std::vector<std::vector<float>> tau; /* per level index */
-  int maxlev = 0, max_step = 1;
+  int maxlev = 0, max_step = 1, max_level_h = 1;
   float taps0[AKZ_MAX_TAPS], taps1[AKZ_MAX_TAPS];
   int R0 = 0;
   /* launches */
@@ -319,6 +430,8 @@ struct akz_batch {
   uint32_t *d_desc = nullptr;
   int *d_nbr = nullptr;
   unsigned char *d_nbc = nullptr;
+  unsigned char *d_cmp = nullptr; /* M-LDB bit table: 512 first then 512 second value indices */
+  int nbits = 486, row_bytes = 61;
   void *d_pack = nullptr; /* packed results of akz_batch_collect_packed, grown on demand */
   bool submitted = false; /* akz_batch_submit issued, akz_batch_collect_packed not yet */
   size_t cap_pack = 0;    /* rows */
@@ -452,6 +565,7 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
         return akz_fail(AKZ_ERR_INVALID_ARG, "image %d: level %dx%d too small for derivative step %d", i, g.w, g.h, g.deriv_step);
       }
       b->max_step = std::max(b->max_step, g.deriv_step);
+      b->max_level_h = std::max(b->max_level_h, g.h);
     }
   }
   if (b->max_step > 16) {
@@ -506,6 +620,11 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
       L.lx = (long long)plane_floats; /* Lx, Ly interleaved: (Lx, Ly) pairs, row pitch 2 * pitch */
       L.ly = L.lx + 1;
       plane_floats += 2 * pf;
+      L.ldet = -1;
+      if (opt->extrema_3d) { /* the 3 x 3 x 3 rule reads the adjacent levels' determinants */
+        L.ldet = (long long)plane_floats;
+        plane_floats += pf;
+      }
       L.rows = rows + rt;
       rt += g.h;
       L.bitmap_pitch = (g.w + 31) / 32;
@@ -706,6 +825,7 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
   const size_t o_desc = take(raw * 64);
   const size_t o_nbr = take(raw * AKZ_NMS_NB * sizeof(int));
   const size_t o_nbc = take(raw);
+  const size_t o_cmp = take(1024);
   b->arena_bytes = off;
   cudaError_t e = cudaMalloc(&b->arena, b->arena_bytes);
   if (e != cudaSuccess) {
@@ -736,7 +856,14 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
   b->d_desc = (uint32_t *)(a + o_desc);
   b->d_nbr = (int *)(a + o_nbr);
   b->d_nbc = (unsigned char *)(a + o_nbc);
-  e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+  b->d_cmp = (unsigned char *)(a + o_cmp);
+  {
+    unsigned char cmp[1024] = {0};
+    b->nbits = akz_mldb_table(b->opt.descriptor_channels, b->opt.descriptor_size, cmp, cmp + 512);
+    b->row_bytes = akz_row_bytes(&b->opt);
+    e = cudaMemcpy(b->d_cmp, cmp, sizeof(cmp), cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost(&b->h_stats, (size_t)n * sizeof(akz_image_stats));
   for (auto &ev : b->ev)
     if (e == cudaSuccess) e = cudaEventCreate(&ev);
@@ -888,10 +1015,12 @@ static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s, cudaEvent_t *pe
   dp.thr = std::max(b->opt.dthreshold, b->opt.min_dthreshold);
   dp.fac1 = fac1;
   dp.fac2 = fac2;
+  dp.store_det = b->opt.extrema_3d;
   CK(akz_launch_detect(dp, b->detect_tiles, b->max_step, s));
   dp.segs = b->d_segs + b->strip_off;
   dp.nsegs = b->strip_n;
   CK(akz_launch_detect_strip(dp, b->strip_tiles, s));
+  if (b->opt.extrema_3d) CK(akz_launch_extrema3d(dp, (int)b->lv.size(), b->max_level_h, s));
   if (pe) CK(cudaEventRecord(pe[4], s));
   CK(akz_launch_rowscan(t, b->d_rowcnt, b->d_rowscan, s));
   akz_extract_params ep;
@@ -928,6 +1057,10 @@ static akz_status akz_stage_describe(akz_batch *b, cudaStream_t s)
   p.desc = b->d_desc;
   p.upright = b->opt.descriptor == AKZ_MLDB_UPRIGHT;
   p.pattern_size = b->opt.descriptor_pattern_size;
+  p.channels = b->opt.descriptor_channels;
+  p.nbits = b->nbits;
+  p.cmp1 = b->d_cmp;
+  p.cmp2 = b->d_cmp + 512;
   /* exp(-r2/12.5) with the shared deterministic exp (the CPU restatement
    * uses the same routine), so the weights are identical on every host */
   for (int r2 = 0; r2 < 36; r2++) p.gw[r2] = akz_expf((float)(-r2) / (2.5f * 2.5f * 2.0f));
@@ -993,7 +1126,8 @@ static akz_status akz_copy_results(akz_batch *b, int i, akz_keypoint *kpts, uint
   const akz_image_desc &I = b->im[i];
   if (m > 0 && kpts) CK(cudaMemcpyAsync(kpts, b->d_kp + I.kp_base, (size_t)m * sizeof(akz_kp), cudaMemcpyDeviceToHost, b->stream));
   if (m > 0 && desc)
-    CK(cudaMemcpy2DAsync(desc, 61, (const uint8_t *)b->d_desc + (size_t)I.kp_base * 64, 64, 61, m, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaMemcpy2DAsync(desc, b->row_bytes, (const uint8_t *)b->d_desc + (size_t)I.kp_base * 64, 64, b->row_bytes, m,
+                         cudaMemcpyDeviceToHost, b->stream));
   CK(cudaStreamSynchronize(b->stream));
   if (n) *n = nk;
   return AKZ_OK;
@@ -1040,6 +1174,16 @@ AKZ_API akz_status akz_options_default(akz_options *o)
   o->kcontrast_nbins = 300;
   o->ncudaimages = 4;
   o->maxkeypoints = 16 * 8192;
+  o->extrema_3d = 0;
+  return AKZ_OK;
+}
+
+AKZ_API akz_status akz_descriptor_bytes(const akz_options *opt, int *bytes)
+{
+  if (!bytes) return akz_fail(AKZ_ERR_INVALID_ARG, "bytes is NULL");
+  akz_status st = akz_validate(opt);
+  if (st != AKZ_OK) return st;
+  *bytes = akz_row_bytes(opt);
   return AKZ_OK;
 }
 
@@ -1366,7 +1510,8 @@ AKZ_API akz_status akz_batch_detect_describe(akz_batch *b, const uint8_t *const 
     if (m > 0 && kpts && kpts[i])
       CK(cudaMemcpyAsync(kpts[i], b->d_kp + I.kp_base, (size_t)m * sizeof(akz_kp), cudaMemcpyDeviceToHost, b->stream));
     if (m > 0 && desc && desc[i])
-      CK(cudaMemcpy2DAsync(desc[i], 61, (const uint8_t *)b->d_desc + (size_t)I.kp_base * 64, 64, 61, m, cudaMemcpyDeviceToHost, b->stream));
+      CK(cudaMemcpy2DAsync(desc[i], b->row_bytes, (const uint8_t *)b->d_desc + (size_t)I.kp_base * 64, 64, b->row_bytes,
+                           m, cudaMemcpyDeviceToHost, b->stream));
     if (counts) counts[i] = nk;
   }
   CK(cudaStreamSynchronize(b->stream));
@@ -1431,9 +1576,9 @@ AKZ_API akz_status akz_batch_collect_packed(akz_batch *b, akz_keypoint *kpts, ui
   }
   akz_kp *pk = (akz_kp *)b->d_pack;
   uint8_t *pd = (uint8_t *)(pk + b->cap_pack);
-  CK(akz_launch_pack_results(akz_make_tables(b), b->d_kp, b->d_desc, pk, pd, b->stream));
+  CK(akz_launch_pack_results(akz_make_tables(b), b->d_kp, b->d_desc, pk, pd, b->row_bytes, b->stream));
   if (kpts) CK(cudaMemcpyAsync(kpts, pk, (size_t)n * sizeof(akz_kp), cudaMemcpyDeviceToHost, b->stream));
-  if (desc) CK(cudaMemcpyAsync(desc, pd, (size_t)n * 61, cudaMemcpyDeviceToHost, b->stream));
+  if (desc) CK(cudaMemcpyAsync(desc, pd, (size_t)n * b->row_bytes, cudaMemcpyDeviceToHost, b->stream));
   CK(cudaStreamSynchronize(b->stream));
   return AKZ_OK;
 }

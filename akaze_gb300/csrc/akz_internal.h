@@ -39,6 +39,8 @@ struct akz_level_desc {
   long long bitmap;         /* word offset of the bitmap */
   int bitmap_pitch;         /* 32-bit words per row */
   int pad;
+  long long ldet;           /* float offset of the determinant plane (row pitch `pitch`), kept only for
+                             * the 3 x 3 x 3 extrema rule; -1 otherwise */
 };
 
 /* One image of the batch. */

@@ -116,6 +116,7 @@ struct akz_detect_params {
   uint32_t *bitmap;
   int *rowcnt;
   float thr, fac1, fac2;
+  int store_det; /* 1: keep every level's determinant in its plane (L.ldet) for the 3 x 3 x 3 rule */
 };
 
 struct akz_extract_params {
@@ -147,6 +148,9 @@ struct akz_describe_params {
   uint32_t *desc; /* 16 words per keypoint */
   int upright;
   int pattern_size;
+  int channels;   /* 1 (L), 2 (L, |grad|) or 3 (L, rotated dx, dy) */
+  int nbits;      /* bits of a descriptor row (<= 486) */
+  const unsigned char *cmp1, *cmp2; /* bit b: cell value cmp1[b] > cmp2[b] (3 * cell + channel) */
   float gw[36];   /* Gaussian weights exp(-r2/12.5) of the orientation samples */
 };
 
@@ -163,6 +167,10 @@ cudaError_t akz_launch_detect(const akz_detect_params &p, int ntiles, int max_st
 #define AKZ_STRIP_CH 256
 int akz_strip_tile_width(int st); /* 0 for steps the strip kernel does not compile */
 cudaError_t akz_launch_detect_strip(const akz_detect_params &p, int ntiles, cudaStream_t s);
+/* the 3 x 3 x 3 extrema rule: clears the bitmap bits (and row counts) of
+ * candidates that do not exceed the 3 x 3 blocks of the adjacent levels of
+ * their octave; after both detector launches with store_det set */
+cudaError_t akz_launch_extrema3d(const akz_detect_params &p, int nlevels_total, int max_level_h, cudaStream_t s);
 cudaError_t akz_launch_rowscan(const akz_tables &t, const int *rowcnt, int *rowscan, cudaStream_t s);
 cudaError_t akz_launch_extract(const akz_extract_params &p, int nrows, cudaStream_t s);
 cudaError_t akz_launch_nms(const akz_nms_params &p, cudaStream_t s);

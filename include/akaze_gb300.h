@@ -72,6 +72,15 @@ typedef struct akz_options {
   int verbosity;
   int ncudaimages;
   int maxkeypoints; /* capacity of raw extrema per image */
+  /* Extension (no AKAZEOptions field): the scale-space extrema rule.
+   * 0 (default): the reference's FindExtrema (cuda_akaze.cu:727-774), a strict
+   *   maximum over the 8 neighbours in the level, above the threshold.
+   * 1: also a strict maximum over the 3 x 3 neighbourhoods of the level below
+   *   and the level above in the same octave (26 neighbours; the first and
+   *   last sublevel of an octave compare with the one adjacent level they
+   *   have), the rule for which the reference passes, and leaves unused, the
+   *   adjacent levels to FindExtrema (AKAZE.cpp:340-367, cuda_akaze.cu:727). */
+  int extrema_3d;
 } akz_options;
 
 /* cv::KeyPoint layout (28 bytes): pt.x, pt.y, size, angle, response, octave, class_id. */
@@ -109,6 +118,12 @@ AKZ_API const char *akz_last_error(void);
 /* setDefaultAKAZEOptions / AKAZEOptions::AKAZEOptions (AKAZEConfig.h:86-111). */
 AKZ_API akz_status akz_options_default(akz_options *opt);
 
+/* Bytes of one descriptor row for the options, as Compute_Descriptors sizes
+ * its output (AKAZE.cpp:412-423): ceil((6 + 36 + 120) * descriptor_channels
+ * / 8) for the full M-LDB (21, 41 or 61), ceil(descriptor_size / 8) for the
+ * random-bit subset.  On the device every row is 64 bytes, zero-padded. */
+AKZ_API akz_status akz_descriptor_bytes(const akz_options *opt, int *bytes);
+
 /* Level plan of an image, computed on the host without touching the GPU
  * (AKAZE.cpp:146-197, fed.cpp:41-148): level count, and for level >= 0 its
  * size, octave, sublevel, evolution sigma, detector step, extrema border and
@@ -140,8 +155,9 @@ AKZ_API akz_status akz_create_nonlinear_scale_space(akz_context *ctx, const void
  * suppression; returns the number of keypoints. */
 AKZ_API akz_status akz_feature_detection(akz_context *ctx, int *nkeypoints);
 /* AKAZE::Compute_Descriptors (AKAZE.cpp:405-449): orientation + M-LDB;
- * copies min(n, capacity) keypoints and 61-byte descriptor rows to host
- * memory (either pointer may be NULL) and returns n. */
+ * copies min(n, capacity) keypoints and descriptor rows of
+ * akz_descriptor_bytes() bytes (61 for the default options) to host memory
+ * (either pointer may be NULL) and returns n. */
 AKZ_API akz_status akz_compute_descriptors(akz_context *ctx, akz_keypoint *kpts, uint8_t *desc, int capacity, int *nkeypoints);
 /* AKAZE::Get_Computation_Times (AKAZE.h:140-142). */
 AKZ_API akz_status akz_get_timing(akz_context *ctx, akz_timing *t);
@@ -171,7 +187,8 @@ AKZ_API akz_status akz_batch_input(akz_batch *b, int i, uint8_t **dptr, size_t *
 AKZ_API akz_status akz_batch_run(akz_batch *b);
 /* Per-image keypoint counts (synchronises the stream). */
 AKZ_API akz_status akz_batch_counts(akz_batch *b, int *counts);
-/* Copy image i's keypoints and 61-byte descriptors to host memory (sync). */
+/* Copy image i's keypoints and descriptor rows (akz_descriptor_bytes()
+ * bytes each) to host memory (sync). */
 AKZ_API akz_status akz_batch_results(akz_batch *b, int i, akz_keypoint *kpts, uint8_t *desc, int capacity, int *n);
 /* Device addresses of image i's keypoints and 64-byte descriptor rows. */
 AKZ_API akz_status akz_batch_device_results(akz_batch *b, int i, akz_keypoint **kpts, uint8_t **desc64);
@@ -333,7 +350,7 @@ AKZ_API akz_status akz_batch_collect_packed(akz_batch *b, akz_keypoint *kpts, ui
                                             int *total);
 
 /* akz_batch_detect_describe with packed host output: kpts (capacity
- * records) and desc (capacity x 61 bytes) receive every image's keypoints
+ * records) and desc (capacity x akz_descriptor_bytes() bytes) receive every image's keypoints
  * and descriptors back to back, image i starting at row sum_{j<i} counts[j];
  * counts[i] receives image i's count and *total their sum.  If the sum
  * exceeds capacity nothing is copied and AKZ_ERR_OVERFLOW is returned (call

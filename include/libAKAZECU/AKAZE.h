@@ -173,6 +173,7 @@ struct AKAZEOptions {
   bool verbosity;
   int ncudaimages;
   int maxkeypoints;
+  int extrema_3d; /* extension: akz_options.extrema_3d (0, the reference's 3x3 rule, by default) */
 
   akz_options to_c() const
   {
@@ -201,6 +202,7 @@ struct AKAZEOptions {
     c.verbosity = verbosity;
     c.ncudaimages = ncudaimages;
     c.maxkeypoints = maxkeypoints;
+    c.extrema_3d = extrema_3d;
     return c;
   }
   void from_c(const akz_options &c)
@@ -228,6 +230,7 @@ struct AKAZEOptions {
     verbosity = c.verbosity != 0;
     ncudaimages = c.ncudaimages;
     maxkeypoints = c.maxkeypoints;
+    extrema_3d = c.extrema_3d;
   }
 
   /* The option listing of AKAZEConfig.h:145-172: one "name =  value" line

@@ -219,6 +219,7 @@ struct ako_ctx {
   int nkp;
   uint8_t *desc;
   int ndesc;
+  int desc_bytes; /* bytes of one descriptor row */
 };
 
 void ako_options_default(ako_options *o)
@@ -237,6 +238,7 @@ void ako_options_default(ako_options *o)
   o->descriptor_pattern_size = 10;
   o->kcontrast_percentile = 0.7f;
   o->kcontrast_nbins = 300;
+  o->extrema_3d = 0;
 }
 
 void ako_set_threads(int n)
@@ -581,9 +583,25 @@ static void ako_hessian(const float *lx, const float *ly, float *det, int w, int
   }
 }
 
+/* 1 when v exceeds the 9 values of the 3 x 3 block at p of the level plane
+ * A (same size as the current level), or when there is no such level. */
+static int ako_above3x3(const float *A, size_t p, int w, float v)
+{
+  if (!A) return 1;
+  for (int dy = -1; dy <= 1; dy++)
+    for (int dx = -1; dx <= 1; dx++)
+      if (!(v > A[(long)p + (long)dy * w + dx])) return 0;
+  return 1;
+}
+
 /* cuda_akaze.cu:727-774 for one level, in raster order (the order the
- * reference's per-level bitonic sort by (y, x) produces, :884-939). */
-static int ako_find_extrema(const float *D, int w, int h, const ako_level *L, int level, float thr, ako_extremum *out, int cap)
+ * reference's per-level bitonic sort by (y, x) produces, :884-939).  With
+ * Dp / Dn (the determinants of the previous and next level of the same
+ * octave, NULL where there is none) a candidate must also exceed their 3 x 3
+ * blocks at its position: the 3 x 3 x 3 rule for which the reference passes
+ * those planes to FindExtrema and leaves them unused (AKAZE.cpp:340-367). */
+static int ako_find_extrema(const float *D, const float *Dp, const float *Dn, int w, int h, const ako_level *L,
+                            int level, float thr, ako_extremum *out, int cap)
 {
   int n = 0;
   const float border = L->border;
@@ -598,7 +616,7 @@ static int ako_find_extrema(const float *D, int w, int h, const ako_level *L, in
       const size_t p = (size_t)y * w + x;
       const float v = D[p];
       if (v > thr && v > D[p - w - 1] && v > D[p + w + 1] && v > D[p + w - 1] && v > D[p - w + 1] && v > D[p - 1] &&
-          v > D[p + 1] && v > D[p + w] && v > D[p - w]) {
+          v > D[p + 1] && v > D[p + w] && v > D[p - w] && ako_above3x3(Dp, p, w, v) && ako_above3x3(Dn, p, w, v)) {
         const float dx = 0.5f * (D[p + 1] - D[p - 1]);
         const float dy = 0.5f * (D[p + w] - D[p - w]);
         const float dxx = D[p + 1] + D[p - 1] - 2.0f * v;
@@ -798,10 +816,18 @@ int ako_detect(ako_ctx *c)
     ako_deriv_pair(c->Ls + c->off[i], c->Lx + c->off[i], c->Ly + c->off[i], L->width, L->height, L->deriv_step, fac1, fac2);
     ako_hessian(c->Lx + c->off[i], c->Ly + c->off[i], c->Ld + c->off[i], L->width, L->height, L->deriv_step, fac1, fac2);
   }
+  /* adjacent levels of the same octave for the 3 x 3 x 3 rule */
+  const float *Dp[AKO_MAX_LEVELS], *Dn[AKO_MAX_LEVELS];
+  for (int i = 0; i < c->nlev; i++) {
+    const int same_p = c->opt.extrema_3d && i > 0 && c->lev[i - 1].octave == c->lev[i].octave;
+    const int same_n = c->opt.extrema_3d && i + 1 < c->nlev && c->lev[i + 1].octave == c->lev[i].octave;
+    Dp[i] = same_p ? c->Ld + c->off[i - 1] : NULL;
+    Dn[i] = same_n ? c->Ld + c->off[i + 1] : NULL;
+  }
   int total = 0;
   for (int i = 0; i < c->nlev; i++) {
     const ako_level *L = &c->lev[i];
-    total += ako_find_extrema(c->Ld + c->off[i], L->width, L->height, L, i, thr, NULL, 0);
+    total += ako_find_extrema(c->Ld + c->off[i], Dp[i], Dn[i], L->width, L->height, L, i, thr, NULL, 0);
   }
   free(c->ext);
   c->ext = (ako_extremum *)malloc(sizeof(ako_extremum) * (size_t)(total > 0 ? total : 1));
@@ -809,7 +835,7 @@ int ako_detect(ako_ctx *c)
   for (int i = 0; i < c->nlev; i++) {
     const ako_level *L = &c->lev[i];
     c->ext_off[i] = n;
-    n += ako_find_extrema(c->Ld + c->off[i], L->width, L->height, L, i, thr, c->ext + n, total - n);
+    n += ako_find_extrema(c->Ld + c->off[i], Dp[i], Dn[i], L->width, L->height, L, i, thr, c->ext + n, total - n);
   }
   c->ext_off[c->nlev] = n;
   c->next = n;
@@ -876,13 +902,147 @@ static int ako_cmp_pairs(int *i1, int *i2)
   return n;
 }
 
+/* The generator behind srand()/rand() of the GNU C library (its TYPE_3
+ * additive feedback generator, which the reference's
+ * generateDescriptorSubsample uses through srand(1024), AKAZE.cpp:535):
+ * r[0] = seed, r[i] = 16807 r[i-1] mod (2^31 - 1) for i < 31,
+ * r[i] = r[i-31] for i = 31..33, then r[i] = r[i-31] + r[i-3] (mod 2^32);
+ * the first 310 of those are discarded and output k is r[344+k] >> 1. */
+typedef struct {
+  uint32_t r[34];
+  int i;
+} ako_glibc_rand;
+
+static void ako_glibc_srand(ako_glibc_rand *g, uint32_t seed)
+{
+  int32_t v[344];
+  v[0] = (int32_t)(seed ? seed : 1);
+  for (int i = 1; i < 31; i++) {
+    const int64_t t = (16807LL * v[i - 1]) % 2147483647LL;
+    v[i] = (int32_t)(t < 0 ? t + 2147483647LL : t);
+  }
+  for (int i = 31; i < 34; i++) v[i] = v[i - 31];
+  uint32_t u[344];
+  for (int i = 0; i < 34; i++) u[i] = (uint32_t)v[i];
+  for (int i = 34; i < 344; i++) u[i] = u[i - 31] + u[i - 3];
+  for (int k = 0; k < 34; k++) g->r[k] = u[310 + k];
+  g->i = 0;
+}
+
+static int ako_glibc_rand_next(ako_glibc_rand *g)
+{
+  /* the ring holds r[n-34 .. n-1]; next = r[n-31] + r[n-3] */
+  const uint32_t a = g->r[(g->i + 3) % 34], b = g->r[(g->i + 31) % 34];
+  const uint32_t v = a + b;
+  g->r[g->i] = v;
+  g->i = (g->i + 1) % 34;
+  return (int)(v >> 1);
+}
+
+int ako_glibc_rand_sequence(uint32_t seed, int *out, int n)
+{
+  ako_glibc_rand g;
+  ako_glibc_srand(&g, seed);
+  for (int k = 0; k < n; k++) out[k] = ako_glibc_rand_next(&g);
+  return n;
+}
+
+/* Comparison table of the M-LDB bits: value indices 3*cell + channel into
+ * the 29 x 3 cell sums (cells 0-3 the 2x2 grid, 4-12 the 3x3, 13-28 the 4x4,
+ * each row-major in the rotated frame: row = the sample offset along the
+ * keypoint direction).  Returns the bit count.
+ *  - descriptor_size 0: every pair i < j of each grid, per channel in
+ *    increasing channel order (AKAZE.cpp:412-418: (6+36+120)*channels bits);
+ *  - descriptor_size n > 0: the random selection of generateDescriptorSubsample
+ *    (AKAZE.cpp:498-603): of the 162 grid pairs, pick k = rand() % (162 - i)
+ *    (forced to i for the first 6 picks) from a list shrunk by moving its
+ *    last live row into the picked one; each pick's two cells become samples
+ *    (reused when already listed) and give `channels` comparisons, channel c
+ *    of the first cell against channel c of the second; the first n kept.
+ *    The subset's cell with list index j of a g x g grid lies at row j % g
+ *    and column j / g (Get_MLDB_Descriptor_Subset, the upstream libAKAZE
+ *    routine the reference's table feeds, takes the sample's first offset
+ *    along the keypoint direction). */
+int ako_mldb_table(int channels, int nbits_subset, int *c1, int *c2)
+{
+  static const int g0[3] = {0, 4, 13};
+  if (nbits_subset <= 0) {
+    int n = 0;
+    for (int grid = 0; grid < 3; grid++) {
+      const int gs = (grid + 2) * (grid + 2);
+      for (int ch = 0; ch < channels; ch++)
+        for (int j = 0; j < gs - 1; j++)
+          for (int i = j + 1; i < gs; i++) {
+            c1[n] = 3 * (g0[grid] + j) + ch;
+            c2[n] = 3 * (g0[grid] + i) + ch;
+            n++;
+          }
+    }
+    return n;
+  }
+  /* the 162 grid pairs as (grid, cell a, cell b) in the reference's order */
+  int full[162][3], nf = 0;
+  for (int grid = 0; grid < 3; grid++) {
+    const int gs = (grid + 2) * (grid + 2);
+    for (int j = 0; j < gs; j++)
+      for (int k = j + 1; k < gs; k++) {
+        full[nf][0] = grid;
+        full[nf][1] = j;
+        full[nf][2] = k;
+        nf++;
+      }
+  }
+  const int npicks = (nbits_subset + channels - 1) / channels;
+  int samp[29][2], count = 0; /* listed samples: (grid, cell index in the subset's order) */
+  int *cm1 = (int *)malloc(sizeof(int) * (size_t)npicks * channels), *cm2 = (int *)malloc(sizeof(int) * (size_t)npicks * channels);
+  ako_glibc_rand g;
+  ako_glibc_srand(&g, 1024);
+  for (int i = 0; i < npicks; i++) {
+    int k = ako_glibc_rand_next(&g) % (nf - i);
+    if (i < 6) k = i;
+    int which[2];
+    for (int e = 0; e < 2; e++) {
+      const int grid = full[k][0], cell = full[k][1 + e];
+      int j;
+      for (j = 0; j < count; j++)
+        if (samp[j][0] == grid && samp[j][1] == cell) break;
+      if (j == count) {
+        samp[count][0] = grid;
+        samp[count][1] = cell;
+        count++;
+      }
+      which[e] = j;
+    }
+    for (int ch = 0; ch < channels; ch++) {
+      cm1[i * channels + ch] = which[0] * 3 + ch; /* sample index * 3 + channel, mapped below */
+      cm2[i * channels + ch] = which[1] * 3 + ch;
+    }
+    for (int q = 0; q < 3; q++) full[k][q] = full[nf - i - 1][q];
+  }
+  for (int b = 0; b < nbits_subset; b++) {
+    const int s1 = cm1[b] / 3, ch = cm1[b] % 3, s2 = cm2[b] / 3;
+    const int gd1 = samp[s1][0] + 2, gd2 = samp[s2][0] + 2;
+    const int cell1 = g0[samp[s1][0]] + (samp[s1][1] % gd1) * gd1 + samp[s1][1] / gd1;
+    const int cell2 = g0[samp[s2][0]] + (samp[s2][1] % gd2) * gd2 + samp[s2][1] / gd2;
+    c1[b] = 3 * cell1 + ch;
+    c2[b] = 3 * cell2 + ch;
+  }
+  free(cm1);
+  free(cm2);
+  return nbits_subset;
+}
+
 int ako_describe(ako_ctx *c)
 {
   if (!c || !c->built) return -1;
   int i1[486], i2[486];
-  ako_cmp_pairs(i1, i2);
+  const int channels = c->opt.descriptor_channels;
+  if (channels < 1 || channels > 3 || c->opt.descriptor_size < 0 || c->opt.descriptor_size > 162 * channels) return -1;
+  const int nbits = ako_mldb_table(channels, c->opt.descriptor_size, i1, i2);
+  const int rb = (nbits + 7) / 8;
+  c->desc_bytes = rb;
   free(c->desc);
-  c->desc = (uint8_t *)calloc((size_t)(c->nkp > 0 ? c->nkp : 1), 61);
+  c->desc = (uint8_t *)calloc((size_t)(c->nkp > 0 ? c->nkp : 1), (size_t)rb);
   const int ps = c->opt.descriptor_pattern_size;
   const int size2 = ps;
   const int size3 = (int)ceilf(2.0f * (float)ps / 3.0f);
@@ -915,7 +1075,10 @@ int ako_describe(ako_ctx *c)
         yp = ako_clampi(yp, 0, h - 1);
         const size_t pos = (size_t)yp * w + xp;
         const float im = imd[pos], dx = dxd[pos], dy = dyd[pos];
-        const float rx = -dx * si + dy * co;
+        /* channels 2 and 3 of the cells: the rotated derivatives, or for a
+         * 2-channel descriptor the gradient magnitude (MLDB_Fill_Values of
+         * upstream libAKAZE; the reference's own kernel is 3-channel only) */
+        const float rx = channels == 2 ? sqrtf(dx * dx + dy * dy) : -dx * si + dy * co;
         const float ry = dx * co + dy * si;
         if (m < 2 * size2) {
           const int x2 = x < size2 ? 0 : 1, y2 = y < size2 ? 0 : 1;
@@ -948,19 +1111,21 @@ int ako_describe(ako_ctx *c)
         for (int j = 0; j < 32; j += 2 * d) a[j] = a[j] + a[j + d];
       vals[q] = a[0];
     }
-    uint8_t *d = c->desc + (size_t)p * 61;
-    for (int b = 0; b < 486; b++)
+    uint8_t *d = c->desc + (size_t)p * rb;
+    for (int b = 0; b < nbits; b++)
       if (vals[i1[b]] > vals[i2[b]]) d[b >> 3] |= (uint8_t)(1u << (b & 7));
   }
   c->ndesc = c->nkp;
   return c->nkp;
 }
 
+int ako_descriptor_bytes(const ako_ctx *c) { return c ? c->desc_bytes : -1; }
+
 int ako_get_descriptors(const ako_ctx *c, uint8_t *out, int cap_rows)
 {
   if (!c || !c->desc) return -1;
   const int n = c->ndesc < cap_rows ? c->ndesc : cap_rows;
-  memcpy(out, c->desc, (size_t)n * 61);
+  memcpy(out, c->desc, (size_t)n * c->desc_bytes);
   return n;
 }
 

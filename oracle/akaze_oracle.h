@@ -52,6 +52,7 @@ typedef struct {
   int descriptor_pattern_size;
   float kcontrast_percentile;
   int kcontrast_nbins;
+  int extrema_3d; /* 1: also a strict maximum over the adjacent levels of the octave */
 } ako_options;
 
 /* cv::KeyPoint layout (28 bytes). */
@@ -126,6 +127,13 @@ int ako_get_keypoints(const ako_ctx *c, ako_keypoint *out, int cap);
 /* M-LDB descriptors, 61 bytes per keypoint. */
 int ako_describe(ako_ctx *c);
 int ako_get_descriptors(const ako_ctx *c, uint8_t *out, int cap_rows);
+/* bytes of one descriptor row after ako_describe */
+int ako_descriptor_bytes(const ako_ctx *c);
+/* the M-LDB comparison table (value indices 3*cell + channel) for channels
+ * 1..3 and a descriptor_size (0: the full descriptor); returns its bits */
+int ako_mldb_table(int channels, int nbits_subset, int *c1, int *c2);
+/* the first n outputs of the GNU C library's rand() after srand(seed) */
+int ako_glibc_rand_sequence(uint32_t seed, int *out, int n);
 
 /* Whole path on one u8 image (timed CPU baseline). Returns keypoints or <0. */
 int ako_run_u8(ako_ctx *c, const uint8_t *img);

@@ -24,6 +24,7 @@ class AkoOptions(ctypes.Structure):
         ("descriptor", ctypes.c_int), ("descriptor_size", ctypes.c_int),
         ("descriptor_channels", ctypes.c_int), ("descriptor_pattern_size", ctypes.c_int),
         ("kcontrast_percentile", ctypes.c_float), ("kcontrast_nbins", ctypes.c_int),
+        ("extrema_3d", ctypes.c_int),
     ]
 
 
@@ -104,6 +105,9 @@ def lib():
         L.ako_run_u8.argtypes = [P, P]
         L.ako_bfmatch.argtypes = [P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, P]
         L.ako_set_threads.argtypes = [ctypes.c_int]
+        L.ako_descriptor_bytes.argtypes = [P]
+        L.ako_mldb_table.argtypes = [ctypes.c_int, ctypes.c_int, P, P]
+        L.ako_glibc_rand_sequence.argtypes = [ctypes.c_uint32, P, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -221,6 +225,20 @@ def gaussian_taps(sigma):
     return buf[:n].copy()
 
 
+def mldb_table(channels=3, descriptor_size=0):
+    """The oracle's M-LDB comparison table: (c1, c2) value indices 3*cell + channel."""
+    c1 = np.zeros(512, np.int32)
+    c2 = np.zeros(512, np.int32)
+    n = lib().ako_mldb_table(int(channels), int(descriptor_size), c1.ctypes.data, c2.ctypes.data)
+    return c1[:n].copy(), c2[:n].copy()
+
+
+def glibc_rand_sequence(seed, n):
+    out = np.zeros(n, np.int32)
+    lib().ako_glibc_rand_sequence(int(seed), out.ctypes.data, int(n))
+    return out
+
+
 def bfmatch(q, t):
     q = np.ascontiguousarray(q, np.uint8)
     t = np.ascontiguousarray(t, np.uint8)
@@ -334,7 +352,7 @@ class Oracle:
         n = lib().ako_describe(self.ptr)
         if n < 0:
             raise RuntimeError("ako_describe failed")
-        out = np.zeros((n, 61), np.uint8)
+        out = np.zeros((n, lib().ako_descriptor_bytes(self.ptr)), np.uint8)
         lib().ako_get_descriptors(self.ptr, out.ctypes.data, n)
         return out
 
@@ -345,6 +363,6 @@ class Oracle:
         if n < 0:
             raise RuntimeError("ako_run_u8 failed")
         kp = self.keypoints()
-        d = np.zeros((n, 61), np.uint8)
+        d = np.zeros((n, lib().ako_descriptor_bytes(self.ptr)), np.uint8)
         lib().ako_get_descriptors(self.ptr, d.ctypes.data, n)
         return kp, d

@@ -107,6 +107,62 @@ def test_uneven_batch_of_64_matches_oracle(gpu_lib, oracle):
     assert total > 64 * 50
 
 
+@pytest.mark.parametrize("w,h,seed,dfac", [(640, 480, 4041, 1.5), (1920, 1080, 4042, 1.5), (331, 257, 4043, 1.5),
+                                           (640, 480, 4044, 0.8), (640, 480, 4045, 2.0)])
+def test_extrema_3d_matches_oracle(gpu_lib, oracle, w, h, seed, dfac):
+    """The 3 x 3 x 3 extrema option (akz_options.extrema_3d): candidates must
+    also exceed the adjacent levels of their octave.  derivative_factor 0.8
+    and 2.0 run the tile detector (steps 1 and 5) as well as the strip one."""
+    img = synth.synth_image(seed, w, h)
+    ak = _ak(gpu_lib, w, h, extrema_3d=1, derivative_factor=dfac)
+    kp, d = ak.detect_and_compute(img)
+    orc = _oracle(oracle, w, h, extrema_3d=1, derivative_factor=dfac)
+    okp, od = orc.run(img)
+    ext, oext = ak.extrema(), orc.extrema()
+    assert ext.tobytes() == oext.tobytes(), (len(ext), len(oext))
+    assert kp.tobytes() == okp.tobytes() and np.array_equal(d, od)
+    plain = _oracle(oracle, w, h, derivative_factor=dfac)
+    plain.run(img)
+    assert 0 < len(oext) < len(plain.extrema())  # the rule removes candidates, never adds
+
+
+def test_extrema_3d_uneven_batch(gpu_lib, oracle):
+    sizes = synth.uneven_sizes(77, 5)
+    imgs = [synth.synth_image(7700 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    b = gpu_lib.Batch(gpu_lib.AKAZEOptions(extrema_3d=1), sizes)
+    b.upload(imgs)
+    b.run()
+    for i, ((w, h), img) in enumerate(zip(sizes, imgs)):
+        kp, d = b.results(i)
+        okp, od = _oracle(oracle, w, h, extrema_3d=1).run(img)
+        assert kp.tobytes() == okp.tobytes() and np.array_equal(d, od), (i, w, h)
+
+
+@pytest.mark.parametrize("desc,channels,size", [(5, 1, 0), (5, 2, 0), (5, 3, 256), (5, 1, 64), (5, 2, 100),
+                                                (4, 3, 128), (4, 2, 0), (5, 3, 486)])
+def test_descriptor_modes_match_oracle(gpu_lib, oracle, desc, channels, size):
+    """descriptor_channels 1 and 2 (rows of ceil(162 c / 8) bytes; the second
+    channel of 2 is the gradient magnitude) and the random-bit subsets of
+    descriptor_size bits (generateDescriptorSubsample, AKAZE.cpp:498-603),
+    rotation-invariant and upright, against the oracle bit for bit; the
+    matcher on those rows too."""
+    w, h = 640, 480
+    img = synth.synth_image(4100 + channels + size, w, h)
+    kw = dict(descriptor=desc, descriptor_channels=channels, descriptor_size=size)
+    ak = _ak(gpu_lib, w, h, **kw)
+    kp, d = ak.detect_and_compute(img)
+    okp, od = _oracle(oracle, w, h, **kw).run(img)
+    rb = (size if size else 162 * channels) + 7 >> 3
+    assert d.shape == od.shape == (len(okp), rb)
+    assert kp.tobytes() == okp.tobytes()
+    assert np.array_equal(d, od)
+    bits = size if size else 162 * channels
+    if bits % 8:  # the pad bits of the last byte stay zero
+        assert not np.any(d[:, -1] >> (bits % 8))
+    m = gpu_lib.Matcher().bfmatch(d, d[::-1].copy())
+    assert m.tobytes() == oracle.bfmatch(od, od[::-1].copy()).tobytes()
+
+
 def test_upright_mldb_matches_oracle(gpu_lib, oracle):
     img = synth.synth_image(4040, 640, 480)
     ak = _ak(gpu_lib, 640, 480, descriptor=4)

@@ -41,9 +41,11 @@ def test_defaults_mirror_akazeoptions(gpu_lib):
 
 @pytest.mark.parametrize("field,value,status", [
     ("descriptor", 1, 6),            # SURF: not implemented (the reference prints the same)
-    ("descriptor_size", 64, 6),      # random bit subsets: not implemented
-    ("descriptor_channels", 2, 6),   # only the 3-channel row; never a silently wrong row size
-    ("descriptor_channels", 1, 6),
+    ("descriptor_size", 487, 1),     # more bits than the full 3-channel descriptor (AKAZE.cpp:508-509)
+    ("descriptor_size", -1, 1),
+    ("descriptor_channels", 4, 1),   # 1, 2 or 3 channels
+    ("descriptor_channels", 0, 1),
+    ("extrema_3d", 2, 1),
     ("omax", 0, 1),
     ("kcontrast_nbins", 0, 1),
     ("soffset", 0.1, 1),
@@ -124,3 +126,12 @@ def test_cxx_wrapper_compiles_and_links(gpu_lib, tmp_path, opencv_branch):
     assert "upright, other diffusivity" in r.stdout
     r = subprocess.run([str(out), "--descriptor", "9"], capture_output=True, text=True)  # out of range -> MLDB
     assert "akaze_options.descriptor".ljust(33) + " =  5" in r.stdout.splitlines()
+
+
+@pytest.mark.parametrize("channels,size,want", [(3, 0, 61), (2, 0, 41), (1, 0, 21), (3, 256, 32), (1, 64, 8),
+                                                (2, 100, 13), (3, 486, 61)])
+def test_descriptor_row_bytes(gpu_lib, channels, size, want):
+    """AKAZE.cpp:412-423: ceil(162 * channels / 8) bytes for the full M-LDB,
+    ceil(descriptor_size / 8) for the random-bit subset."""
+    o = gpu_lib.AKAZEOptions(descriptor_channels=channels, descriptor_size=size)
+    assert gpu_lib.descriptor_bytes(o) == want
