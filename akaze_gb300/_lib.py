@@ -46,7 +46,7 @@ class AkzOptions(ctypes.Structure):
         ("descriptor_pattern_size", ctypes.c_int), ("kcontrast", ctypes.c_float),
         ("kcontrast_percentile", ctypes.c_float), ("kcontrast_nbins", ctypes.c_size_t),
         ("save_scale_space", ctypes.c_int), ("save_keypoints", ctypes.c_int), ("verbosity", ctypes.c_int),
-        ("ncudaimages", ctypes.c_int), ("maxkeypoints", ctypes.c_int), ("extrema_3d", ctypes.c_int),
+        ("ncudaimages", ctypes.c_int), ("maxkeypoints", ctypes.c_int), ("extrema_3d", ctypes.c_int), ("fast_math", ctypes.c_int),
     ]
 
 

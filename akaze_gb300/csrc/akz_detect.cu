@@ -125,7 +125,7 @@ __device__ __forceinline__ int akz_refl_clamp(int i, int n)
   return akz_clampi(i, 0, n - 1);
 }
 
-template <int ST>
+template <int ST, bool FUSED>
 __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, const akz_level_desc &L, float *sm, int tx0,
                                                  int ty0)
 {
@@ -172,8 +172,8 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
       const float2 lc = (ST & 1) ? make_float2(sd[d + ST], sd[d + ST + 1]) : ld2(sd + d + ST);
       const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
       const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(lc, uc);
-      const float2 a = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
-      const float2 b = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+      const float2 a = akz_lin2<FUSED>(fac1, ax, fac2, bx);
+      const float2 b = akz_lin2<FUSED>(fac1, ay, fac2, by);
       st2(ox + d, a);
       st2(oy + d, b);
       const int x = tx0 - A + d; /* even */
@@ -202,14 +202,14 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
       const float2 xdc = (ST & 1) ? make_float2(xd[d], xd[d + 1]) : ld2(xd + d);
       const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
       const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(xdc, xuc);
-      const float2 lxx = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
-      const float2 lyx = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+      const float2 lxx = akz_lin2<FUSED>(fac1, ax, fac2, bx);
+      const float2 lyx = akz_lin2<FUSED>(fac1, ay, fac2, by);
       const float2 vul = ld2(yu + d - ST), vur = ld2(yu + d + ST), vll = ld2(yd + d - ST), vlr = ld2(yd + d + ST);
       const float2 yuc = (ST & 1) ? make_float2(yu[d], yu[d + 1]) : ld2(yu + d);
       const float2 ydc = (ST & 1) ? make_float2(yd[d], yd[d + 1]) : ld2(yd + d);
       const float2 cy = f2sub(f2sub(f2add(vlr, vll), vur), vul), dy = f2sub(ydc, yuc);
-      const float2 lyy = f2add(make_float2(fac1 * cy.x, fac1 * cy.y), make_float2(fac2 * dy.x, fac2 * dy.y));
-      st2(o + e, f2sub(make_float2(lxx.x * lyy.x, lxx.y * lyy.y), make_float2(lyx.x * lyx.x, lyx.y * lyx.y)));
+      const float2 lyy = akz_lin2<FUSED>(fac1, cy, fac2, dy);
+      st2(o + e, akz_det2<FUSED>(lxx, lyy, lyx));
     }
   };
   /* a centre tap of a ring row: a pair, or two floats for odd ST */
@@ -232,8 +232,8 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
       const float2 ll = t ? L3 : L2, lc = t ? C3 : C2, lr = t ? R3 : R2;
       const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
       const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(lc, uc);
-      const float2 a = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
-      const float2 b = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+      const float2 a = akz_lin2<FUSED>(fac1, ax, fac2, bx);
+      const float2 b = akz_lin2<FUSED>(fac1, ay, fac2, by);
       const int r = rA + t * ST;
       st2(sX + (r & (ND - 1)) * 128 + d, a);
       st2(sY + (r & (ND - 1)) * 128 + d, b);
@@ -270,12 +270,12 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
       const float2 yuc = t ? YC1 : YC0, ydc = t ? YC3 : YC2;
       const float2 ax = f2sub(f2sub(f2add(ur, lr), ul), ll), bx = f2sub(cr, cl);
       const float2 ay = f2sub(f2sub(f2add(lr, ll), ur), ul), by = f2sub(xdc, xuc);
-      const float2 lxx = f2add(make_float2(fac1 * ax.x, fac1 * ax.y), make_float2(fac2 * bx.x, fac2 * bx.y));
-      const float2 lyx = f2add(make_float2(fac1 * ay.x, fac1 * ay.y), make_float2(fac2 * by.x, fac2 * by.y));
+      const float2 lxx = akz_lin2<FUSED>(fac1, ax, fac2, bx);
+      const float2 lyx = akz_lin2<FUSED>(fac1, ay, fac2, by);
       const float2 cy = f2sub(f2sub(f2add(vlr, vll), vur), vul), dy = f2sub(ydc, yuc);
-      const float2 lyy = f2add(make_float2(fac1 * cy.x, fac1 * cy.y), make_float2(fac2 * dy.x, fac2 * dy.y));
+      const float2 lyy = akz_lin2<FUSED>(fac1, cy, fac2, dy);
       st2(sE + ((rA + t * ST) & (NE - 1)) * EW + e,
-          f2sub(make_float2(lxx.x * lyy.x, lxx.y * lyy.y), make_float2(lyx.x * lyx.x, lyx.y * lyx.y)));
+          akz_det2<FUSED>(lxx, lyy, lyx));
     }
   };
   const int xlo = max(akz_border_lo(L.border), tx0), xhi = min(akz_border_hi(L.border, W), tx0 + TW - 1);
@@ -345,6 +345,7 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
   akz_cp_async_wait_all();
 }
 
+template <bool FUSED>
 __global__ void __launch_bounds__(256) k_detect_strip(akz_detect_params p)
 {
   extern __shared__ float sm[];
@@ -355,11 +356,11 @@ __global__ void __launch_bounds__(256) k_detect_strip(akz_detect_params p)
   const int lt = blockIdx.x - sg.tile_begin;
   const int tx0 = (lt % sg.tiles_x) * akz_strip_tile_width_rt(st), ty0 = (lt / sg.tiles_x) * AKZ_STRIP_CH;
   if (st == 2)
-    akz_detect_strip<2>(p, L, sm, tx0, ty0);
+    akz_detect_strip<2, FUSED>(p, L, sm, tx0, ty0);
   else if (st == 3)
-    akz_detect_strip<3>(p, L, sm, tx0, ty0);
+    akz_detect_strip<3, FUSED>(p, L, sm, tx0, ty0);
   else if (st == 4)
-    akz_detect_strip<4>(p, L, sm, tx0, ty0);
+    akz_detect_strip<4, FUSED>(p, L, sm, tx0, ty0);
 }
 
 size_t akz_detect_strip_smem()
@@ -372,9 +373,16 @@ cudaError_t akz_launch_detect_strip(const akz_detect_params &p, int ntiles, cuda
 {
   if (ntiles <= 0) return cudaSuccess;
   const size_t smem = akz_detect_strip_smem();
-  cudaError_t e = cudaFuncSetAttribute(k_detect_strip, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_detect_strip<<<ntiles, 256, smem, s>>>(p);
+  cudaError_t e;
+  if (p.fused) {
+    e = cudaFuncSetAttribute(k_detect_strip<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_detect_strip<true><<<ntiles, 256, smem, s>>>(p);
+  } else {
+    e = cudaFuncSetAttribute(k_detect_strip<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_detect_strip<false><<<ntiles, 256, smem, s>>>(p);
+  }
   return cudaGetLastError();
 }
 

@@ -163,6 +163,57 @@ __device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c)
 }
 __device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
 __device__ __forceinline__ void st2(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
+/* Packed product, for the fused-arithmetic kernels only (see above). */
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b)
+{
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(akz_f2u(a)), "l"(akz_f2u(b)));
+  return akz_u2f(r);
+}
+
+/* Products and multiply-adds of the level and detector kernels in their two
+ * arithmetic modes.  FUSED = false: the reference's operation order, every
+ * product and sum rounded on its own (scalar products, packed sums), which
+ * reproduces the CPU restatement bit for bit.  FUSED = true: packed products
+ * and packed fused multiply-adds (one rounding per multiply-add), about half
+ * the instructions; results stay within the tolerances the fused mode is
+ * tested to (levels 1e-4 relative). */
+template <bool FUSED>
+__device__ __forceinline__ float2 akz_k2(float k, float2 v) /* k * v */
+{
+  if (FUSED) return f2mul(make_float2(k, k), v);
+  return make_float2(k * v.x, k * v.y);
+}
+template <bool FUSED>
+__device__ __forceinline__ float2 akz_axpy2(float k, float2 v, float2 acc) /* acc + k * v */
+{
+  if (FUSED) return f2fma(make_float2(k, k), v, acc);
+  return f2add(acc, make_float2(k * v.x, k * v.y));
+}
+template <bool FUSED>
+__device__ __forceinline__ float2 akz_mul2(float2 a, float2 b) /* a * b */
+{
+  if (FUSED) return f2mul(a, b);
+  return make_float2(a.x * b.x, a.y * b.y);
+}
+template <bool FUSED>
+__device__ __forceinline__ float2 akz_sq2sum(float2 a, float2 b) /* a^2 + b^2 */
+{
+  if (FUSED) return f2fma(a, a, f2mul(b, b));
+  return f2add(make_float2(a.x * a.x, a.y * a.y), make_float2(b.x * b.x, b.y * b.y));
+}
+template <bool FUSED>
+__device__ __forceinline__ float2 akz_lin2(float ka, float2 a, float kb, float2 b) /* ka * a + kb * b */
+{
+  if (FUSED) return f2fma(make_float2(ka, ka), a, f2mul(make_float2(kb, kb), b));
+  return f2add(make_float2(ka * a.x, ka * a.y), make_float2(kb * b.x, kb * b.y));
+}
+template <bool FUSED>
+__device__ __forceinline__ float2 akz_det2(float2 a, float2 b, float2 c) /* a * b - c * c */
+{
+  if (FUSED) return f2fma(a, b, f2mul(make_float2(-c.x, -c.y), c));
+  return f2sub(make_float2(a.x * b.x, a.y * b.y), make_float2(c.x * c.x, c.y * c.y));
+}
 
 struct akz_plane_acc {
   const float *p;

@@ -345,6 +345,7 @@ static akz_status akz_validate(const akz_options *o)
     return akz_fail(AKZ_ERR_INVALID_ARG, "kcontrast_percentile must be in [0, 1]");
   if (o->maxkeypoints < 1) return akz_fail(AKZ_ERR_INVALID_ARG, "maxkeypoints must be positive");
   if (o->extrema_3d != 0 && o->extrema_3d != 1) return akz_fail(AKZ_ERR_INVALID_ARG, "extrema_3d must be 0 or 1");
+  if (o->fast_math != 0 && o->fast_math != 1) return akz_fail(AKZ_ERR_INVALID_ARG, "fast_math must be 0 or 1");
   return AKZ_OK;
 }
 
@@ -915,6 +916,7 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe 
     for (int k = 0; k < 3; k++) lp.taps1[k] = b->taps1[k];
     lp.nbins = (int)b->opt.kcontrast_nbins;
     lp.hist = b->d_hist;
+    lp.fused = b->opt.fast_math;
     CK(akz_launch_level0(lp, b->l0_tiles, s));
     CK(akz_launch_contrast_final(t, b->d_hist, lp.nbins, b->opt.kcontrast_percentile, b->d_kc, s));
     if (pe) {
@@ -967,6 +969,7 @@ static akz_status akz_stage_scale(akz_batch *b, cudaStream_t s, cudaEvent_t *pe 
       p.chk = b->d_sg_chk;
       p.gate = gate;
       p.gate_tol = b->sg_tol;
+      p.fused = b->opt.fast_math;
       return akz_launch_fed(p, fl.ntiles, fl.tw, fl.th, s);
     };
     if (!b->sg_on || l / b->opt.nsublevels < b->sg_first_octave) {
@@ -1016,6 +1019,7 @@ static akz_status akz_stage_detect(akz_batch *b, cudaStream_t s, cudaEvent_t *pe
   dp.fac1 = fac1;
   dp.fac2 = fac2;
   dp.store_det = b->opt.extrema_3d;
+  dp.fused = b->opt.fast_math;
   CK(akz_launch_detect(dp, b->detect_tiles, b->max_step, s));
   dp.segs = b->d_segs + b->strip_off;
   dp.nsegs = b->strip_n;
@@ -1175,6 +1179,7 @@ AKZ_API akz_status akz_options_default(akz_options *o)
   o->ncudaimages = 4;
   o->maxkeypoints = 16 * 8192;
   o->extrema_3d = 0;
+  o->fast_math = 0;
   return AKZ_OK;
 }
 

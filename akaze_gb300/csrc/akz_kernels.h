@@ -47,6 +47,7 @@ struct akz_level0_params {
   float taps1[3]; /* sigma 1 */
   int nbins;
   unsigned int *hist;
+  int fused; /* 1: the fused-arithmetic kernel (akz_options.fast_math) */
 };
 
 struct akz_gauss_params {
@@ -85,6 +86,7 @@ struct akz_fed_params {
   int dst;            /* 0 Lt of the level, 1 T1, 2 T2, 3 chk */
   int write_g;        /* store the conductance for later launches */
   int diffusivity;
+  int fused;          /* 1: the fused-arithmetic kernel (akz_options.fast_math) */
   float taps1[5];
   float h[AKZ_MAX_CHUNK]; /* 0.5 * tau per step */
   float *chk;         /* dst 3: a plane with the level's pitch */
@@ -117,6 +119,7 @@ struct akz_detect_params {
   int *rowcnt;
   float thr, fac1, fac2;
   int store_det; /* 1: keep every level's determinant in its plane (L.ldet) for the 3 x 3 x 3 rule */
+  int fused;     /* 1: the strip detector's fused-arithmetic kernel (akz_options.fast_math) */
 };
 
 struct akz_extract_params {

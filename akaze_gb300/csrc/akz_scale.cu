@@ -167,6 +167,7 @@ __global__ void k_contrast_final(akz_tables t, const unsigned int *hist, int nbi
  * the reference's operation order, so every value equals the per-pixel
  * kernels k_gauss0 / k_contrast. */
 
+template <bool FUSED>
 __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
 {
   constexpr int TW = AKZ_L0_TW, TH = AKZ_L0_TH;
@@ -224,17 +225,17 @@ __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
     const float2 s17 = f2add(make_float2(A0.y, A1.x), make_float2(A3.y, A4.x));
     const float2 s26 = f2add(A1, A3);
     const float2 s35 = f2add(make_float2(A1.y, A2.x), make_float2(A2.y, A3.x));
-    float2 acc = make_float2(t0 * s08.x, t0 * s08.y);
-    acc = f2add(acc, make_float2(t1 * s17.x, t1 * s17.y));
-    acc = f2add(acc, make_float2(t2 * s26.x, t2 * s26.y));
-    acc = f2add(acc, make_float2(t3 * s35.x, t3 * s35.y));
-    acc = f2add(acc, make_float2(t4 * A2.x, t4 * A2.y));
+    float2 acc = akz_k2<FUSED>(t0, s08);
+    acc = akz_axpy2<FUSED>(t1, s17, acc);
+    acc = akz_axpy2<FUSED>(t2, s26, acc);
+    acc = akz_axpy2<FUSED>(t3, s35, acc);
+    acc = akz_axpy2<FUSED>(t4, A2, acc);
     st2(sA + r * TW + c, acc);
     if (r >= 1 && r <= BH) { /* sigma 1 at x = tx0 + c, c + 1: taps sP columns c + 2 .. c + 7 */
       const float2 s15 = s26, s24 = s35;
-      float2 g = make_float2(k0 * s15.x, k0 * s15.y);
-      g = f2add(g, make_float2(k1 * s24.x, k1 * s24.y));
-      g = f2add(g, make_float2(k2 * A2.x, k2 * A2.y));
+      float2 g = akz_k2<FUSED>(k0, s15);
+      g = akz_axpy2<FUSED>(k1, s24, g);
+      g = akz_axpy2<FUSED>(k2, A2, g);
       float *o = sB + (r - 1) * BW + c + 1;
       o[0] = g.x;
       o[1] = g.y;
@@ -244,8 +245,13 @@ __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
     const int r = tid >> 1, d = (tid & 1) ? BW - 1 : 0;
     const float *q = sP + (r + 1) * PW + d + 3; /* centre */
     float g = k0 * (q[-2] + q[2]);
-    g = g + k1 * (q[-1] + q[1]);
-    g = g + k2 * q[0];
+    if (FUSED) {
+      g = __fmaf_rn(k1, q[-1] + q[1], g);
+      g = __fmaf_rn(k2, q[0], g);
+    } else {
+      g = g + k1 * (q[-1] + q[1]);
+      g = g + k2 * q[0];
+    }
     sB[r * BW + d] = g;
   }
   __syncthreads();
@@ -266,11 +272,11 @@ __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
       for (int j = 0; j < 8; j++) {
         const float2 s08 = f2add(v[j], v[j + 8]), s17 = f2add(v[j + 1], v[j + 7]);
         const float2 s26 = f2add(v[j + 2], v[j + 6]), s35 = f2add(v[j + 3], v[j + 5]);
-        float2 acc = make_float2(t0 * s08.x, t0 * s08.y);
-        acc = f2add(acc, make_float2(t1 * s17.x, t1 * s17.y));
-        acc = f2add(acc, make_float2(t2 * s26.x, t2 * s26.y));
-        acc = f2add(acc, make_float2(t3 * s35.x, t3 * s35.y));
-        acc = f2add(acc, make_float2(t4 * v[j + 4].x, t4 * v[j + 4].y));
+        float2 acc = akz_k2<FUSED>(t0, s08);
+        acc = akz_axpy2<FUSED>(t1, s17, acc);
+        acc = akz_axpy2<FUSED>(t2, s26, acc);
+        acc = akz_axpy2<FUSED>(t3, s35, acc);
+        acc = akz_axpy2<FUSED>(t4, v[j + 4], acc);
         const int y = ty0 + g * 8 + j;
         if (y < H) {
           float *o = out + (long long)y * L.pitch + x;
@@ -298,11 +304,11 @@ __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
       { /* sigma-1 row y - 1 + (k - 4), y = ty0 + 8 g */
         const float2 sa04 = f2add(ba[0], ba[4]), sa13 = f2add(ba[1], ba[3]);
         const float2 sb04 = f2add(bb[0], bb[4]), sb13 = f2add(bb[1], bb[3]);
-        float2 a = make_float2(k0 * sa04.x, k0 * sa04.y), b = make_float2(k0 * sb04.x, k0 * sb04.y);
-        a = f2add(a, make_float2(k1 * sa13.x, k1 * sa13.y));
-        b = f2add(b, make_float2(k1 * sb13.x, k1 * sb13.y));
-        a = f2add(a, make_float2(k2 * ba[2].x, k2 * ba[2].y));
-        b = f2add(b, make_float2(k2 * bb[2].x, k2 * bb[2].y));
+        float2 a = akz_k2<FUSED>(k0, sa04), b = akz_k2<FUSED>(k0, sb04);
+        a = akz_axpy2<FUSED>(k1, sa13, a);
+        b = akz_axpy2<FUSED>(k1, sb13, b);
+        a = akz_axpy2<FUSED>(k2, ba[2], a);
+        b = akz_axpy2<FUSED>(k2, bb[2], b);
         ga[0] = ga[1];
         ga[1] = ga[2];
         ga[2] = a;
@@ -315,12 +321,12 @@ __global__ void __launch_bounds__(256) k_level0(akz_level0_params p)
       const float2 m0 = ga[0], m1 = gb[0], c0 = ga[1], c1 = gb[1], p0 = ga[2], p1 = gb[2];
       const float2 hm = f2sub(m1, m0), h0 = f2sub(c1, c0), hp = f2sub(p1, p0); /* v[x+1] - v[x-1] */
       const float2 u = f2add(hm, hp);
-      const float2 lx = f2add(make_float2(3.0f * u.x, 3.0f * u.y), make_float2(10.0f * h0.x, 10.0f * h0.y));
+      const float2 lx = akz_lin2<FUSED>(3.0f, u, 10.0f, h0);
       const float2 sp = f2add(p0, p1), sm = f2add(m0, m1); /* (v[x-1] + v[x+1]) */
-      const float2 syp = f2add(make_float2(3.0f * sp.x, 3.0f * sp.y), make_float2(10.0f * p0.y, 10.0f * p1.x));
-      const float2 sym = f2add(make_float2(3.0f * sm.x, 3.0f * sm.y), make_float2(10.0f * m0.y, 10.0f * m1.x));
+      const float2 syp = akz_lin2<FUSED>(3.0f, sp, 10.0f, make_float2(p0.y, p1.x));
+      const float2 sym = akz_lin2<FUSED>(3.0f, sm, 10.0f, make_float2(m0.y, m1.x));
       const float2 ly = f2sub(syp, sym);
-      const float2 m = f2add(make_float2(lx.x * lx.x, lx.y * lx.y), make_float2(ly.x * ly.x, ly.y * ly.y));
+      const float2 m = akz_sq2sum<FUSED>(lx, ly);
       const int y = ty0 + g * 8 + k - 6;
       if (y < 1 || y >= H - 1) continue;
       float *o = mp + (long long)y * L.pitch + x;
@@ -413,9 +419,16 @@ cudaError_t akz_launch_level0(const akz_level0_params &p, int ntiles, cudaStream
   if (ntiles <= 0) return cudaSuccess;
   constexpr int smem = ((AKZ_L0_TH + 8) * (AKZ_L0_TW + 8) + (AKZ_L0_TH + 8) * AKZ_L0_TW + (AKZ_L0_TH + 6) * (AKZ_L0_TW + 2)) *
                        (int)sizeof(float);
-  cudaError_t e0 = cudaFuncSetAttribute(k_level0, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e0 != cudaSuccess) return e0;
-  k_level0<<<ntiles, 256, smem, s>>>(p);
+  cudaError_t e0;
+  if (p.fused) {
+    e0 = cudaFuncSetAttribute(k_level0<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e0 != cudaSuccess) return e0;
+    k_level0<true><<<ntiles, 256, smem, s>>>(p);
+  } else {
+    e0 = cudaFuncSetAttribute(k_level0<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e0 != cudaSuccess) return e0;
+    k_level0<false><<<ntiles, 256, smem, s>>>(p);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_contrast_hist<<<ntiles, 256, 0, s>>>(p);
@@ -546,8 +559,16 @@ __device__ __forceinline__ float akz_conductance_m(float m, float inv_k, int typ
  * where both round to the same float that float is its correct rounding; the
  * lanes where they differ (a rounding midpoint within 2^-41 of v, about one
  * in 2^17) take the double evaluation. */
+template <bool FUSED>
 __device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
 {
+  if (FUSED) { /* one rounding of 1 + f, the hardware reciprocal (relative error below 2^-22) */
+    const float2 s = f2fma(make_float2(inv_k, inv_k), m, make_float2(1.0f, 1.0f));
+    float2 q;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(q.x) : "f"(s.x));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(q.y) : "f"(s.y));
+    return q;
+  }
   const float2 f = make_float2(inv_k * m.x, inv_k * m.y);
   const float2 one = make_float2(1.0f, 1.0f);
   const float2 s = f2add(one, f);
@@ -595,7 +616,7 @@ __device__ __forceinline__ float2 akz_pm_g2_pair(float2 m, float inv_k)
  *             gy = s[y+1] - s[y-1],  s = 3*(v[x-1] + v[x+1]) + 10*v[x].
  * Returns false when the input box did not arrive within the bounded wait
  * (the image's status is then AKZ_ERR_TIMEOUT). */
-template <int SRCK>
+template <int SRCK, bool FUSED>
 __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const akz_level_desc &L,
                                                  const akz_image_desc &I, int level_desc, float *sm, int ox, int oy,
                                                  int tx0, int ty0, int tx1, int ty1, int lx0, int ly0, float (&g)[3][4])
@@ -697,9 +718,9 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
     const float2 A = ld2(r), B = ld2(r + 2), C = ld2(r + 4);
     const float2 s04 = f2add(A, C);
     const float2 s13 = f2add(make_float2(A.y, B.x), make_float2(B.y, C.x));
-    float2 acc = make_float2(k0 * s04.x, k0 * s04.y);
-    acc = f2add(acc, make_float2(k1 * s13.x, k1 * s13.y));
-    acc = f2add(acc, make_float2(k2 * B.x, k2 * B.y));
+    float2 acc = akz_k2<FUSED>(k0, s04);
+    acc = akz_axpy2<FUSED>(k1, s13, acc);
+    acc = akz_axpy2<FUSED>(k2, B, acc);
     st2(sT + row * SS + c, acc);
   };
   {
@@ -725,9 +746,9 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
     for (int j = 0; j < VR; j++) {
       const float2 s04 = f2add(v[j], v[j + 4]);
       const float2 s13 = f2add(v[j + 1], v[j + 3]);
-      float2 acc = make_float2(k0 * s04.x, k0 * s04.y);
-      acc = f2add(acc, make_float2(k1 * s13.x, k1 * s13.y));
-      acc = f2add(acc, make_float2(k2 * v[j + 2].x, k2 * v[j + 2].y));
+      float2 acc = akz_k2<FUSED>(k0, s04);
+      acc = akz_axpy2<FUSED>(k1, s13, acc);
+      acc = akz_axpy2<FUSED>(k2, v[j + 2], acc);
       const int n = g * VR + j;
       st2(sS + n * SS + c, acc);
       const int y = oy - 1 + n;
@@ -780,15 +801,15 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
       const float2 P = make_float2(A.y, B.x), Q = make_float2(B.y, C.x);
       dh[j] = f2sub(Q, P);
       const float2 t = f2add(P, Q);
-      sh[j] = f2add(make_float2(3.0f * t.x, 3.0f * t.y), make_float2(10.0f * P.y, 10.0f * Q.x));
+      sh[j] = akz_lin2<FUSED>(3.0f, t, 10.0f, make_float2(P.y, Q.x));
     }
 #pragma unroll
     for (int r = 0; r < 3; r++) {
       const float2 u = f2add(dh[r], dh[r + 2]);
-      const float2 gx = f2add(make_float2(3.0f * u.x, 3.0f * u.y), make_float2(10.0f * dh[r + 1].x, 10.0f * dh[r + 1].y));
+      const float2 gx = akz_lin2<FUSED>(3.0f, u, 10.0f, dh[r + 1]);
       const float2 gy = f2sub(sh[r + 2], sh[r]);
-      const float2 m = f2add(make_float2(gx.x * gx.x, gx.y * gx.y), make_float2(gy.x * gy.x, gy.y * gy.y));
-      const float2 gv = p.diffusivity == 1 ? akz_pm_g2_pair(m, inv_k)
+      const float2 m = akz_sq2sum<FUSED>(gx, gy);
+      const float2 gv = p.diffusivity == 1 ? akz_pm_g2_pair<FUSED>(m, inv_k)
                                            : make_float2(akz_conductance_m(m.x, inv_k, p.diffusivity),
                                                          akz_conductance_m(m.y, inv_k, p.diffusivity));
       g[r][2 * h] = gv.x;
@@ -856,8 +877,10 @@ __device__ __forceinline__ void akz_fed_pairs(const float (&g)[3][4], const floa
  * Each flux product is formed once and used twice, which is exact: the
  * reference's xneg at x+1 is (c(x) + c(x+1)) * (L(x+1) - L(x)), the same
  * operands in the same order as xpos at x, and likewise yneg at y+1 and ypos
- * at y.  Additions run as packed FP32x2 pairs; products stay scalar.  above
+ * at y.  Additions run as packed FP32x2 pairs; products stay scalar (with
+ * FUSED: packed products and L + h * t as one packed multiply-add).  above
  * and below are the rows next to the band (old values). */
+template <bool FUSED>
 __device__ __forceinline__ void akz_fed_step4(float (&Lp)[3][4], float4 above, float4 below, float h,
                                               const float (&gh)[3][5], const float (&gs)[3][4], const float (&gn)[4])
 {
@@ -872,10 +895,11 @@ __device__ __forceinline__ void akz_fed_step4(float (&Lp)[3][4], float4 above, f
   {
     const float2 d0 = f2sub(make_float2(Lp[0][0], Lp[0][1]), make_float2(ab[0], ab[1]));
     const float2 d1 = f2sub(make_float2(Lp[0][2], Lp[0][3]), make_float2(ab[2], ab[3]));
-    Fn[0] = gn[0] * d0.x;
-    Fn[1] = gn[1] * d0.y;
-    Fn[2] = gn[2] * d1.x;
-    Fn[3] = gn[3] * d1.y;
+    const float2 f0 = akz_mul2<FUSED>(make_float2(gn[0], gn[1]), d0), f1 = akz_mul2<FUSED>(make_float2(gn[2], gn[3]), d1);
+    Fn[0] = f0.x;
+    Fn[1] = f0.y;
+    Fn[2] = f1.x;
+    Fn[3] = f1.y;
   }
   float nv[3][4];
 #pragma unroll
@@ -885,8 +909,9 @@ __device__ __forceinline__ void akz_fed_step4(float (&Lp)[3][4], float4 above, f
     const float2 e01 = f2sub(make_float2(L[0], L[1]), make_float2(Lw[r], L[0]));
     const float2 e23 = f2sub(make_float2(L[2], L[3]), make_float2(L[1], L[2]));
     const float e4 = Le[r] - L[3];
-    const float F0 = gh[r][0] * e01.x, F1 = gh[r][1] * e01.y, F2 = gh[r][2] * e23.x, F3 = gh[r][3] * e23.y,
-                F4 = gh[r][4] * e4;
+    const float2 F01 = akz_mul2<FUSED>(make_float2(gh[r][0], gh[r][1]), e01);
+    const float2 F23 = akz_mul2<FUSED>(make_float2(gh[r][2], gh[r][3]), e23);
+    const float F0 = F01.x, F1 = F01.y, F2 = F23.x, F3 = F23.y, F4 = gh[r][4] * e4;
     const float2 xs01 = f2sub(make_float2(F1, F2), make_float2(F0, F1)); /* xpos - xneg */
     const float2 xs23 = f2sub(make_float2(F3, F4), make_float2(F2, F3));
     float nb[4];
@@ -894,11 +919,13 @@ __device__ __forceinline__ void akz_fed_step4(float (&Lp)[3][4], float4 above, f
     for (int k = 0; k < 4; k++) nb[k] = r < 2 ? Lp[r + 1][k] : bl[k];
     const float2 ds01 = f2sub(make_float2(nb[0], nb[1]), make_float2(L[0], L[1]));
     const float2 ds23 = f2sub(make_float2(nb[2], nb[3]), make_float2(L[2], L[3]));
-    const float Fs[4] = {gs[r][0] * ds01.x, gs[r][1] * ds01.y, gs[r][2] * ds23.x, gs[r][3] * ds23.y}; /* ypos */
-    const float2 t01 = f2sub(f2add(xs01, make_float2(Fs[0], Fs[1])), make_float2(Fn[0], Fn[1]));
-    const float2 t23 = f2sub(f2add(xs23, make_float2(Fs[2], Fs[3])), make_float2(Fn[2], Fn[3]));
-    const float2 n01 = f2add(make_float2(L[0], L[1]), make_float2(h * t01.x, h * t01.y));
-    const float2 n23 = f2add(make_float2(L[2], L[3]), make_float2(h * t23.x, h * t23.y));
+    const float2 Fs01 = akz_mul2<FUSED>(make_float2(gs[r][0], gs[r][1]), ds01); /* ypos */
+    const float2 Fs23 = akz_mul2<FUSED>(make_float2(gs[r][2], gs[r][3]), ds23);
+    const float Fs[4] = {Fs01.x, Fs01.y, Fs23.x, Fs23.y};
+    const float2 t01 = f2sub(f2add(xs01, Fs01), make_float2(Fn[0], Fn[1]));
+    const float2 t23 = f2sub(f2add(xs23, Fs23), make_float2(Fn[2], Fn[3]));
+    const float2 n01 = akz_axpy2<FUSED>(h, t01, make_float2(L[0], L[1]));
+    const float2 n23 = akz_axpy2<FUSED>(h, t23, make_float2(L[2], L[3]));
     nv[r][0] = n01.x;
     nv[r][1] = n01.y;
     nv[r][2] = n23.x;
@@ -912,6 +939,7 @@ __device__ __forceinline__ void akz_fed_step4(float (&Lp)[3][4], float4 above, f
     for (int k = 0; k < 4; k++) Lp[r][k] = nv[r][k];
 }
 
+template <bool FUSED>
 __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
 {
   extern __shared__ __align__(128) float sm_raw[];
@@ -946,11 +974,11 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
     float *sP = sm, *sT = sm + (RH + 6) * PS;
     bool ok;
     if (srck == 1)
-      ok = akz_fed_prologue<1>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0, g);
+      ok = akz_fed_prologue<1, FUSED>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0, g);
     else if (srck == 0)
-      ok = akz_fed_prologue<0>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0, g);
+      ok = akz_fed_prologue<0, FUSED>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0, g);
     else
-      ok = akz_fed_prologue<2>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0, g);
+      ok = akz_fed_prologue<2, FUSED>(p, L, I, sg.level_desc, sm, ox, oy, tx0, ty0, tx1, ty1, lx0, ly0, g);
     if (!ok) return; /* uniform: every thread saw the same barrier state */
     const float *sL = sP + 3 * PS + 4; /* level values of R0 */
 #pragma unroll
@@ -1015,7 +1043,7 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
                                   : make_float4(Lp[0][0], Lp[0][1], Lp[0][2], Lp[0][3]);
     const float4 below = warp < 15 ? *reinterpret_cast<const float4 *>(xb + ((par * 2 + 0) * 16 + warp + 1) * RW + lx0)
                                    : make_float4(Lp[2][0], Lp[2][1], Lp[2][2], Lp[2][3]);
-    akz_fed_step4(Lp, above, below, p.h[s], gh, gs, gn);
+    akz_fed_step4<FUSED>(Lp, above, below, p.h[s], gh, gs, gn);
     if (s + 1 < d) {
       put(par ^ 1);
       __syncthreads();
@@ -1099,9 +1127,16 @@ cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int, int, cudaSt
   if (p.steps < 0 || p.steps > 8) return cudaErrorInvalidValue; /* 0: Lsmooth, conductance and the start image only */
   if (p.first && !p.tmaps) return cudaErrorInvalidValue;         /* the input box needs the tensor maps */
   const size_t smem = akz_fed_smem_bytes(0, 0, p.steps, p.first);
-  cudaError_t e = cudaFuncSetAttribute(k_fed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_fed<<<ntiles, AKZ_FED_THREADS, smem, s>>>(p);
+  cudaError_t e;
+  if (p.fused) {
+    e = cudaFuncSetAttribute(k_fed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_fed<true><<<ntiles, AKZ_FED_THREADS, smem, s>>>(p);
+  } else {
+    e = cudaFuncSetAttribute(k_fed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_fed<false><<<ntiles, AKZ_FED_THREADS, smem, s>>>(p);
+  }
   return cudaGetLastError();
 }
 
@@ -1125,7 +1160,7 @@ __global__ void k_pm_g2_check(const float *in, float *out, int n, int fn)
   const float a = in[i], b = i + 1 < n ? in[i + 1] : 0.0f;
   float2 r;
   if (fn == 0)
-    r = akz_pm_g2_pair(make_float2(a, b), 1.0f);
+    r = akz_pm_g2_pair<false>(make_float2(a, b), 1.0f);
   else
     r = make_float2(akz_recip1pf(a), akz_recip1pf(b));
   out[i] = r.x;

@@ -81,6 +81,15 @@ typedef struct akz_options {
    *   have), the rule for which the reference passes, and leaves unused, the
    *   adjacent levels to FindExtrema (AKAZE.cpp:340-367, cuda_akaze.cu:727). */
   int extrema_3d;
+  /* Extension: the arithmetic of the scale-space and detector kernels.
+   * 0 (default): every float operation in the reference's order, rounded on
+   *   its own, the PM-g2 reciprocal exactly as the reference's double
+   *   division rounds (bit-identical to the CPU restatement).
+   * 1: fused multiply-adds and the hardware reciprocal in those kernels; the
+   *   results stay within levels 1e-4 relative, >= 99% of keypoints within
+   *   0.5 px at the same level and descriptors within Hamming 2 of the
+   *   reference arithmetic (tests/test_gpu_fast_math.py). */
+  int fast_math;
 } akz_options;
 
 /* cv::KeyPoint layout (28 bytes): pt.x, pt.y, size, angle, response, octave, class_id. */

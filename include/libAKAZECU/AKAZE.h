@@ -174,6 +174,7 @@ struct AKAZEOptions {
   int ncudaimages;
   int maxkeypoints;
   int extrema_3d; /* extension: akz_options.extrema_3d (0, the reference's 3x3 rule, by default) */
+  int fast_math;  /* extension: akz_options.fast_math (0, the reference's arithmetic, by default) */
 
   akz_options to_c() const
   {
@@ -203,6 +204,7 @@ struct AKAZEOptions {
     c.ncudaimages = ncudaimages;
     c.maxkeypoints = maxkeypoints;
     c.extrema_3d = extrema_3d;
+    c.fast_math = fast_math;
     return c;
   }
   void from_c(const akz_options &c)
@@ -231,6 +233,7 @@ struct AKAZEOptions {
     ncudaimages = c.ncudaimages;
     maxkeypoints = c.maxkeypoints;
     extrema_3d = c.extrema_3d;
+    fast_math = c.fast_math;
   }
 
   /* The option listing of AKAZEConfig.h:145-172: one "name =  value" line
