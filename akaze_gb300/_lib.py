@@ -33,6 +33,7 @@ EXPORTS = [
     "akz_batch_detect_describe_packed", "akz_sg_set_tcgen05", "akz_sg_tcgen05_status", "akz_selfcheck_pm_g2",
     "akz_batch_autotune", "akz_batch_set_fed_depth", "akz_batch_submit", "akz_batch_collect_packed",
     "akz_batch_image_info", "akz_batch_set_nms_round_cap", "akz_selfcheck_bounded_wait", "akz_descriptor_bytes",
+    "akz_matcher_set_tensor_cores", "akz_matcher_tensor_status",
 ]
 
 
@@ -79,6 +80,7 @@ def load():
         "akz_version": ([], ctypes.c_char_p), "akz_last_error": ([], ctypes.c_char_p),
         "akz_options_default": ([ctypes.POINTER(AkzOptions)], I),
         "akz_descriptor_bytes": ([ctypes.POINTER(AkzOptions), IP], I),
+        "akz_matcher_set_tensor_cores": ([I], I), "akz_matcher_tensor_status": ([IP], I),
         "akz_plan_info": ([ctypes.POINTER(AkzOptions), I, I, I, IP, IP, IP, IP, IP, ctypes.POINTER(ctypes.c_float), IP,
                            ctypes.POINTER(ctypes.c_float), P, I, IP], I),
         "akz_gaussian_taps": ([ctypes.c_float, P, I, IP], I),

@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libakaze_gb300.so")
-SOURCES = ["akz_scale.cu", "akz_detect.cu", "akz_describe.cu", "akz_match.cu", "akz_engine.cu", "akz_probe.cu", "akz_surrogate.cu", "akz_surrogate_infer.cu", "akz_eval.cu"]
+SOURCES = ["akz_scale.cu", "akz_detect.cu", "akz_describe.cu", "akz_match.cu", "akz_match_tc.cu", "akz_engine.cu",
+           "akz_probe.cu", "akz_surrogate.cu", "akz_surrogate_infer.cu", "akz_eval.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "--expt-relaxed-constexpr",
                 "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden,-Wall,-Wno-unknown-pragmas"]

@@ -100,12 +100,30 @@ __global__ void k_match_merge(const akz_top2 *partial, int nq, int nsplit, int4 
   out[2 * qi + 1] = make_int4(qi, r.si, 0, __float_as_int((float)r.sd));
 }
 
+cudaError_t akz_match_tc_launch(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit,
+                                int nsm, cudaStream_t s);
+cudaError_t akz_match_tc_status(int *timed_out);
+
+/* Process-wide choice of the pair-distance engine for large calls: the
+ * tensor-core kernels (akz_match_tc.cu, on by default) or xor + popc. */
+static int g_akz_match_tc_on = 1;
+#define AKZ_TC_MIN_PAIRS (1LL << 20) /* below ~1 M pairs one popc launch is latency-bound either way */
+
 /* out: 2*nq records {queryIdx, trainIdx, imgIdx, distance(float bits)};
  * partial: scratch of nq*nsplit top-2 records (may be null when nsplit==1). */
 cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit, cudaStream_t s)
 {
   if (nq <= 0) return cudaSuccess;
   if (nsplit < 1) nsplit = 1;
+  if (g_akz_match_tc_on && nt >= 128 && (long long)nq * nt >= AKZ_TC_MIN_PAIRS) {
+    int dev = 0, nsm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = akz_match_tc_launch(dq, nq, dt, nt, dout, partial, nsplit, nsm, s);
+    if (e != cudaSuccess || nsplit == 1) return e;
+    k_match_merge<<<(nq + 255) / 256, 256, 0, s>>>((const akz_top2 *)partial, nq, nsplit, (int4 *)dout);
+    return cudaGetLastError();
+  }
   const int split_len = nt > 0 ? (nt + nsplit - 1) / nsplit : 0;
   const dim3 grid((nq + AKZ_MQ - 1) / AKZ_MQ, nsplit);
   k_match<<<grid, AKZ_MQ, 0, s>>>((const uint4 *)dq, (const uint4 *)dt, nq, nt, split_len, nsplit, (akz_top2 *)partial,
@@ -205,6 +223,21 @@ extern "C" AKZ_API akz_status akz_matcher_bfmatch_noalloc(const uint8_t *query64
   const int fit = AKZ_NOALLOC_MAX_RECORDS / nq;
   if (ns > fit) ns = fit;
   e = akz_match_run(query64, nq, train64, nt, out, scratch, ns, (cudaStream_t)stream);
+  if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
+  return AKZ_OK;
+}
+
+extern "C" AKZ_API akz_status akz_matcher_set_tensor_cores(int on)
+{
+  if (on != 0 && on != 1) return akz_report(AKZ_ERR_INVALID_ARG, "akz_matcher_set_tensor_cores: on must be 0 or 1");
+  g_akz_match_tc_on = on;
+  return AKZ_OK;
+}
+
+extern "C" AKZ_API akz_status akz_matcher_tensor_status(int *timed_out)
+{
+  if (!timed_out) return akz_report(AKZ_ERR_INVALID_ARG, "akz_matcher_tensor_status: NULL");
+  cudaError_t e = akz_match_tc_status(timed_out);
   if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
   return AKZ_OK;
 }

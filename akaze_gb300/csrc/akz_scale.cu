@@ -624,8 +624,10 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
   constexpr int RW = AKZ_FED_RW, RH = AKZ_FED_RH, NT = AKZ_FED_THREADS;
   constexpr int PS = AKZ_FED_PS, SS = AKZ_FED_SS, PH = RH + 6, SH = RH + 2;
   constexpr int NP = SS / 2;          /* column pairs of the smoothing regions */
-  constexpr int VR = 10, VG = SH / VR; /* rows per thread and row groups of the vertical pass */
-  static_assert(SH % VR == 0 && NP * VG <= NT && NP == 66 && NT == 512, "k_fed prologue geometry");
+  /* rows per thread and row groups of the vertical pass: 7 groups of 8 rows
+   * (the last one 2 rows) keep 462 of the 512 threads busy */
+  constexpr int VR = 8, VG = (SH + VR - 1) / VR;
+  static_assert(NP * VG <= NT && NP == 66 && NT == 512 && (VG - 1) * VR < SH, "k_fed prologue geometry");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int W = L.width, H = L.height;
   float *sP = sm, *sT = sm + PH * PS, *sS = sT + PH * SS;
@@ -735,21 +737,22 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
   /* 3. columns of the Gaussian: Lsmooth on rows R0 +- 1 (sS row n is y = oy - 1 + n) */
   if (tid < NP * VG) {
     const int g = tid / NP, c = 2 * (tid - g * NP);
-    const float *col = sT + (g * VR) * SS + c;
+    const float *col = sT + c;
     float2 v[VR + 4];
 #pragma unroll
-    for (int j = 0; j < VR + 4; j++) v[j] = ld2(col + j * SS);
+    for (int j = 0; j < VR + 4; j++) v[j] = ld2(col + min(g * VR + j, PH - 1) * SS); /* rows past sT: unused */
     const int x = ox - 2 + c; /* even */
     const bool w0 = x >= tx0 && x < tx1, w1 = x + 1 < tx1;
     float *lsp = p.t.planes + L.ls + x;
 #pragma unroll
     for (int j = 0; j < VR; j++) {
+      const int n = g * VR + j;
+      if (n >= SH) break;
       const float2 s04 = f2add(v[j], v[j + 4]);
       const float2 s13 = f2add(v[j + 1], v[j + 3]);
       float2 acc = akz_k2<FUSED>(k0, s04);
       acc = akz_axpy2<FUSED>(k1, s13, acc);
       acc = akz_axpy2<FUSED>(k2, v[j + 2], acc);
-      const int n = g * VR + j;
       st2(sS + n * SS + c, acc);
       const int y = oy - 1 + n;
       if (w0 && y >= ty0 && y < ty1) {

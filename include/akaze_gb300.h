@@ -248,6 +248,16 @@ AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *que
 AKZ_API akz_status akz_matcher_bfmatch_noalloc(const uint8_t *query64, int nq, const uint8_t *train64, int nt,
                                               akz_dmatch *out, void *stream);
 
+/* Pair-distance engine of the matcher calls above with at least 2^20 pairs
+ * and 128 train rows (no counterpart in the reference; process-wide):
+ * on = 1 (default) forms the distances with tcgen05 FP8 matrix multiplies,
+ * popc(q) + sum_k b_k (1 - 2 a_k) exact in FP32, on = 0 with 16 xor + popc
+ * per pair.  Both give the same matches bit for bit.
+ * akz_matcher_tensor_status reports (and clears) whether a tensor-core
+ * matcher kernel gave up waiting for its MMAs (synchronous). */
+AKZ_API akz_status akz_matcher_set_tensor_cores(int on);
+AKZ_API akz_status akz_matcher_tensor_status(int *timed_out);
+
 /* Measurement helper for the matcher's roofline (no counterpart in the
  * reference, whose README.md:22 publishes no matcher figure): the sustained
  * rate of 32-bit (xor, popc, add) triples on the current GPU, from one timed
