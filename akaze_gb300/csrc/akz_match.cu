@@ -103,11 +103,17 @@ __global__ void k_match_merge(const akz_top2 *partial, int nq, int nsplit, int4 
 cudaError_t akz_match_tc_launch(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit,
                                 int nsm, cudaStream_t s);
 cudaError_t akz_match_tc_status(int *timed_out);
+int akz_match_tc_splits(int nq, int nt, int nsm);
 
 /* Process-wide choice of the pair-distance engine for large calls: the
  * tensor-core kernels (akz_match_tc.cu, on by default) or xor + popc. */
 static int g_akz_match_tc_on = 1;
 #define AKZ_TC_MIN_PAIRS (1LL << 20) /* below ~1 M pairs one popc launch is latency-bound either way */
+
+static bool akz_match_tensor_path(int nq, int nt)
+{
+  return g_akz_match_tc_on && nt >= 128 && (long long)nq * nt >= AKZ_TC_MIN_PAIRS;
+}
 
 /* out: 2*nq records {queryIdx, trainIdx, imgIdx, distance(float bits)};
  * partial: scratch of nq*nsplit top-2 records (may be null when nsplit==1). */
@@ -115,7 +121,7 @@ cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *
 {
   if (nq <= 0) return cudaSuccess;
   if (nsplit < 1) nsplit = 1;
-  if (g_akz_match_tc_on && nt >= 128 && (long long)nq * nt >= AKZ_TC_MIN_PAIRS) {
+  if (akz_match_tensor_path(nq, nt) && (nt + nsplit - 1) / nsplit < (1 << 21)) {
     int dev = 0, nsm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -134,11 +140,13 @@ cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *
   return cudaGetLastError();
 }
 
-/* Number of train splits so that the grid holds about 4 CTAs per SM, with at
- * least 64 train rows per split: a small query set is otherwise a handful of
- * CTAs each walking the whole train set, bound by the latency of one row. */
+/* Number of train splits.  Tensor path: akz_match_tc_splits (whole waves of
+ * 256-query items).  Popc path: about 4 CTAs per SM, with at least 64 train
+ * rows per split: a small query set is otherwise a handful of CTAs each
+ * walking the whole train set, bound by the latency of one row. */
 int akz_match_splits(int nq, int nt, int nsm)
 {
+  if (akz_match_tensor_path(nq, nt)) return akz_match_tc_splits(nq, nt, nsm);
   const int qb = (nq + AKZ_MQ - 1) / AKZ_MQ;
   int ns = (4 * nsm + qb - 1) / qb;
   const int maxs = (nt + 63) / 64;

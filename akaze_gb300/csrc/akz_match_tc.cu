@@ -8,33 +8,40 @@
  *
  * For 512-bit rows q (query) and t (train), with a, b their bits:
  *   hamming(q, t) = popc(q) + sum_k b_k (1 - 2 a_k).
- * Query rows are expanded to E4M3 values 1 - 2a in {+1, -1}, train rows to
- * b in {0, +1}; one K = 512 product per pair gives the sums, exact in the FP32
- * accumulator (integers of magnitude <= 512).  The epilogue keeps the running
- * best and second best per query in train order with strict <, so equal
- * distances keep the lower train index (the cv::BFMatcher rule of the popc
- * kernel); the initial entry is {distance 512, index 0}, as there.
+ * Train bits become E4M3 values b w_k (w_k a power of two chosen by the
+ * bit's position in its byte) and query bits (1 - 2a) / w_k, so every
+ * product is 0 or +-1; one K = 512 product per pair gives the sums, exact in
+ * the FP32 accumulator (integers of magnitude <= 512).  The result is the
+ * popc kernel's: the two smallest (distance, train index) pairs, ties to
+ * the lower index (the cv::BFMatcher rule), starting from two entries
+ * {distance 512, index 0}.
  *
- * A CTA (8 warps, one per SM: it holds 256 TMEM columns) loops over work
- * items of 256 queries x one train split.  Per item the queries are expanded
+ * A CTA (one per SM: it holds 256 TMEM columns) loops over work items of
+ * 256 queries x one train split.  Eight warps expand operands and read
+ * accumulators; a ninth issues the MMAs.  Per item the queries are expanded
  * once into shared memory (two 64 KB operands of 128 rows, K-major 8-row x
  * 16-byte core matrices).  The split's train rows stream through in tiles of
- * 64: each thread loads its quarter of a row's 64 packed bytes into
- * registers one tile ahead and expands it into one of two 32 KB operand
- * buffers; one thread then issues the tile's 32 MMAs (two query halves x
- * K 512 / 32, M 128, N 64) into one of two pairs of 64-column TMEM
- * accumulators; while they run, every warp takes the previous tile's
- * accumulator of its query half (warp w: TMEM lanes of quarter w % 4, half
- * w / 4) through tcgen05.ld.  Each thread owns one query and sees every
- * train column in order.  Every mbarrier wait is bounded; a wait that runs
- * out sets the error flag, ends the loop, and the CTA frees its TMEM after
- * waiting (bounded) for its last MMAs.
+ * 64: each expanding thread loads its quarter of a row's 64 packed bytes
+ * into registers one tile ahead and expands it into one of two 32 KB
+ * operand buffers; the MMA warp then issues the tile's 32 MMAs (two query
+ * halves x K 512 / 32, M 128, N 64) into one of two pairs of 64-column TMEM
+ * accumulators; while they run, every expanding warp takes the previous
+ * tile's accumulator of its query half (warp w: TMEM lanes of quarter w % 4,
+ * half w / 4) through tcgen05.ld.  The roles hand over through mbarriers
+ * only.  Each thread owns one query and keeps its top two as packed
+ * (key, column) words, so equal distances keep the lower train index.  Every
+ * mbarrier wait is bounded; a wait that runs out sets the error flag, every
+ * role leaves its loop, and the CTA frees its TMEM after waiting (bounded)
+ * for its last MMAs.
  */
 #include <cuda_runtime.h>
 
 #include "akz_device.cuh"
 
-#define AKZ_TC_THREADS 256
+#define AKZ_TC_CWARPS 8                        /* expanding / epilogue warps; one more issues the MMAs */
+#define AKZ_TC_CTHREADS (32 * AKZ_TC_CWARPS)
+#define AKZ_TC_THREADS (AKZ_TC_CTHREADS + 32)
+#define AKZ_TC_ITEM_COST 16                    /* fixed cost of an item, in tiles (split choice) */
 #define AKZ_TC_Q 256                          /* queries per item */
 #define AKZ_TC_N 64                           /* train rows per tile */
 #define AKZ_TC_A_BYTES (128 * 512)            /* one query half: 128 rows x 512 E4M3 values */
@@ -78,19 +85,46 @@ __device__ __forceinline__ bool tc_mbar_wait(uint32_t mb, uint32_t parity)
   return done != 0;
 }
 
-/* 16 row bits -> 16 E4M3 bytes: train 0 / +1 (0x38), query +1 / -1 (0x38 / 0xB8) */
-__device__ __forceinline__ uint4 tc_expand16(uint32_t bits, bool query)
+/* The K order and the operand values.  Source byte i of a row (bits
+ * b0..b7) gives K positions 8 i .. 8 i + 7 = bits 3, 4, 5, 6, 7, 0, 1, 2.
+ * A train byte there is the source byte masked to that one bit, moved (for
+ * bits 7, 0, 1, 2, by a nibble swap) to bit position 3, 4, 5 or 6: E4M3
+ * 0x08, 0x10, 0x20, 0x40 = 2^-6, 2^-5, 2^-3, 2^1 when the bit is set, else
+ * 0.  The query byte at the same K position is (1 - 2a) / w with w that
+ * weight: 0x68, 0x60, 0x50, 0x30 = 64, 32, 8, 0.5, with the sign bit when
+ * a = 1.  Every product is 0 or +-1 exactly.  The masked word is one
+ * byte-permute and one AND per 4 K bytes. */
+#define AKZ_TC_WMASK 0x40201008u /* bytes 0..3: bit 3, 4, 5, 6 */
+#define AKZ_TC_QMAG 0x30506068u  /* bytes 0..3: 64, 32, 8, 0.5 */
+
+__device__ __forceinline__ uint32_t tc_nibswap(uint32_t w)
 {
-  uint32_t w[4];
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const uint32_t ones = (((bits >> (4 * i)) & 15u) * 0x00204081u) & 0x01010101u; /* byte j = bit 4i + j */
-    w[i] = query ? (0x38383838u | (ones << 7)) : ones * 0x38u;
-  }
-  return make_uint4(w[0], w[1], w[2], w[3]);
+  return ((w >> 4) & 0x0f0f0f0fu) | ((w << 4) & 0xf0f0f0f0u);
 }
 
-/* Writes nw consecutive 32-bit words of a packed row (starting at word w0)
+/* source word w (bytes 0..3) -> the 32 K bytes of its 4 bytes, as two
+ * 16-byte chunks */
+__device__ __forceinline__ void tc_expand_word(uint32_t w, bool query, uint4 &c0, uint4 &c1)
+{
+  const uint32_t y = tc_nibswap(w);
+  uint32_t o[8];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const uint32_t a = __byte_perm(w, 0, 0x1111u * (uint32_t)i) & AKZ_TC_WMASK;
+    const uint32_t b = __byte_perm(y, 0, 0x1111u * (uint32_t)i) & AKZ_TC_WMASK;
+    if (query) { /* a set bit (<= 0x40) plus 0x7f reaches bit 7, without carry into the next byte */
+      o[2 * i] = AKZ_TC_QMAG | ((a + 0x7f7f7f7fu) & 0x80808080u);
+      o[2 * i + 1] = AKZ_TC_QMAG | ((b + 0x7f7f7f7fu) & 0x80808080u);
+    } else {
+      o[2 * i] = a;
+      o[2 * i + 1] = b;
+    }
+  }
+  c0 = make_uint4(o[0], o[1], o[2], o[3]);
+  c1 = make_uint4(o[4], o[5], o[6], o[7]);
+}
+
+/* Writes NW consecutive 32-bit words of a packed row (starting at word w0)
  * into an operand of `rows` rows: row r, K byte k at core matrix (r / 8,
  * k / 16), K-adjacent core matrices rows * 16 bytes apart (LBO), row-adjacent
  * 128 (SBO).  The 32 lanes of a warp take 32 consecutive rows: each 16-byte
@@ -102,12 +136,96 @@ __device__ __forceinline__ void tc_expand_words(const uint32_t (&w)[NW], int r, 
   const uint32_t ro = (uint32_t)((r >> 3) * 128 + (r & 7) * 16), kstride = (uint32_t)rows * 16;
 #pragma unroll
   for (int m = 0; m < NW; m++) {
-    const uint32_t c = (uint32_t)(2 * (w0 + m)); /* core column of the word's first 16 bits */
-    *reinterpret_cast<uint4 *>(op + c * kstride + ro) = tc_expand16(w[m] & 0xffffu, query);
-    *reinterpret_cast<uint4 *>(op + (c + 1) * kstride + ro) = tc_expand16(w[m] >> 16, query);
+    const uint32_t c = (uint32_t)(2 * (w0 + m)); /* core column of the word's first 16 K bytes */
+    uint4 c0, c1;
+    tc_expand_word(w[m], query, c0, c1);
+    *reinterpret_cast<uint4 *>(op + c * kstride + ro) = c0;
+    *reinterpret_cast<uint4 *>(op + (c + 1) * kstride + ro) = c1;
   }
 }
 
+/* Waits (bounded) for phase `parity` of the mbarrier at mb; gives up early
+ * when another thread of the CTA has flagged a failure, and flags one when
+ * its own limit runs out. */
+__device__ __forceinline__ bool tc_wait(uint32_t mb, uint32_t parity, volatile int *bad)
+{
+  for (int it = 0; it < AKZ_TC_SPIN; it++) {
+    uint32_t done;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done)
+                 : "r"(mb), "r"(parity)
+                 : "memory");
+    if (done) return true;
+    if (*bad) return false;
+  }
+  *bad = 1;
+  return false;
+}
+
+__device__ __forceinline__ void tc_arrive(uint32_t mb)
+{
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(mb) : "memory");
+}
+
+/* Running top two of one query as packed keys: (hamming - popc(q) + 512)
+ * in bits 21..31, the column within the split in bits 0..20, so that the
+ * unsigned order is the (distance, train index) order of the popc kernel
+ * and min / max keep the lexicographic top two in any processing order.
+ * kf is the float key of the second entry: a column whose value is not
+ * below kf cannot enter. */
+struct tc_top2 {
+  uint32_t ub, us;
+  float kf;
+};
+
+/* one 32-column half of a tile's accumulator row: v[cc] = key of column
+ * col0 + cc; PART: columns cc >= lim lie past the split */
+template <bool PART>
+__device__ __forceinline__ void tc_scan32(const uint32_t (&r)[32], uint32_t col0, int lim, tc_top2 &st)
+{
+  /* (0x4B400000 + key) << 21 + BIAS = (key + 512) << 21 (mod 2^32) */
+  constexpr uint32_t BIAS = (512u - 0x4B400000u) << 21;
+  float m8[4];
+#pragma unroll
+  for (int g = 0; g < 4; g++) {
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) v[e] = __uint_as_float(r[8 * g + e]);
+    m8[g] = fminf(fminf(fminf(v[0], v[1]), fminf(v[2], v[3])), fminf(fminf(v[4], v[5]), fminf(v[6], v[7])));
+  }
+  if (fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3])) < st.kf) {
+    const uint32_t cb = col0 + BIAS;
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+      if (m8[g] < st.kf) {
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+          const int cc = 8 * g + e;
+          /* the key is an integer of magnitude <= 512: adding 1.5 * 2^23 puts it in the low mantissa bits */
+          const uint32_t x = __float_as_uint(__uint_as_float(r[cc]) + 12582912.0f);
+          uint32_t u = (x << 21) + cb + (uint32_t)cc;
+          if (PART && cc >= lim) u = 0xffffffffu;
+          const uint32_t hi = max(st.ub, u);
+          st.ub = min(st.ub, u);
+          st.us = min(st.us, hi);
+        }
+        st.kf = (float)((int)(st.us >> 21) - 512);
+      }
+    }
+  }
+}
+
+/* Warp roles: warps 0..7 expand the operands and run the epilogue (warp w
+ * reads TMEM lane quarter w % 4 of query half w / 4); warp 8 (one lane)
+ * issues the MMAs.  Hand-offs, per tile batch c over the CTA's lifetime
+ * (barrier index c & 1, phase (c >> 1) & 1):
+ *   full:    the 256 expanding threads arrive once the train tile (and, for
+ *            an item's first tile, the queries) is in shared memory;
+ *   done:    the MMA batch's commit;
+ *   accfree: the 256 threads arrive once they have read the batch's
+ *            accumulators, which batch c + 2 overwrites.
+ * A thread rewrites train buffer c & 1 (and the queries, at an item's
+ * start) only after it has seen batch c - 2 (every earlier batch) done. */
 __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__restrict__ q, const uint4 *__restrict__ t,
                                                              int nq, int nt, int split_len, int nsplit,
                                                              akz_tc_top2 *partial, int4 *out)
@@ -115,20 +233,23 @@ __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__r
   extern __shared__ __align__(1024) unsigned char tcsm[];
   unsigned char *base = tcsm + ((1024u - ((uint32_t)__cvta_generic_to_shared(tcsm) & 1023u)) & 1023u);
   unsigned char *sA = base, *sB = base + 2 * AKZ_TC_A_BYTES; /* sA: halves 0 and 1; sB: tiles 0 and 1 */
-  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ __align__(8) unsigned long long mbar[6];          /* full[2], done[2], accfree[2] */
   __shared__ uint32_t tbase;
-  __shared__ int sBad;
+  __shared__ volatile int sBad;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, qh = warp >> 2; /* TMEM lane quarter, query half */
 
   if (warp == 0) {
     const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tbase);
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(dst));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  const uint32_t mfull = (uint32_t)__cvta_generic_to_shared(&mbar[0]), mdone = mfull + 16u, mfree = mfull + 32u;
   if (tid == 0) {
-    for (int b = 0; b < 2; b++)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&mbar[b])));
+    for (int b = 0; b < 2; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mfull + 8u * b), "r"(AKZ_TC_CTHREADS));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mdone + 8u * b));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mfree + 8u * b), "r"(AKZ_TC_CTHREADS));
+    }
     asm volatile("fence.mbarrier_init.release.cluster;");
     sBad = 0;
   }
@@ -136,189 +257,197 @@ __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__r
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tbase;
-  constexpr uint32_t idesc = tc_idesc(128, AKZ_TC_N);
   const uint32_t aaddr = (uint32_t)__cvta_generic_to_shared(sA), baddr = (uint32_t)__cvta_generic_to_shared(sB);
-  const uint32_t mb0 = (uint32_t)__cvta_generic_to_shared(&mbar[0]);
-  /* MMA batches (one per tile) committed by thread 0 / seen complete, over
-   * the CTA's lifetime: batch c uses mbar[c & 1], phase (c >> 1) & 1 */
-  uint32_t issued = 0, committed = 0, retired = 0;
-  bool ok = true;
-
   const int nqb = (nq + AKZ_TC_Q - 1) / AKZ_TC_Q;
   const int nitems = nqb * nsplit;
-  /* expansion roles: train tiles, row er = tid % 64 and words 4 eh .. 4 eh + 3 */
-  const int er = tid & 63, eh = tid >> 6;
-  for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-    const int qb = item % nqb, sp = item / nqb;
-    const int j0 = sp * split_len, j1 = min(nt, j0 + split_len);
-    const int ntile = j1 > j0 ? (j1 - j0 + AKZ_TC_N - 1) / AKZ_TC_N : 0;
-    const int myq = qb * AKZ_TC_Q + qh * 128 + quarter * 32 + lane; /* this thread's query */
+  uint32_t committed = 0; /* MMA lane: batches committed */
 
-    auto load_tile = [&](int k, uint4 &v) { /* row er of tile k, words 4 eh .. 4 eh + 3; zeros past the split */
-      const int j = j0 + k * AKZ_TC_N + er;
-      v = j < j1 ? __ldg(t + (long long)j * 4 + eh) : make_uint4(0, 0, 0, 0);
-    };
-    uint4 cur = make_uint4(0, 0, 0, 0), nxt = cur;
-    if (ntile > 0) load_tile(0, cur);
-    { /* the 256 queries: thread i expands rows i % 128 of both halves, words 8 (i / 128) .. + 7 */
-      const int r = tid & 127, h = tid >> 7;
+  if (warp == AKZ_TC_CWARPS) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc_idesc(128, AKZ_TC_N);
+      uint32_t c = 0;
+      for (int item = blockIdx.x; item < nitems && !sBad; item += gridDim.x) {
+        const int sp = item / nqb;
+        const int j0 = sp * split_len, j1 = min(nt, j0 + split_len);
+        const int ntile = j1 > j0 ? (j1 - j0 + AKZ_TC_N - 1) / AKZ_TC_N : 0;
+        for (int k = 0; k < ntile; k++, c++) {
+          const uint32_t b = c & 1u;
+          if (!tc_wait(mfull + 8u * b, (c >> 1) & 1u, &sBad)) break;
+          if (c >= 2 && !tc_wait(mfree + 8u * b, ((c >> 1) - 1u) & 1u, &sBad)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t bb = baddr + b * (uint32_t)AKZ_TC_B_BYTES;
 #pragma unroll
-      for (int half = 0; half < 2; half++) {
-        const int qi = qb * AKZ_TC_Q + half * 128 + r;
-        uint4 a = make_uint4(0, 0, 0, 0), b = a;
-        if (qi < nq) {
-          a = __ldg(q + (long long)qi * 4 + 2 * h);
-          b = __ldg(q + (long long)qi * 4 + 2 * h + 1);
-        }
-        const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-        tc_expand_words<8>(w, r, 8 * h, 128, sA + half * AKZ_TC_A_BYTES, true);
-      }
-    }
-    int pq = 0;
-    if (myq < nq) {
+          for (int h = 0; h < 2; h++) {
+            const uint32_t d = tmem + (b * 2u + (uint32_t)h) * AKZ_TC_N;
+            const uint32_t ah = aaddr + (uint32_t)(h * AKZ_TC_A_BYTES);
 #pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const uint4 v = __ldg(q + (long long)myq * 4 + c);
-        pq += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
-      }
-    }
-    float bk = (float)(512 - pq), sk = bk; /* keys: hamming - popc(q) */
-    int bi = 0, si = 0;
-
-    auto epilogue = [&](uint32_t c, int k) { /* batch c = tile k's accumulators */
-      const int jt = j0 + k * AKZ_TC_N;
-      const int lim0 = j1 - jt;
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        uint32_t r[32];
-        const uint32_t taddr =
-            tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((((c & 1u) * 2u + (uint32_t)qh) * AKZ_TC_N) + 32 * h);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
-              "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-              "=r"(r[30]), "=r"(r[31])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
-        const int lim = lim0 - 32 * h; /* columns past the split are not candidates */
-#pragma unroll
-        for (int cc = 0; cc < 32; cc++) {
-          const float v = __uint_as_float(r[cc]);
-          if (cc < lim && v < sk) {
-            const int j = jt + 32 * h + cc;
-            if (v < bk) {
-              sk = bk;
-              si = bi;
-              bk = v;
-              bi = j;
-            } else {
-              sk = v;
-              si = j;
+            for (int s = 0; s < 16; s++) { /* K step s: bytes 32 s .. 32 s + 31, two core columns */
+              const uint64_t ad = tc_smem_desc(ah + (uint32_t)(s * 4096), 2048, 128);
+              const uint64_t bd = tc_smem_desc(bb + (uint32_t)(s * 2048), 1024, 128);
+              const uint32_t acc = s > 0 ? 1u : 0u;
+              asm volatile(
+                  "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                  "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+                  "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
             }
           }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mdone +
+                                                                                                            8u * b));
+          committed = c + 1;
         }
       }
-    };
+    }
+    __syncwarp();
+  } else {
+    const int quarter = warp & 3, qh = warp >> 2; /* TMEM lane quarter, query half */
+    /* expansion roles: train tiles, row er = tid % 64 and words 4 eh .. 4 eh + 3 */
+    const int er = tid & 63, eh = tid >> 6;
+    uint32_t c = 0;
+    for (int item = blockIdx.x; item < nitems && !sBad; item += gridDim.x) {
+      const int qb = item % nqb, sp = item / nqb;
+      const int j0 = sp * split_len, j1 = min(nt, j0 + split_len);
+      const int ntile = j1 > j0 ? (j1 - j0 + AKZ_TC_N - 1) / AKZ_TC_N : 0;
+      const int myq = qb * AKZ_TC_Q + qh * 128 + quarter * 32 + lane; /* this thread's query */
 
-    for (int k = 0; k < ntile; k++) {
-      if (k + 1 < ntile) load_tile(k + 1, nxt); /* in flight while tile k is expanded */
-      /* operand buffer k & 1: its last reader, tile k - 2's MMAs, retired before tile k - 1's barrier */
-      {
-        const uint32_t w[4] = {cur.x, cur.y, cur.z, cur.w};
-        tc_expand_words<4>(w, er, 4 * eh, AKZ_TC_N, sB + (k & 1) * AKZ_TC_B_BYTES, false);
+      auto load_tile = [&](int k, uint4 &v) { /* row er of tile k, words 4 eh .. 4 eh + 3; zeros past the split */
+        const int j = j0 + k * AKZ_TC_N + er;
+        v = j < j1 ? __ldg(t + (long long)j * 4 + eh) : make_uint4(0, 0, 0, 0);
+      };
+      uint4 cur = make_uint4(0, 0, 0, 0), nxt = cur;
+      if (ntile > 0) {
+        load_tile(0, cur);
+        /* the 256 queries: thread i expands rows i % 128 of both halves, words 8 (i / 128) .. + 7 */
+        const int r = tid & 127, h = tid >> 7;
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+          const int qi = qb * AKZ_TC_Q + half * 128 + r;
+          uint4 a = make_uint4(0, 0, 0, 0), b = a;
+          if (qi < nq) {
+            a = __ldg(q + (long long)qi * 4 + 2 * h);
+            b = __ldg(q + (long long)qi * 4 + 2 * h + 1);
+          }
+          const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+          tc_expand_words<8>(w, r, 8 * h, 128, sA + half * AKZ_TC_A_BYTES, true);
+        }
       }
-      cur = nxt;
-      asm volatile("fence.proxy.async.shared::cta;");
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncthreads();
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t c = issued++;
-      if (tid == 0) {
-        const uint32_t bb = baddr + (uint32_t)((k & 1) * AKZ_TC_B_BYTES);
+      int pq = 0;
+      if (myq < nq) {
+#pragma unroll
+        for (int w = 0; w < 4; w++) {
+          const uint4 v = __ldg(q + (long long)myq * 4 + w);
+          pq += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+        }
+      }
+      tc_top2 st; /* both entries start as {distance 512, index 0} */
+      st.ub = st.us = (uint32_t)(1024 - pq) << 21;
+      st.kf = (float)(512 - pq);
+
+      auto epilogue = [&](uint32_t cb, int k) -> bool { /* batch cb = tile k of this item */
+        /* tcgen05.ld is warp-collective: the warp goes on only if every lane saw the batch done */
+        if (!__all_sync(0xffffffffu, tc_wait(mdone + 8u * (cb & 1u), (cb >> 1) & 1u, &sBad))) {
+          sBad = 1;
+          return false;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const int lim0 = j1 - (j0 + k * AKZ_TC_N);
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-          const uint32_t d = tmem + (uint32_t)(((c & 1u) * 2u + (uint32_t)h) * AKZ_TC_N);
-          const uint32_t ah = aaddr + (uint32_t)(h * AKZ_TC_A_BYTES);
-#pragma unroll
-          for (int s = 0; s < 16; s++) { /* K step s: bytes 32 s .. 32 s + 31, two core columns */
-            const uint64_t ad = tc_smem_desc(ah + (uint32_t)(s * 4096), 2048, 128);
-            const uint64_t bd = tc_smem_desc(bb + (uint32_t)(s * 2048), 1024, 128);
-            const uint32_t acc = s > 0 ? 1u : 0u;
-            asm volatile(
-                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}" ::"r"(d),
-                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-          }
+          uint32_t r[32];
+          const uint32_t taddr =
+              tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((((cb & 1u) * 2u + (uint32_t)qh) * AKZ_TC_N) + 32 * h);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+              "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+              : "r"(taddr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+          const int lim = lim0 - 32 * h;
+          const uint32_t col0 = (uint32_t)(k * AKZ_TC_N + 32 * h);
+          if (lim >= 32)
+            tc_scan32<false>(r, col0, lim, st);
+          else
+            tc_scan32<true>(r, col0, lim, st);
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb0 + 8u * (c & 1u)));
-        committed = c + 1;
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        tc_arrive(mfree + 8u * (cb & 1u));
+        return true;
+      };
+
+      bool ok = true;
+      for (int k = 0; k < ntile; k++, c++) {
+        if (k + 1 < ntile) load_tile(k + 1, nxt); /* in flight while tile k is expanded */
+        {
+          const uint32_t w[4] = {cur.x, cur.y, cur.z, cur.w};
+          tc_expand_words<4>(w, er, 4 * eh, AKZ_TC_N, sB + (c & 1u) * AKZ_TC_B_BYTES, false);
+        }
+        cur = nxt;
+        asm volatile("fence.proxy.async.shared::cta;");
+        tc_arrive(mfull + 8u * (c & 1u));
+        if (k >= 1 && !(ok = epilogue(c - 1, k - 1))) break; /* tile k - 1 while tile k's MMAs run */
       }
-      if (k >= 1) { /* tile k - 1's accumulators while tile k's MMAs run */
-        const uint32_t cp = c - 1;
-        if (!tc_mbar_wait(mb0 + 8u * (cp & 1u), (cp >> 1) & 1u)) {
-          sBad = 1;
+      if (!ok) break;
+      if (ntile > 0 && !epilogue(c - 1, ntile - 1)) break;
+      if (myq < nq) {
+        const int bd = pq + (int)(st.ub >> 21) - 512, sd = pq + (int)(st.us >> 21) - 512;
+        const int bi = j0 + (int)(st.ub & 0x1fffffu), si = j0 + (int)(st.us & 0x1fffffu);
+        if (nsplit == 1) {
+          out[2 * myq] = make_int4(myq, bi, 0, __float_as_int((float)bd));
+          out[2 * myq + 1] = make_int4(myq, si, 0, __float_as_int((float)sd));
         } else {
-          retired = cp + 1;
-          asm volatile("tcgen05.fence::after_thread_sync;");
-          epilogue(cp, k - 1);
+          partial[(long long)myq * nsplit + sp] = akz_tc_top2{bd, bi, sd, si};
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncthreads();
-      if (sBad) {
-        ok = false;
-        break;
-      }
-    }
-    if (!ok) break;
-    if (ntile > 0) { /* the last tile */
-      const uint32_t cp = issued - 1;
-      if (!tc_mbar_wait(mb0 + 8u * (cp & 1u), (cp >> 1) & 1u)) {
-        sBad = 1;
-      } else {
-        retired = cp + 1;
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        epilogue(cp, ntile - 1);
-      }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads(); /* sA and the accumulators are reused by the next item */
-    if (sBad) {
-      ok = false;
-      break;
-    }
-    if (myq < nq) {
-      const int bd = pq + (int)bk, sd = pq + (int)sk;
-      if (nsplit == 1) {
-        out[2 * myq] = make_int4(myq, bi, 0, __float_as_int((float)bd));
-        out[2 * myq + 1] = make_int4(myq, si, 0, __float_as_int((float)sd));
-      } else {
-        partial[(long long)myq * nsplit + sp] = akz_tc_top2{bd, bi, sd, si};
-      }
     }
   }
-  if (!ok && tid == 0) {
-    atomicExch(&g_akz_tc_err, 1);
-    if (retired < committed) { /* batches complete in order: wait (bounded) for the last one */
-      const uint32_t cp = committed - 1;
-      tc_mbar_wait(mb0 + 8u * (cp & 1u), (cp >> 1) & 1u);
-    }
+  if (warp == AKZ_TC_CWARPS && lane == 0 && committed > 0) {
+    /* every batch's MMAs finished before the CTA frees TMEM and exits; on
+     * the normal path the epilogue has already seen the last one */
+    const uint32_t cp = committed - 1;
+    tc_mbar_wait(mdone + 8u * (cp & 1u), (cp >> 1) & 1u);
   }
+  if (tid == 0 && sBad) atomicExch(&g_akz_tc_err, 1);
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
 }
 
+/* Train splits for the tensor path: items of 256 queries x one split are
+ * spread over one CTA per SM, so the cost is waves x (tiles per split + a
+ * fixed cost per item: the query expansion, and the first columns of a split,
+ * where the top two change often).  A split's columns must fit 21 bits. */
+int akz_match_tc_splits(int nq, int nt, int nsm)
+{
+  const long long nqb = (nq + AKZ_TC_Q - 1) / AKZ_TC_Q;
+  const int smax = (1 << 21) - 1;
+  const int min_s = nt > smax ? (nt + smax - 1) / smax : 1;
+  int best = min_s;
+  long long bestc = -1;
+  for (int ns = min_s; ns <= 64; ns++) {
+    const long long len = ((long long)nt + ns - 1) / ns;
+    if (ns > min_s && len < 4 * AKZ_TC_N) break;
+    const long long waves = (nqb * ns + nsm - 1) / nsm;
+    const long long cost = waves * ((len + AKZ_TC_N - 1) / AKZ_TC_N + AKZ_TC_ITEM_COST);
+    if (bestc < 0 || cost < bestc) {
+      bestc = cost;
+      best = ns;
+    }
+  }
+  return best;
+}
+
 /* Launches k_match_tc over nq queries and nt >= 1 train rows split in nsplit
- * parts, at most one CTA per SM; with nsplit > 1 the caller merges partial
- * (nq x nsplit records in the popc kernel's akz_top2 layout). */
+ * parts (split length < 2^21), at most one CTA per SM; with nsplit > 1 the
+ * caller merges partial (nq x nsplit records in the popc kernel's akz_top2
+ * layout). */
 cudaError_t akz_match_tc_launch(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit,
                                 int nsm, cudaStream_t s)
 {
   const int split_len = (nt + nsplit - 1) / nsplit;
+  if (split_len >= (1 << 21)) return cudaErrorInvalidValue;
   const int nitems = ((nq + AKZ_TC_Q - 1) / AKZ_TC_Q) * nsplit;
   const int grid = nitems < nsm ? nitems : nsm;
   cudaError_t e = cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AKZ_TC_SMEM);
