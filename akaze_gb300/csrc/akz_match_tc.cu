@@ -16,19 +16,21 @@
  * the lower index (the cv::BFMatcher rule), starting from two entries
  * {distance 512, index 0}.
  *
- * A CTA (one per SM: it holds 256 TMEM columns) loops over work items of
+ * A CTA (one per SM: it holds all 512 TMEM columns) loops over work items of
  * 256 queries x one train split.  Eight warps expand operands and read
- * accumulators; a ninth issues the MMAs.  Per item the queries are expanded
- * once into shared memory (two 64 KB operands of 128 rows, K-major 8-row x
- * 16-byte core matrices).  The split's train rows stream through in tiles of
- * 64: each expanding thread loads its quarter of a row's 64 packed bytes
+ * accumulators; a ninth issues the MMAs.  Per item each thread expands its
+ * query row once into tensor memory (the MMAs' A operand, 2 x 128 rows x
+ * 512 bytes).  The split's train rows stream through shared memory in tiles
+ * of 64: each expanding thread loads its quarter of a row's 64 packed bytes
  * into registers one tile ahead and expands it into one of two 32 KB
- * operand buffers; the MMA warp then issues the tile's 32 MMAs (two query
- * halves x K 512 / 32, M 128, N 64) into one of two pairs of 64-column TMEM
- * accumulators; while they run, every expanding warp takes the previous
- * tile's accumulator of its query half (warp w: TMEM lanes of quarter w % 4,
- * half w / 4) through tcgen05.ld.  The roles hand over through mbarriers
- * only.  Each thread owns one query and keeps its top two as packed
+ * operand buffers (K-major 8-row x 16-byte core matrices); the MMA warp then
+ * issues the tile's 32 MMAs (two query halves x K 512 / 32, M 128, N 64)
+ * into one of two pairs of 64-column TMEM accumulators; while they run,
+ * every expanding warp takes the previous tile's accumulator of its query
+ * half (warp w: TMEM lanes of quarter w % 4, half w / 4) through
+ * tcgen05.ld.  Shared memory carries only the train operand: the query
+ * operand, read by every MMA, stays in TMEM.  The roles hand over through
+ * mbarriers only.  Each thread owns one query and keeps its top two as packed
  * (key, column) words, so equal distances keep the lower train index.  Every
  * mbarrier wait is bounded; a wait that runs out sets the error flag, every
  * role leaves its loop, and the CTA frees its TMEM after waiting (bounded)
@@ -44,9 +46,14 @@
 #define AKZ_TC_ITEM_COST 16                    /* fixed cost of an item, in tiles (split choice) */
 #define AKZ_TC_Q 256                          /* queries per item */
 #define AKZ_TC_N 64                           /* train rows per tile */
-#define AKZ_TC_A_BYTES (128 * 512)            /* one query half: 128 rows x 512 E4M3 values */
 #define AKZ_TC_B_BYTES (AKZ_TC_N * 512)       /* one train tile */
-#define AKZ_TC_SMEM (2 * AKZ_TC_A_BYTES + 2 * AKZ_TC_B_BYTES + 1024)
+#define AKZ_TC_STAGES 2                        /* train buffers = accumulator sets = barrier sets */
+#define AKZ_TC_LAG (AKZ_TC_STAGES - 1)          /* tiles between a hand-over and its epilogue */
+#define AKZ_TC_SMEM (AKZ_TC_STAGES * AKZ_TC_B_BYTES + 1024)
+/* requested at launch: more than half an SM's shared memory, so that one CTA
+ * per SM holds the whole TMEM (a second CTA's allocation would wait) */
+#define AKZ_TC_SMEM_LAUNCH (AKZ_TC_SMEM > 120 * 1024 ? AKZ_TC_SMEM : 120 * 1024)
+#define AKZ_TC_ACOL 256                        /* TMEM column of the query operand (half h: + 128 h) */
 #define AKZ_TC_SPIN (1 << 24)
 
 /* set when an MMA wait of k_match_tc ran out (read and cleared by
@@ -167,6 +174,32 @@ __device__ __forceinline__ void tc_arrive(uint32_t mb)
   asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(mb) : "memory");
 }
 
+/* 32 consecutive accumulator columns of this warp's 32 TMEM lanes (no wait) */
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&r)[32])
+{
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
+/* 32 consecutive TMEM columns of this warp's 32 lanes (no wait) */
+__device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&r)[32])
+{
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]),
+      "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]),
+      "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+
 /* Running top two of one query as packed keys: (hamming - popc(q) + 512)
  * in bits 21..31, the column within the split in bits 0..20, so that the
  * unsigned order is the (distance, train index) order of the popc kernel
@@ -216,39 +249,45 @@ __device__ __forceinline__ void tc_scan32(const uint32_t (&r)[32], uint32_t col0
 }
 
 /* Warp roles: warps 0..7 expand the operands and run the epilogue (warp w
- * reads TMEM lane quarter w % 4 of query half w / 4); warp 8 (one lane)
- * issues the MMAs.  Hand-offs, per tile batch c over the CTA's lifetime
- * (barrier index c & 1, phase (c >> 1) & 1):
- *   full:    the 256 expanding threads arrive once the train tile (and, for
- *            an item's first tile, the queries) is in shared memory;
+ * owns TMEM lane quarter w % 4 of query half w / 4: its query rows of the
+ * operand and its accumulator rows); warp 8 (one lane) issues the MMAs.
+ * TMEM: accumulator sets at columns 0..255 (set s, half h: 128 s + 64 h),
+ * the expanded queries at 256..511 (half h: 256 + 128 h, 4 K bytes per
+ * column).  Tile batch c over the CTA's lifetime uses stage c % 2: train
+ * buffer, accumulator set and the barriers, at phase (c / 2) & 1:
+ *   full:    each expanding warp arrives once its lanes have written the
+ *            train tile (and, for an item's first tile, their query rows);
  *   done:    the MMA batch's commit;
- *   accfree: the 256 threads arrive once they have read the batch's
- *            accumulators, which batch c + 2 overwrites.
- * A thread rewrites train buffer c & 1 (and the queries, at an item's
- * start) only after it has seen batch c - 2 (every earlier batch) done. */
+ *   accfree: each expanding warp arrives once its lanes have read the
+ *            batch's accumulators, which batch c + 2 overwrites.
+ * The expanding warps read batch c - 1's accumulators after handing over
+ * tile c.  A thread rewrites train buffer c % 2 only after it has seen batch
+ * c - 2 done, and its query row (at an item's start) after every batch of
+ * the previous item. */
 __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__restrict__ q, const uint4 *__restrict__ t,
                                                              int nq, int nt, int split_len, int nsplit,
                                                              akz_tc_top2 *partial, int4 *out)
 {
   extern __shared__ __align__(1024) unsigned char tcsm[];
   unsigned char *base = tcsm + ((1024u - ((uint32_t)__cvta_generic_to_shared(tcsm) & 1023u)) & 1023u);
-  unsigned char *sA = base, *sB = base + 2 * AKZ_TC_A_BYTES; /* sA: halves 0 and 1; sB: tiles 0 and 1 */
-  __shared__ __align__(8) unsigned long long mbar[6];          /* full[2], done[2], accfree[2] */
+  unsigned char *sB = base; /* the train stages */
+  __shared__ __align__(8) unsigned long long mbar[3 * AKZ_TC_STAGES]; /* full, done, accfree */
   __shared__ uint32_t tbase;
   __shared__ volatile int sBad;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (warp == 0) {
     const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tbase);
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(dst));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(dst));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  const uint32_t mfull = (uint32_t)__cvta_generic_to_shared(&mbar[0]), mdone = mfull + 16u, mfree = mfull + 32u;
+  const uint32_t mfull = (uint32_t)__cvta_generic_to_shared(&mbar[0]), mdone = mfull + 8u * AKZ_TC_STAGES,
+                 mfree = mdone + 8u * AKZ_TC_STAGES;
   if (tid == 0) {
-    for (int b = 0; b < 2; b++) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mfull + 8u * b), "r"(AKZ_TC_CTHREADS));
+    for (int b = 0; b < AKZ_TC_STAGES; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mfull + 8u * b), "r"(AKZ_TC_CWARPS));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mdone + 8u * b));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mfree + 8u * b), "r"(AKZ_TC_CTHREADS));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mfree + 8u * b), "r"(AKZ_TC_CWARPS));
     }
     asm volatile("fence.mbarrier_init.release.cluster;");
     sBad = 0;
@@ -257,47 +296,52 @@ __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__r
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tbase;
-  const uint32_t aaddr = (uint32_t)__cvta_generic_to_shared(sA), baddr = (uint32_t)__cvta_generic_to_shared(sB);
+  const uint32_t baddr = (uint32_t)__cvta_generic_to_shared(sB);
   const int nqb = (nq + AKZ_TC_Q - 1) / AKZ_TC_Q;
   const int nitems = nqb * nsplit;
   uint32_t committed = 0; /* MMA lane: batches committed */
 
   if (warp == AKZ_TC_CWARPS) {
-    if (lane == 0) {
-      constexpr uint32_t idesc = tc_idesc(128, AKZ_TC_N);
-      uint32_t c = 0;
-      for (int item = blockIdx.x; item < nitems && !sBad; item += gridDim.x) {
-        const int sp = item / nqb;
-        const int j0 = sp * split_len, j1 = min(nt, j0 + split_len);
-        const int ntile = j1 > j0 ? (j1 - j0 + AKZ_TC_N - 1) / AKZ_TC_N : 0;
-        for (int k = 0; k < ntile; k++, c++) {
-          const uint32_t b = c & 1u;
-          if (!tc_wait(mfull + 8u * b, (c >> 1) & 1u, &sBad)) break;
-          if (c >= 2 && !tc_wait(mfree + 8u * b, ((c >> 1) - 1u) & 1u, &sBad)) break;
-          asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t bb = baddr + b * (uint32_t)AKZ_TC_B_BYTES;
-#pragma unroll
-          for (int h = 0; h < 2; h++) {
-            const uint32_t d = tmem + (b * 2u + (uint32_t)h) * AKZ_TC_N;
-            const uint32_t ah = aaddr + (uint32_t)(h * AKZ_TC_A_BYTES);
-#pragma unroll
-            for (int s = 0; s < 16; s++) { /* K step s: bytes 32 s .. 32 s + 31, two core columns */
-              const uint64_t ad = tc_smem_desc(ah + (uint32_t)(s * 4096), 2048, 128);
-              const uint64_t bd = tc_smem_desc(bb + (uint32_t)(s * 2048), 1024, 128);
-              const uint32_t acc = s > 0 ? 1u : 0u;
-              asm volatile(
-                  "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                  "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}" ::"r"(d),
-                  "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-            }
-          }
-          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mdone +
-                                                                                                            8u * b));
-          committed = c + 1;
+    /* the whole warp runs the loop, so that the operands are warp-uniform;
+     * elect.sync inside each asm picks the one lane that issues (a lone
+     * lane's issue costs about twice as many cycles per MMA) */
+    constexpr uint32_t idesc = tc_idesc(128, AKZ_TC_N);
+    uint32_t c = 0;
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      const int sp = item / nqb;
+      const int j0 = sp * split_len, j1 = min(nt, j0 + split_len);
+      const int ntile = j1 > j0 ? (j1 - j0 + AKZ_TC_N - 1) / AKZ_TC_N : 0;
+      for (int k = 0; k < ntile; k++, c++) {
+        const uint32_t st = c % AKZ_TC_STAGES, ph = (c / AKZ_TC_STAGES) & 1u;
+        ok = __all_sync(0xffffffffu, tc_wait(mfull + 8u * st, ph, &sBad));
+        if (ok && c >= AKZ_TC_STAGES) ok = __all_sync(0xffffffffu, tc_wait(mfree + 8u * st, ph ^ 1u, &sBad));
+        if (!ok) {
+          sBad = 1;
+          break;
         }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t bb = baddr + st * (uint32_t)AKZ_TC_B_BYTES;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const uint32_t d = tmem + (st * 2u + (uint32_t)h) * AKZ_TC_N;
+          const uint32_t ah = tmem + (uint32_t)(AKZ_TC_ACOL + 128 * h);
+#pragma unroll
+          for (int s = 0; s < 16; s++) { /* K step s: bytes 32 s .. 32 s + 31: A columns 8 s .. 8 s + 7, B two core columns */
+            const uint64_t bd = tc_smem_desc(bb + (uint32_t)(s * 2048), 1024, 128);
+            const uint32_t acc = s > 0 ? 1u : 0u;
+            asm volatile(
+                "{\n.reg .pred p, e;\nsetp.ne.b32 p, %4, 0;\nelect.sync _|e, 0xffffffff;\n"
+                "@e tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n}" ::"r"(d),
+                "r"(ah + 8u * (uint32_t)s), "l"(bd), "r"(idesc), "r"(acc));
+          }
+        }
+        asm volatile(
+            "{\n.reg .pred e;\nelect.sync _|e, 0xffffffff;\n"
+            "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}" ::"r"(mdone + 8u * st));
+        committed = c + 1;
       }
     }
-    __syncwarp();
   } else {
     const int quarter = warp & 3, qh = warp >> 2; /* TMEM lane quarter, query half */
     /* expansion roles: train tiles, row er = tid % 64 and words 4 eh .. 4 eh + 3 */
@@ -316,19 +360,26 @@ __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__r
       uint4 cur = make_uint4(0, 0, 0, 0), nxt = cur;
       if (ntile > 0) {
         load_tile(0, cur);
-        /* the 256 queries: thread i expands rows i % 128 of both halves, words 8 (i / 128) .. + 7 */
-        const int r = tid & 127, h = tid >> 7;
+        /* this thread's query row into its TMEM lane of the query operand:
+         * source word m -> columns 8 m .. 8 m + 7 (K bytes 32 m .. 32 m + 31) */
+        uint4 qv[4];
 #pragma unroll
-        for (int half = 0; half < 2; half++) {
-          const int qi = qb * AKZ_TC_Q + half * 128 + r;
-          uint4 a = make_uint4(0, 0, 0, 0), b = a;
-          if (qi < nq) {
-            a = __ldg(q + (long long)qi * 4 + 2 * h);
-            b = __ldg(q + (long long)qi * 4 + 2 * h + 1);
+        for (int w = 0; w < 4; w++) qv[w] = myq < nq ? __ldg(q + (long long)myq * 4 + w) : make_uint4(0, 0, 0, 0);
+        const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(AKZ_TC_ACOL + 128 * qh);
+#pragma unroll
+        for (int w = 0; w < 4; w++) {
+          const uint32_t src[4] = {qv[w].x, qv[w].y, qv[w].z, qv[w].w};
+          uint32_t o[32];
+#pragma unroll
+          for (int m = 0; m < 4; m++) {
+            uint4 c0, c1;
+            tc_expand_word(src[m], true, c0, c1);
+            o[8 * m] = c0.x, o[8 * m + 1] = c0.y, o[8 * m + 2] = c0.z, o[8 * m + 3] = c0.w;
+            o[8 * m + 4] = c1.x, o[8 * m + 5] = c1.y, o[8 * m + 6] = c1.z, o[8 * m + 7] = c1.w;
           }
-          const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-          tc_expand_words<8>(w, r, 8 * h, 128, sA + half * AKZ_TC_A_BYTES, true);
+          tc_st32(ta + 32u * (uint32_t)w, o);
         }
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       }
       int pq = 0;
       if (myq < nq) {
@@ -338,62 +389,68 @@ __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__r
           pq += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
         }
       }
-      tc_top2 st; /* both entries start as {distance 512, index 0} */
-      st.ub = st.us = (uint32_t)(1024 - pq) << 21;
-      st.kf = (float)(512 - pq);
+      tc_top2 top; /* both entries start as {distance 512, index 0} */
+      top.ub = top.us = (uint32_t)(1024 - pq) << 21;
+      top.kf = (float)(512 - pq);
 
       auto epilogue = [&](uint32_t cb, int k) -> bool { /* batch cb = tile k of this item */
+        const uint32_t st = cb % AKZ_TC_STAGES;
         /* tcgen05.ld is warp-collective: the warp goes on only if every lane saw the batch done */
-        if (!__all_sync(0xffffffffu, tc_wait(mdone + 8u * (cb & 1u), (cb >> 1) & 1u, &sBad))) {
+        if (!__all_sync(0xffffffffu, tc_wait(mdone + 8u * st, (cb / AKZ_TC_STAGES) & 1u, &sBad))) {
           sBad = 1;
           return false;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const int lim0 = j1 - (j0 + k * AKZ_TC_N);
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          uint32_t r[32];
-          const uint32_t taddr =
-              tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((((cb & 1u) * 2u + (uint32_t)qh) * AKZ_TC_N) + 32 * h);
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-              "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-                "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-                "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-              : "r"(taddr));
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
-          const int lim = lim0 - 32 * h;
-          const uint32_t col0 = (uint32_t)(k * AKZ_TC_N + 32 * h);
-          if (lim >= 32)
-            tc_scan32<false>(r, col0, lim, st);
-          else
-            tc_scan32<true>(r, col0, lim, st);
-        }
+        uint32_t r0[32], r1[32];
+        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (st * 2u + (uint32_t)qh) * AKZ_TC_N;
+        tc_ld32(taddr, r0);
+        tc_ld32(taddr + 32u, r1);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;");
-        tc_arrive(mfree + 8u * (cb & 1u));
+        __syncwarp();
+        if (lane == 0) tc_arrive(mfree + 8u * st);
+        const int lim = j1 - (j0 + k * AKZ_TC_N);
+        const uint32_t col0 = (uint32_t)(k * AKZ_TC_N);
+        if (lim >= AKZ_TC_N) {
+          tc_scan32<false>(r0, col0, lim, top);
+          tc_scan32<false>(r1, col0 + 32u, lim - 32, top);
+        } else {
+          tc_scan32<true>(r0, col0, lim, top);
+          tc_scan32<true>(r1, col0 + 32u, lim - 32, top);
+        }
         return true;
       };
 
-      bool ok = true;
-      for (int k = 0; k < ntile; k++, c++) {
-        if (k + 1 < ntile) load_tile(k + 1, nxt); /* in flight while tile k is expanded */
+      /* tile k: expand, hand over, then read batch c - 1's accumulators */
+      auto step = [&](int k, const uint4 &v) -> bool {
         {
-          const uint32_t w[4] = {cur.x, cur.y, cur.z, cur.w};
-          tc_expand_words<4>(w, er, 4 * eh, AKZ_TC_N, sB + (c & 1u) * AKZ_TC_B_BYTES, false);
+          const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+          tc_expand_words<4>(w, er, 4 * eh, AKZ_TC_N, sB + (c % AKZ_TC_STAGES) * AKZ_TC_B_BYTES, false);
         }
-        cur = nxt;
-        asm volatile("fence.proxy.async.shared::cta;");
-        tc_arrive(mfull + 8u * (c & 1u));
-        if (k >= 1 && !(ok = epilogue(c - 1, k - 1))) break; /* tile k - 1 while tile k's MMAs run */
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) tc_arrive(mfull + 8u * (c % AKZ_TC_STAGES));
+        const bool r = k < AKZ_TC_LAG || epilogue(c - AKZ_TC_LAG, k - AKZ_TC_LAG);
+        c++;
+        return r;
+      };
+      /* two register sets in turn: each tile's rows are loaded one step ahead
+       * and used where they landed, with no copy that would wait for them */
+      bool ok = true;
+      for (int k = 0; k < ntile && ok; k += 2) {
+        if (k + 1 < ntile) load_tile(k + 1, nxt);
+        ok = step(k, cur);
+        if (!ok || k + 1 >= ntile) break;
+        if (k + 2 < ntile) load_tile(k + 2, cur);
+        ok = step(k + 1, nxt);
       }
       if (!ok) break;
-      if (ntile > 0 && !epilogue(c - 1, ntile - 1)) break;
+      for (int k = max(0, ntile - AKZ_TC_LAG); k < ntile && ok; k++) ok = epilogue(c - (uint32_t)(ntile - k), k);
+      if (!ok) break;
       if (myq < nq) {
-        const int bd = pq + (int)(st.ub >> 21) - 512, sd = pq + (int)(st.us >> 21) - 512;
-        const int bi = j0 + (int)(st.ub & 0x1fffffu), si = j0 + (int)(st.us & 0x1fffffu);
+        const int bd = pq + (int)(top.ub >> 21) - 512, sd = pq + (int)(top.us >> 21) - 512;
+        const int bi = j0 + (int)(top.ub & 0x1fffffu), si = j0 + (int)(top.us & 0x1fffffu);
         if (nsplit == 1) {
           out[2 * myq] = make_int4(myq, bi, 0, __float_as_int((float)bd));
           out[2 * myq + 1] = make_int4(myq, si, 0, __float_as_int((float)sd));
@@ -403,16 +460,16 @@ __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__r
       }
     }
   }
-  if (warp == AKZ_TC_CWARPS && lane == 0 && committed > 0) {
+  if (warp == AKZ_TC_CWARPS && committed > 0) {
     /* every batch's MMAs finished before the CTA frees TMEM and exits; on
      * the normal path the epilogue has already seen the last one */
     const uint32_t cp = committed - 1;
-    tc_mbar_wait(mdone + 8u * (cp & 1u), (cp >> 1) & 1u);
+    tc_mbar_wait(mdone + 8u * (cp % AKZ_TC_STAGES), (cp / AKZ_TC_STAGES) & 1u);
   }
   if (tid == 0 && sBad) atomicExch(&g_akz_tc_err, 1);
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
 }
 
 /* Train splits for the tensor path: items of 256 queries x one split are
@@ -450,9 +507,10 @@ cudaError_t akz_match_tc_launch(const void *dq, int nq, const void *dt, int nt, 
   if (split_len >= (1 << 21)) return cudaErrorInvalidValue;
   const int nitems = ((nq + AKZ_TC_Q - 1) / AKZ_TC_Q) * nsplit;
   const int grid = nitems < nsm ? nitems : nsm;
-  cudaError_t e = cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AKZ_TC_SMEM);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AKZ_TC_SMEM_LAUNCH);
   if (e != cudaSuccess) return e;
-  k_match_tc<<<grid, AKZ_TC_THREADS, AKZ_TC_SMEM, s>>>((const uint4 *)dq, (const uint4 *)dt, nq, nt, split_len, nsplit,
+  k_match_tc<<<grid, AKZ_TC_THREADS, AKZ_TC_SMEM_LAUNCH, s>>>((const uint4 *)dq, (const uint4 *)dt, nq, nt, split_len, nsplit,
                                                       (akz_tc_top2 *)partial, (int4 *)dout);
   return cudaGetLastError();
 }
