@@ -674,36 +674,53 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
               "r"(dst), "l"(tmap), "r"(ox - 4), "r"(oy - 3), "r"(mb)
           : "memory");
     }
-    uint32_t done = 0;
-    for (int it = 0; it < AKZ_FED_TMA_SPIN && !done; it++)
-      asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
-                   : "=r"(done)
-                   : "r"(mb)
-                   : "memory");
-    if (__syncthreads_or(!done)) { /* (CTA-uniform) record it, give the copy one more bounded wait, and leave */
-      if (tid == 0) atomicExch(&p.t.stats[L.image].status, (int)AKZ_ERR_TIMEOUT);
+    /* one warp polls the barrier; the others wait at the block barrier,
+     * where they issue nothing (the SM's other CTA keeps the slots) */
+    uint32_t done = 1;
+    if (warp == 0) {
+      done = 0;
       for (int it = 0; it < AKZ_FED_TMA_SPIN && !done; it++)
         asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
                      : "=r"(done)
                      : "r"(mb)
                      : "memory");
+    }
+    if (__syncthreads_or(!done)) { /* (CTA-uniform) record it, give the copy one more bounded wait, and leave */
+      if (tid == 0) {
+        atomicExch(&p.t.stats[L.image].status, (int)AKZ_ERR_TIMEOUT);
+        done = 0;
+        for (int it = 0; it < AKZ_FED_TMA_SPIN && !done; it++)
+          asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
+                       : "=r"(done)
+                       : "r"(mb)
+                       : "memory");
+      }
+      __syncthreads();
       return false;
     }
     /* replicate border: columns first (each row from its own clamped
      * column), then whole rows; the box always contains column and row 0
      * or W-1 / H-1 where it crosses the image edge */
     if (ox - 4 < 0 || ox + 132 > W || oy - 3 < 0 || oy - 3 + PH > H) {
-      if (ox - 4 < 0 || ox + 132 > W) {
-        for (int i = tid; i < PH * PS; i += NT) {
-          const int r = i / PS, c = i - r * PS, x = ox - 4 + c, xc = akz_clampi(x, 0, W - 1);
-          if (xc != x) sP[i] = sP[r * PS + (xc - (ox - 4))];
+      /* only the box columns left of x = 0 (nl) and from x = W on (from
+       * cr), then the rows above y = 0 (nt) and from y = H on (from rb) */
+      const int nl = max(0, 4 - ox), cr = min(PS, W - (ox - 4));
+      const int nc = nl + (PS - cr);
+      if (nc > 0) {
+        for (int i = tid; i < PH * nc; i += NT) {
+          const int r = i / nc, k = i - r * nc, c = k < nl ? k : cr + (k - nl);
+          const int xc = akz_clampi(ox - 4 + c, 0, W - 1);
+          sP[r * PS + c] = sP[r * PS + (xc - (ox - 4))];
         }
         __syncthreads();
       }
-      if (oy - 3 < 0 || oy - 3 + PH > H) {
-        for (int i = tid; i < PH * PS; i += NT) {
-          const int r = i / PS, c = i - r * PS, y = oy - 3 + r, yc = akz_clampi(y, 0, H - 1);
-          if (yc != y) sP[i] = sP[(yc - (oy - 3)) * PS + c];
+      const int nt = max(0, 3 - oy), rb = min(PH, H - (oy - 3));
+      const int nr = nt + (PH - rb);
+      if (nr > 0) {
+        for (int i = tid; i < nr * PS; i += NT) {
+          const int k = i / PS, c = i - k * PS, r = k < nt ? k : rb + (k - nt);
+          const int yc = akz_clampi(oy - 3 + r, 0, H - 1);
+          sP[r * PS + c] = sP[(yc - (oy - 3)) * PS + c];
         }
         __syncthreads();
       }
@@ -734,16 +751,14 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
   }
   __syncthreads();
 
-  /* 3. columns of the Gaussian: Lsmooth on rows R0 +- 1 (sS row n is y = oy - 1 + n) */
+  /* 3. columns of the Gaussian: Lsmooth on rows R0 +- 1 (sS row n is y = oy - 1 + n); the
+   *    tile's Lsmooth goes to HBM from step 5, by the threads that own its pixels */
   if (tid < NP * VG) {
     const int g = tid / NP, c = 2 * (tid - g * NP);
     const float *col = sT + c;
     float2 v[VR + 4];
 #pragma unroll
     for (int j = 0; j < VR + 4; j++) v[j] = ld2(col + min(g * VR + j, PH - 1) * SS); /* rows past sT: unused */
-    const int x = ox - 2 + c; /* even */
-    const bool w0 = x >= tx0 && x < tx1, w1 = x + 1 < tx1;
-    float *lsp = p.t.planes + L.ls + x;
 #pragma unroll
     for (int j = 0; j < VR; j++) {
       const int n = g * VR + j;
@@ -754,14 +769,6 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
       acc = akz_axpy2<FUSED>(k1, s13, acc);
       acc = akz_axpy2<FUSED>(k2, v[j + 2], acc);
       st2(sS + n * SS + c, acc);
-      const int y = oy - 1 + n;
-      if (w0 && y >= ty0 && y < ty1) {
-        float *o = lsp + (long long)y * L.pitch;
-        if (w1)
-          st2(o, acc);
-        else
-          o[0] = acc.x;
-      }
     }
   }
   __syncthreads();
@@ -790,10 +797,29 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
    *    thread's k_fed geometry: columns x0 .. x0+3 (x0 = ox + lx0, sS
    *    columns lx0 + 2 ..), rows ly0 .. ly0+2; kept in g, stored to sT
    *    (free since pass 3; neighbours read it after the barrier) and, for
-   *    later chunks, to HBM */
+   *    later chunks, to HBM; first the thread's own Lsmooth pixels go to
+   *    HBM */
   float *sG = sT;
   const float inv_k = p.kc[L.image * 16 + L.octave].y;
   const int x0 = ox + lx0; /* a multiple of 4 */
+  const bool xfull = x0 >= tx0 && x0 + 4 <= tx1, xany = x0 + 4 > tx0 && x0 < tx1;
+#pragma unroll
+  for (int r = 0; r < 3; r++) { /* the thread's Lsmooth pixels (sS row ly0 + r + 1, columns lx0 + 2 ..) */
+    const int y = oy + ly0 + r;
+    if (y >= ty0 && y < ty1 && xany) {
+      const float *row = sS + (ly0 + r + 1) * SS + lx0 + 2;
+      const float2 a = ld2(row), b = ld2(row + 2);
+      float *o = p.t.planes + L.ls + (long long)y * L.pitch + x0;
+      if (xfull) {
+        *reinterpret_cast<float4 *>(o) = make_float4(a.x, a.y, b.x, b.y);
+      } else {
+        const float v[4] = {a.x, a.y, b.x, b.y};
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          if (x0 + k >= tx0 && x0 + k < tx1) o[k] = v[k];
+      }
+    }
+  }
 #pragma unroll
   for (int h = 0; h < 2; h++) { /* column pairs (x0, x0+1), (x0+2, x0+3) */
     float2 dh[5], sh[5];
@@ -823,14 +849,14 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
   for (int r = 0; r < 3; r++) {
     *reinterpret_cast<float4 *>(sG + (ly0 + r) * RW + lx0) = make_float4(g[r][0], g[r][1], g[r][2], g[r][3]);
     const int y = oy + ly0 + r;
-    if (p.write_g && y >= ty0 && y < ty1) {
-      float *o = p.t.planes + I.g + (long long)y * L.pitch + x0;
-      if (x0 >= tx0 && x0 + 4 <= tx1) {
-        *reinterpret_cast<float4 *>(o) = make_float4(g[r][0], g[r][1], g[r][2], g[r][3]);
+    if (p.write_g && y >= ty0 && y < ty1 && xany) {
+      float *og = p.t.planes + I.g + (long long)y * L.pitch + x0;
+      if (xfull) {
+        *reinterpret_cast<float4 *>(og) = make_float4(g[r][0], g[r][1], g[r][2], g[r][3]);
       } else {
 #pragma unroll
         for (int k = 0; k < 4; k++)
-          if (x0 + k >= tx0 && x0 + k < tx1) o[k] = g[r][k];
+          if (x0 + k >= tx0 && x0 + k < tx1) og[k] = g[r][k];
       }
     }
   }
@@ -942,7 +968,11 @@ __device__ __forceinline__ void akz_fed_step4(float (&Lp)[3][4], float4 above, f
     for (int k = 0; k < 4; k++) Lp[r][k] = nv[r][k];
 }
 
-template <bool FUSED>
+/* D > 0: the launch's FED depth as a compile-time constant (p.steps == D),
+ * so that the step loop unrolls (the step size of each step is a constant
+ * parameter offset, the exchange parity a constant, and the new values
+ * land in renamed registers); D == 0: the depth from p.steps at run time. */
+template <bool FUSED, int D>
 __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
 {
   extern __shared__ __align__(128) float sm_raw[];
@@ -956,7 +986,7 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
   const akz_level_desc L = p.t.lv[sg.level_desc];
   const akz_image_desc I = p.t.im[L.image];
   const int W = L.width, H = L.height;
-  const int d = p.steps;
+  const int d = D > 0 ? D : p.steps;
   const int TW = akz_fed_tile_w(d), TH = akz_fed_tile_h(d);
   const int lt = blockIdx.x - sg.tile_begin;
   const int tx0 = (lt % sg.tiles_x) * TW, ty0 = (lt / sg.tiles_x) * TH;
@@ -1040,7 +1070,7 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
     put(0);
     __syncthreads();
   }
-  for (int s = 0; s < d; s++) {
+  auto step = [&](int s) {
     const int par = s & 1;
     const float4 above = warp > 0 ? *reinterpret_cast<const float4 *>(xb + ((par * 2 + 1) * 16 + warp - 1) * RW + lx0)
                                   : make_float4(Lp[0][0], Lp[0][1], Lp[0][2], Lp[0][3]);
@@ -1051,6 +1081,12 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
       put(par ^ 1);
       __syncthreads();
     }
+  };
+  if constexpr (D > 0) {
+#pragma unroll
+    for (int s = 0; s < D; s++) step(s);
+  } else {
+    for (int s = 0; s < d; s++) step(s);
   }
   /* tile interior from registers, one 128-bit store per row */
   float *out = p.dst == 3 ? p.chk : planes + (p.dst == 0 ? L.lt : (p.dst == 1 ? I.t1 : I.t2));
@@ -1130,17 +1166,24 @@ cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int, int, cudaSt
   if (p.steps < 0 || p.steps > 8) return cudaErrorInvalidValue; /* 0: Lsmooth, conductance and the start image only */
   if (p.first && !p.tmaps) return cudaErrorInvalidValue;         /* the input box needs the tensor maps */
   const size_t smem = akz_fed_smem_bytes(0, 0, p.steps, p.first);
-  cudaError_t e;
-  if (p.fused) {
-    e = cudaFuncSetAttribute(k_fed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto go = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_fed<true><<<ntiles, AKZ_FED_THREADS, smem, s>>>(p);
-  } else {
-    e = cudaFuncSetAttribute(k_fed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_fed<false><<<ntiles, AKZ_FED_THREADS, smem, s>>>(p);
+    kern<<<ntiles, AKZ_FED_THREADS, smem, s>>>(p);
+    return cudaGetLastError();
+  };
+  if (!p.fused) return go(k_fed<false, 0>);
+  switch (p.steps) { /* the fused kernels unroll their depth */
+  case 1: return go(k_fed<true, 1>);
+  case 2: return go(k_fed<true, 2>);
+  case 3: return go(k_fed<true, 3>);
+  case 4: return go(k_fed<true, 4>);
+  case 5: return go(k_fed<true, 5>);
+  case 6: return go(k_fed<true, 6>);
+  case 7: return go(k_fed<true, 7>);
+  case 8: return go(k_fed<true, 8>);
+  default: return go(k_fed<true, 0>);
   }
-  return cudaGetLastError();
 }
 
 cudaError_t akz_launch_area(const akz_area_params &p, int maxw, int maxh, cudaStream_t s)
