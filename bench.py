@@ -36,10 +36,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "1080p images/s detect+MLDB, surrogate vs plain FED at fixed repeatability"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the 27 k_fed
-# launches of one 1920x1080 image, from an ncu capture of an 8-image batch
-# (399.2 MB read + 221.5 MB written, / 8) at a blocking depth of 8 FED steps
-# per launch; the level stage's traffic per step is this times the batch.
-FED_TRAFFIC_PER_1080P_IMAGE = 77.59e6
+# launches of one 1920x1080 image, from an ncu capture of an 8-image batch in
+# the fused mode (399.3 MB read + 224.7 MB written, / 8) at a blocking depth
+# of 8 FED steps per launch; the level stage's traffic per step is this times
+# the batch.
+FED_TRAFFIC_PER_1080P_IMAGE = 78.00e6
 FED_TRAFFIC_DEPTH = 8
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
