@@ -730,7 +730,8 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
   /* 2. rows of the Gaussian on columns R0 - 2 .. R0 + 129 (sT column c is
    *    x = ox - 2 + c, its taps sP c .. c + 4): column pairs 0..63 by
    *    (tid & 63) on rows (tid >> 6) + 8k, pairs 64 and 65 by the first
-   *    2 PH threads */
+   *    2 PH threads (an even spread over all threads costs more in index
+   *    arithmetic than it saves) */
   const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
   auto hrow = [&](int row, int c) {
     const float *r = sP + row * PS + c;
@@ -777,14 +778,14 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
    *    (which fixes the corners) */
   const int cm = 1 - ox, cp = W - ox + 2; /* sS columns of x = -1 and x = W */
   const int nm = -oy, np = H - oy + 1;    /* sS rows of y = -1 and y = H */
-  if (cm >= 0 || cp < SS) {
+  if (cm >= 0 || cp < SS) { /* (CTA-uniform) */
     if (tid < SH) {
       float *row = sS + tid * SS;
       if (cm >= 0) row[cm] = row[cm + 2];
       if (cp < SS) row[cp] = row[cp - 2];
     }
+    __syncthreads();
   }
-  __syncthreads();
   if (nm >= 0 || np < SH) {
     if (tid < SS) {
       if (nm >= 0) sS[nm * SS + tid] = sS[(nm + 2) * SS + tid];

@@ -64,3 +64,28 @@ def test_tensor_matcher_largest_sweep_size_sampled(gpu_lib, oracle):
     want["queryIdx"] = idx[:, None]
     assert got[idx].tobytes() == want.tobytes()
     assert _status(gpu_lib) == 0
+
+
+def test_tensor_matcher_train_set_beyond_21_bit_columns(gpu_lib, oracle):
+    """2^21 + 5 train rows: the tensor path's packed top-two words hold a
+    split's column in 21 bits, so the split count must keep every split
+    shorter than 2^21 rows; the nearest neighbours are planted at both ends
+    and at the split boundary region."""
+    nq, nt = 64, (1 << 21) + 5
+    q, t = synth.matcher_rows(31, nq, nt)
+    rng = np.random.default_rng(31)
+    for i, j in enumerate([0, nt - 1, (1 << 20) + 3, (1 << 21) - 1]):
+        t[j] = q[i]
+        t[j, rng.integers(0, 61)] ^= 1  # distance 1
+    tc = _match(gpu_lib, q, t, True)
+    assert tc.tobytes() == _match(gpu_lib, q, t, False).tobytes()
+    assert tc.tobytes() == oracle.bfmatch(q, t).tobytes()
+    assert _status(gpu_lib) == 0
+
+
+def test_few_train_rows_take_the_popc_kernel(gpu_lib, oracle):
+    """At least 2^20 pairs but fewer than 128 train rows: the popc kernel
+    answers, with the same result as the oracle."""
+    q, t = synth.matcher_rows(32, 20000, 100)
+    got = _match(gpu_lib, q, t, True)
+    assert got.tobytes() == oracle.bfmatch(q, t).tobytes()
