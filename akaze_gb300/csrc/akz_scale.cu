@@ -969,6 +969,74 @@ __device__ __forceinline__ void akz_fed_step4(float (&Lp)[3][4], float4 above, f
     for (int k = 0; k < 4; k++) Lp[r][k] = nv[r][k];
 }
 
+/* The flux pair sums of akz_fed_pairs as register pairs, formed once per
+ * launch for the fused step (the packed operations then find their
+ * loop-invariant operands already paired). */
+struct akz_fed_pairs2 {
+  float2 h01[3], h23[3]; /* horizontal sums west of columns 0, 1 and 2, 3 */
+  float h4[3];           /* east of column 3 */
+  float2 s01[3], s23[3]; /* below rows 0..2 */
+  float2 n01, n23;       /* above row 0 */
+};
+
+__device__ __forceinline__ akz_fed_pairs2 akz_fed_pack_pairs(const float (&gh)[3][5], const float (&gs)[3][4],
+                                                            const float (&gn)[4])
+{
+  akz_fed_pairs2 P;
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    P.h01[r] = make_float2(gh[r][0], gh[r][1]);
+    P.h23[r] = make_float2(gh[r][2], gh[r][3]);
+    P.h4[r] = gh[r][4];
+    P.s01[r] = make_float2(gs[r][0], gs[r][1]);
+    P.s23[r] = make_float2(gs[r][2], gs[r][3]);
+  }
+  P.n01 = make_float2(gn[0], gn[1]);
+  P.n23 = make_float2(gn[2], gn[3]);
+  return P;
+}
+
+/* The fused step of akz_fed_step4 on the paired state: the same operations
+ * (so the same results), with the image rows held as pairs (L0, L1), (L2, L3)
+ * and the flux pair sums as P. */
+__device__ __forceinline__ void akz_fed_step4_paired(float2 (&Lq)[3][2], float4 above, float4 below, float h,
+                                                     const akz_fed_pairs2 &P)
+{
+  float Lw[3], Le[3];
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    Lw[r] = __shfl_up_sync(0xffffffffu, Lq[r][1].y, 1);
+    Le[r] = __shfl_down_sync(0xffffffffu, Lq[r][0].x, 1);
+  }
+  float2 Fn01 = f2mul(P.n01, f2sub(Lq[0][0], make_float2(above.x, above.y)));
+  float2 Fn23 = f2mul(P.n23, f2sub(Lq[0][1], make_float2(above.z, above.w)));
+  const float2 hh = make_float2(h, h);
+  float2 nv[3][2];
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    const float2 A = Lq[r][0], B = Lq[r][1];
+    const float2 e01 = f2sub(A, make_float2(Lw[r], A.x));
+    const float2 e23 = f2sub(B, make_float2(A.y, B.x));
+    const float2 F01 = f2mul(P.h01[r], e01), F23 = f2mul(P.h23[r], e23);
+    const float F4 = P.h4[r] * (Le[r] - B.y);
+    const float2 xs01 = make_float2(F01.y - F01.x, F23.x - F01.y); /* xpos - xneg */
+    const float2 xs23 = make_float2(F23.y - F23.x, F4 - F23.y);
+    const float2 nA = r < 2 ? Lq[r + 1][0] : make_float2(below.x, below.y);
+    const float2 nB = r < 2 ? Lq[r + 1][1] : make_float2(below.z, below.w);
+    const float2 Fs01 = f2mul(P.s01[r], f2sub(nA, A)), Fs23 = f2mul(P.s23[r], f2sub(nB, B)); /* ypos */
+    const float2 t01 = f2sub(f2add(xs01, Fs01), Fn01), t23 = f2sub(f2add(xs23, Fs23), Fn23);
+    nv[r][0] = f2fma(hh, t01, A);
+    nv[r][1] = f2fma(hh, t23, B);
+    Fn01 = Fs01;
+    Fn23 = Fs23;
+  }
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    Lq[r][0] = nv[r][0];
+    Lq[r][1] = nv[r][1];
+  }
+}
+
 /* D > 0: the launch's FED depth as a compile-time constant (p.steps == D),
  * so that the step loop unrolls (the step size of each step is a constant
  * parameter offset, the exchange parity a constant, and the new values
@@ -1063,6 +1131,50 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
 
   /* exchange rows: xb[((par * 2 + last) * 16 + warp) * RW + column] */
   float *xb = sm;
+  if constexpr (FUSED) { /* the fused steps on paired registers */
+    const akz_fed_pairs2 P = akz_fed_pack_pairs(gh, gs, gn);
+    float2 Lq[3][2];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      Lq[r][0] = make_float2(Lp[r][0], Lp[r][1]);
+      Lq[r][1] = make_float2(Lp[r][2], Lp[r][3]);
+    }
+    auto putq = [&](int par) {
+      *reinterpret_cast<float4 *>(xb + ((par * 2 + 0) * 16 + warp) * RW + lx0) =
+          make_float4(Lq[0][0].x, Lq[0][0].y, Lq[0][1].x, Lq[0][1].y);
+      *reinterpret_cast<float4 *>(xb + ((par * 2 + 1) * 16 + warp) * RW + lx0) =
+          make_float4(Lq[2][0].x, Lq[2][0].y, Lq[2][1].x, Lq[2][1].y);
+    };
+    if (d > 0) {
+      putq(0);
+      __syncthreads();
+    }
+    auto stepq = [&](int s) {
+      const int par = s & 1;
+      const float4 above = warp > 0 ? *reinterpret_cast<const float4 *>(xb + ((par * 2 + 1) * 16 + warp - 1) * RW + lx0)
+                                    : make_float4(Lq[0][0].x, Lq[0][0].y, Lq[0][1].x, Lq[0][1].y);
+      const float4 below = warp < 15 ? *reinterpret_cast<const float4 *>(xb + ((par * 2 + 0) * 16 + warp + 1) * RW + lx0)
+                                     : make_float4(Lq[2][0].x, Lq[2][0].y, Lq[2][1].x, Lq[2][1].y);
+      akz_fed_step4_paired(Lq, above, below, p.h[s], P);
+      if (s + 1 < d) {
+        putq(par ^ 1);
+        __syncthreads();
+      }
+    };
+    if constexpr (D > 0) {
+#pragma unroll
+      for (int s = 0; s < D; s++) stepq(s);
+    } else {
+      for (int s = 0; s < d; s++) stepq(s);
+    }
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      Lp[r][0] = Lq[r][0].x;
+      Lp[r][1] = Lq[r][0].y;
+      Lp[r][2] = Lq[r][1].x;
+      Lp[r][3] = Lq[r][1].y;
+    }
+  } else {
   auto put = [&](int par) {
     *reinterpret_cast<float4 *>(xb + ((par * 2 + 0) * 16 + warp) * RW + lx0) = make_float4(Lp[0][0], Lp[0][1], Lp[0][2], Lp[0][3]);
     *reinterpret_cast<float4 *>(xb + ((par * 2 + 1) * 16 + warp) * RW + lx0) = make_float4(Lp[2][0], Lp[2][1], Lp[2][2], Lp[2][3]);
@@ -1088,6 +1200,7 @@ __global__ void __launch_bounds__(AKZ_FED_THREADS, 2) k_fed(akz_fed_params p)
     for (int s = 0; s < D; s++) step(s);
   } else {
     for (int s = 0; s < d; s++) step(s);
+  }
   }
   /* tile interior from registers, one 128-bit store per row */
   float *out = p.dst == 3 ? p.chk : planes + (p.dst == 0 ? L.lt : (p.dst == 1 ? I.t1 : I.t2));
