@@ -104,11 +104,12 @@ def level_sizes(w, h, omax=4, nsub=4):
 
 
 def fed_algorithmic_bytes(w, h):
-    """Compulsory HBM bytes of the level stage per image: read the
-    predecessor level (4 B/px of its size) and write the evolved level
-    (4 B/px), for every level >= 1."""
+    """Compulsory HBM bytes of the level stage per image: for every level
+    >= 1, read the predecessor level (4 B/px of its size), write the evolved
+    level (4 B/px) and write its pre-diffusion smoothing Lsmooth (4 B/px),
+    which the stage produces for the detector."""
     L = level_sizes(w, h)
-    return sum(4 * L[i - 1][0] * L[i - 1][1] + 4 * L[i][0] * L[i][1] for i in range(1, len(L)))
+    return sum(4 * L[i - 1][0] * L[i - 1][1] + 8 * L[i][0] * L[i][1] for i in range(1, len(L)))
 
 
 def image_algorithmic_bytes(w, h, nkp):
