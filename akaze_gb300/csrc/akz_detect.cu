@@ -90,6 +90,12 @@ struct akz_strip_geo {
   static constexpr int A = (ST + 2) & ~1;
   static constexpr int TW = (127 - A - ST) & ~1;
   static constexpr int SW = 128 + 2 * ST;
+  /* Lsmooth ring rows: column SO + c holds x = tx0 - A - ST + c.  For even
+   * steps the ring row starts 2 columns earlier, on a 16-byte boundary of the
+   * image row (tx0 is a multiple of 4), so interior strips load it in 16-byte
+   * chunks; SWR is the ring row stride. */
+  static constexpr int SO = (ST & 1) ? 0 : 2;
+  static constexpr int SWR = (ST & 1) ? SW : ((SW + SO + 3) & ~3);
   static constexpr int EO = (ST & 1) ? -1 : -2;
   static constexpr int NEP = (128 - ST - EO - A) / 2; /* E pairs: right tap pair of the last one ends at D 127 */
   static_assert(TW - EO + 1 <= 2 * NEP, "E covers tx0 - 1 .. tx0 + TW");
@@ -109,6 +115,11 @@ int akz_strip_tile_width(int st) { return akz_strip_tile_width_rt(st); }
 #define AKZ_STRIP_NE 16 /* determinant ring rows */
 #define AKZ_STRIP_EW 128
 
+__device__ __forceinline__ void akz_cp_async16(float *dst, const float *src)
+{
+  const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
 __device__ __forceinline__ void akz_cp_async4(float *dst, const float *src)
 {
   const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
@@ -130,37 +141,48 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
                                                  int ty0)
 {
   using G = akz_strip_geo<ST>;
-  constexpr int A = G::A, TW = G::TW, SW = G::SW, EO = G::EO, NEP = G::NEP;
+  constexpr int A = G::A, TW = G::TW, SO = G::SO, SWR = G::SWR, EO = G::EO, NEP = G::NEP;
   constexpr int NS = AKZ_STRIP_NS, ND = AKZ_STRIP_ND, NE = AKZ_STRIP_NE, EW = AKZ_STRIP_EW;
-  constexpr int SJ = (SW + 31) / 32;
+  constexpr int SJ = (SWR + 31) / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int W = L.width, H = L.height;
   constexpr int BH = ST == 3 ? 6 : 8; /* rows per block: pairs (o, o + ST) tile it */
   static_assert(BH % (2 * ST) == 0, "row pairs tile the block");
   const int ch = min(AKZ_STRIP_CH, H - ty0); /* rows of this CTA */
   const int iters = (ch + BH - 1) / BH;
-  float *sS = sm, *sX = sS + NS * SW, *sY = sX + ND * 128, *sE = sY + ND * 128;
+  float *sS = sm, *sX = sS + NS * SWR, *sY = sX + ND * 128, *sE = sY + ND * 128;
   const float fac1 = p.fac1, fac2 = p.fac2;
   const float *ls = p.t.planes + L.ls;
   float *lxyp = p.t.planes + L.lx; /* interleaved (Lx, Ly), row pitch 2 * pitch */
   const long long pitch = L.pitch;
 
-  int xs[SJ]; /* source column of this lane's S columns lane + 32 j */
+  const int xs0 = tx0 - A - ST - SO; /* image column of ring column 0 */
+  int xs[SJ]; /* source column of this lane's ring columns lane + 32 j */
 #pragma unroll
-  for (int j = 0; j < SJ; j++) xs[j] = akz_refl_clamp(tx0 - A - ST + lane + 32 * j, W);
+  for (int j = 0; j < SJ; j++) xs[j] = akz_refl_clamp(xs0 + lane + 32 * j, W);
+  /* (CTA-uniform) the ring row lies inside the image row: 16-byte copies */
+  const bool vec = !(ST & 1) && xs0 >= 0 && xs0 + SWR <= W;
 
   auto load_s = [&](int r) { /* S row r into its ring slot */
     const float *src = ls + (long long)akz_refl_clamp(r, H) * pitch;
-    float *dst = sS + (r & (NS - 1)) * SW;
+    float *dst = sS + (r & (NS - 1)) * SWR;
+    if (vec) {
 #pragma unroll
-    for (int j = 0; j < SJ; j++) {
-      const int c = lane + 32 * j;
-      if (c < SW) akz_cp_async4(dst + c, src + xs[j]);
+      for (int j = 0; j < (SWR / 4 + 31) / 32; j++) {
+        const int q = lane + 32 * j;
+        if (q < SWR / 4) akz_cp_async16(dst + 4 * q, src + xs0 + 4 * q);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < SJ; j++) {
+        const int c = lane + 32 * j;
+        if (c < SWR) akz_cp_async4(dst + c, src + xs[j]);
+      }
     }
   };
   auto comp_d = [&](int r) { /* Lx, Ly row r; HBM for the strip's own pixels */
-    const float *su = sS + ((r - ST) & (NS - 1)) * SW, *sc = sS + (r & (NS - 1)) * SW,
-                *sd = sS + ((r + ST) & (NS - 1)) * SW;
+    const float *su = sS + ((r - ST) & (NS - 1)) * SWR + SO, *sc = sS + (r & (NS - 1)) * SWR + SO,
+                *sd = sS + ((r + ST) & (NS - 1)) * SWR + SO;
     float *ox = sX + (r & (ND - 1)) * 128, *oy = sY + (r & (ND - 1)) * 128;
     const bool wrow = r >= ty0 && r < ty0 + ch;
 #pragma unroll
@@ -217,8 +239,8 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
   /* Lx, Ly rows rA and rA + ST for column pair d: the two share their
    * middle Lsmooth rows, 12 pair loads instead of 16 */
   auto comp_d2 = [&](int rA, int d) {
-    const float *s0 = sS + ((rA - ST) & (NS - 1)) * SW, *s1 = sS + (rA & (NS - 1)) * SW,
-                *s2 = sS + ((rA + ST) & (NS - 1)) * SW, *s3 = sS + ((rA + 2 * ST) & (NS - 1)) * SW;
+    const float *s0 = sS + ((rA - ST) & (NS - 1)) * SWR + SO, *s1 = sS + (rA & (NS - 1)) * SWR + SO,
+                *s2 = sS + ((rA + ST) & (NS - 1)) * SWR + SO, *s3 = sS + ((rA + 2 * ST) & (NS - 1)) * SWR + SO;
     const float2 L0 = ld2(s0 + d), C0 = tap(s0, d + ST), R0 = ld2(s0 + d + 2 * ST);
     const float2 L1 = ld2(s1 + d), C1 = tap(s1, d + ST), R1 = ld2(s1 + d + 2 * ST);
     const float2 L2 = ld2(s2 + d), C2 = tap(s2, d + ST), R2 = ld2(s2 + d + 2 * ST);
@@ -346,7 +368,7 @@ __device__ __forceinline__ void akz_detect_strip(const akz_detect_params &p, con
 }
 
 template <bool FUSED>
-__global__ void __launch_bounds__(256) k_detect_strip(akz_detect_params p)
+__global__ void __launch_bounds__(256, 4) k_detect_strip(akz_detect_params p)
 {
   extern __shared__ float sm[];
   const int si = akz_find_seg_warp(p.segs, p.nsegs, blockIdx.x);
@@ -365,7 +387,9 @@ __global__ void __launch_bounds__(256) k_detect_strip(akz_detect_params p)
 
 size_t akz_detect_strip_smem()
 {
-  return (size_t)(AKZ_STRIP_NS * akz_strip_geo<4>::SW + 2 * AKZ_STRIP_ND * 128 + AKZ_STRIP_NE * AKZ_STRIP_EW) *
+  static_assert(akz_strip_geo<4>::SWR >= akz_strip_geo<2>::SWR && akz_strip_geo<4>::SWR >= akz_strip_geo<3>::SWR,
+                "the step-4 ring row is the widest");
+  return (size_t)(AKZ_STRIP_NS * akz_strip_geo<4>::SWR + 2 * AKZ_STRIP_ND * 128 + AKZ_STRIP_NE * AKZ_STRIP_EW) *
          sizeof(float);
 }
 
