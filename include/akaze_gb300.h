@@ -148,7 +148,9 @@ AKZ_API akz_status akz_gaussian_taps(float sigma, float *taps, int cap, int *nta
 /* ---- single image: libAKAZECU::AKAZE (AKAZE.h:58-143) ---------------- */
 
 /* AKAZE::AKAZE(options) + Allocate_Memory_Evolution (AKAZE.cpp:126-208):
- * level geometry for options.img_width x img_height, device memory. */
+ * level geometry for options.img_width x img_height, device memory.  Image
+ * sides from 16 to 32768 pixels; others are AKZ_ERR_INVALID_ARG (here and in
+ * akz_batch_create). */
 AKZ_API akz_status akz_create(const akz_options *opt, akz_context **out);
 /* AKAZE::~AKAZE (AKAZE.cpp:140-143). */
 AKZ_API akz_status akz_destroy(akz_context *ctx);

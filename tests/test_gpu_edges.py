@@ -113,3 +113,41 @@ def test_suppression_round_cap_reports_timeout(gpu_lib):
     b.run()
     kp1, d1 = b.results(0)
     assert np.array_equal(kp0.view(np.uint8), kp1.view(np.uint8)) and np.array_equal(d0, d1)
+
+
+TINY = [(16, 16, 61), (17, 16, 62), (33, 29, 63), (64, 48, 64), (97, 61, 65), (101, 77, 66)]
+
+
+@pytest.mark.parametrize("w,h,seed", TINY)
+@pytest.mark.parametrize("fast_math", [0, 1])
+def test_tiny_and_odd_sizes(gpu_lib, oracle, w, h, seed, fast_math):
+    """Every stage at sizes where tiles, strips, halos and level geometry
+    are mostly border (the bounds checks of the sanitizer, which is closed
+    on this hardware, stand on these cases and the oracle): exact mode
+    equals the oracle at every level, with NaN where both are NaN; fused
+    mode stays within 1e-4 of each level's largest magnitude."""
+    img = synth.synth_image(seed, w, h)
+    ak = _ak(gpu_lib, w, h, fast_math=fast_math)
+    kp, d = ak.detect_and_compute(img)
+    orc = oracle.Oracle(w, h)
+    okp, od = orc.run(img)
+    assert ak.nlevels == orc.nlevels
+    for lv in range(ak.nlevels):
+        for name in ("Lt", "Lsmooth", "Lx", "Ly"):
+            g, c = ak.plane(lv, name), orc.plane(lv, name)
+            if fast_math == 0:
+                assert np.array_equal(g, c, equal_nan=True), (lv, name)
+            elif np.isfinite(c).all():
+                rel = np.max(np.abs(g - c)) / max(float(np.max(np.abs(c))), 1e-30)
+                assert rel <= 1e-4, (lv, name, rel)
+    if fast_math == 0:
+        assert kp.tobytes() == okp.tobytes() and np.array_equal(d, od)
+
+
+def test_sizes_outside_the_supported_range_are_rejected(gpu_lib):
+    """Images narrower or lower than 16 pixels (or above 32768) are refused
+    before any device work with AKZ_ERR_INVALID_ARG; the context is not
+    created."""
+    for w, h in [(15, 16), (16, 15), (9, 7), (32769, 16)]:
+        with pytest.raises(gpu_lib.AkazeError):
+            _ak(gpu_lib, w, h)
