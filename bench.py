@@ -660,7 +660,7 @@ def main():
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
-    e_steps = max(1, min(args.steps, 10))
+    e_steps = max(1, min(args.steps, 20))
     # consecutive steps pipelined per group: a group's next upload starts once its
     # results are read back, while the other groups still compute
     c2 = batch.detect_describe_packed_steps([np_in] * e_steps, kp_out, d_out)
