@@ -63,7 +63,7 @@ def parse():
                     help="surrogate4k: run the net's 32-channel layers on tcgen05 (1) or mma.sync (0)")
     ap.add_argument("--check-tol", type=float, default=2e-3,
                     help="surrogate4k: per-level tolerance of the surrogate against plain FED before it falls back")
-    ap.add_argument("--groups", type=int, default=4,
+    ap.add_argument("--groups", type=int, default=6,
                     help="1080p batch: images split into this many native batches on their own streams (BatchGroup)")
     ap.add_argument("--fed-depth", default=None, choices=["auto", "4", "5", "6", "7", "8"],
                     help="FED steps per level-kernel launch; auto times each depth per level on the batch first "
