@@ -683,7 +683,8 @@ def main():
         "config": {"workload": f"plain A-KAZE detect+MLDB, {W}x{H} u8, 4 octaves x 4 sublevels, default options",
                    "fed": "plain (the learned surrogate is built but 2.6x slower at 4K on this GPU: --workload surrogate4k)",
                    "images_per_step_per_gpu": B, "parallelism": f"replicas x{ws}",
-                   "groups": f"{len(batch.parts)} native batches of {B // len(batch.parts)} images, one stream and graph each",
+                   "groups": "%d native batches of %s images, one stream and graph each"
+                             % (len(batch.parts), "/".join(str(b.n) for b in batch.parts)),
                    "l2": "inputs and working set larger than L2 (~%.1f GB per step)" % (B * image_algorithmic_bytes(W, H, 0) / 1e9),
                    "keypoints_per_image": nkp,
                    "fed_depth_per_level": fed_depth, "level_stage_ms_by_depth": depth_ms,
