@@ -105,3 +105,32 @@ def test_fast_math_pair_matches(gpu_lib, oracle):
         good = m[:, 0]["distance"] < 0.8 * m[:, 1]["distance"]
         res[fm] = int(good.sum())
     assert abs(res[1] - res[0]) <= max(3, int(0.02 * res[0])), res
+
+
+@pytest.mark.parametrize("kw", [dict(descriptor=4), dict(descriptor_channels=1), dict(descriptor_channels=2),
+                                dict(descriptor_size=256), dict(extrema_3d=1), dict(derivative_factor=0.8),
+                                dict(derivative_factor=2.0)],
+                         ids=["upright", "channels1", "channels2", "subset256", "extrema3d", "dfac0.8", "dfac2.0"])
+def test_fast_math_with_other_options(gpu_lib, oracle, kw):
+    """The fused mode combined with the other options (upright and 1- or
+    2-channel descriptors, a random-bit subset, the 3 x 3 x 3 extrema rule,
+    and derivative factors that run the tile detector): the same tolerances
+    against the oracle with those options."""
+    w, h = 640, 480
+    img = synth.synth_image(4300 + len(str(kw)), w, h)
+    o = gpu_lib.AKAZEOptions(fast_math=1, **kw)
+    o.setWidth(w)
+    o.setHeight(h)
+    ak = gpu_lib.AKAZE(o)
+    kp, d = ak.detect_and_compute(img)
+    okp, od = oracle.Oracle(w, h, oracle.default_options(**kw)).run(img)
+    assert d.shape[1] == od.shape[1]
+    if "derivative_factor" in kw:  # the detector's derivative planes at the other steps
+        orc = oracle.Oracle(w, h, oracle.default_options(**kw))
+        orc.run(img)
+        for lv in range(ak.nlevels):
+            for name in ("Lx", "Ly"):
+                g, c = ak.plane(lv, name), orc.plane(lv, name)
+                rel = np.max(np.abs(g - c)) / max(float(np.max(np.abs(c))), 1e-30)
+                assert rel <= LEVEL_TOL, (lv, name, rel)
+    _check(kp, d, okp, od)
