@@ -1286,8 +1286,20 @@ cudaError_t akz_launch_fed(const akz_fed_params &p, int ntiles, int, int, cudaSt
     kern<<<ntiles, AKZ_FED_THREADS, smem, s>>>(p);
     return cudaGetLastError();
   };
-  if (!p.fused) return go(k_fed<false, 0>);
-  switch (p.steps) { /* the fused kernels unroll their depth */
+  if (!p.fused) {
+    switch (p.steps) { /* both modes unroll their depth */
+    case 1: return go(k_fed<false, 1>);
+    case 2: return go(k_fed<false, 2>);
+    case 3: return go(k_fed<false, 3>);
+    case 4: return go(k_fed<false, 4>);
+    case 5: return go(k_fed<false, 5>);
+    case 6: return go(k_fed<false, 6>);
+    case 7: return go(k_fed<false, 7>);
+    case 8: return go(k_fed<false, 8>);
+    default: return go(k_fed<false, 0>);
+    }
+  }
+  switch (p.steps) {
   case 1: return go(k_fed<true, 1>);
   case 2: return go(k_fed<true, 2>);
   case 3: return go(k_fed<true, 3>);
