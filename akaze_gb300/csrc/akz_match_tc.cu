@@ -250,7 +250,8 @@ __device__ __forceinline__ void tc_scan32(const uint32_t (&r)[32], uint32_t col0
 
 /* Warp roles: warps 0..7 expand the operands and run the epilogue (warp w
  * owns TMEM lane quarter w % 4 of query half w / 4: its query rows of the
- * operand and its accumulator rows); warp 8 (one lane) issues the MMAs.
+ * operand and its accumulator rows); warp 8 issues the MMAs (the whole warp
+ * runs the loop, elect.sync picks the issuing lane).
  * TMEM: accumulator sets at columns 0..255 (set s, half h: 128 s + 64 h),
  * the expanded queries at 256..511 (half h: 256 + 128 h, 4 K bytes per
  * column).  Tile batch c over the CTA's lifetime uses stage c % 2: train
