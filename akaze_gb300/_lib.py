@@ -32,7 +32,7 @@ EXPORTS = [
     "akz_batch_surrogate_errors", "akz_nndr_homography_inliers", "akz_save_keypoints",
     "akz_batch_detect_describe_packed", "akz_sg_set_tcgen05", "akz_sg_tcgen05_status", "akz_selfcheck_pm_g2",
     "akz_batch_autotune", "akz_batch_set_fed_depth", "akz_batch_submit", "akz_batch_collect_packed",
-    "akz_batch_image_info", "akz_batch_set_nms_round_cap", "akz_selfcheck_bounded_wait", "akz_descriptor_bytes",
+    "akz_batch_image_info", "akz_batch_set_nms_round_cap", "akz_selfcheck_bounded_wait", "akz_selfcheck_matcher_timeout", "akz_descriptor_bytes",
     "akz_matcher_set_tensor_cores", "akz_matcher_tensor_status",
 ]
 
@@ -132,6 +132,7 @@ def load():
         "akz_batch_image_info": ([P, I, IP, IP, IP, ctypes.POINTER(ctypes.c_float)], I),
         "akz_batch_set_nms_round_cap": ([P, I], I),
         "akz_selfcheck_bounded_wait": ([I, I, IP], I),
+        "akz_selfcheck_matcher_timeout": ([I, IP], I),
         "akz_batch_collect_packed": ([P, P, P, I, P, IP], I),
         "akz_sg_infer_level": ([P, P, ctypes.c_size_t, I, I, ctypes.c_float, ctypes.c_float, P, P, P, P, P], I),
     }

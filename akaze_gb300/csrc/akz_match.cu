@@ -101,7 +101,7 @@ __global__ void k_match_merge(const akz_top2 *partial, int nq, int nsplit, int4 
 }
 
 cudaError_t akz_match_tc_launch(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit,
-                                int nsm, cudaStream_t s);
+                                int nsm, cudaStream_t s, int spin, int no_mma);
 cudaError_t akz_match_tc_status(int *timed_out);
 int akz_match_tc_splits(int nq, int nt, int nsm);
 
@@ -125,7 +125,7 @@ cudaError_t akz_match_run(const void *dq, int nq, const void *dt, int nt, void *
     int dev = 0, nsm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = akz_match_tc_launch(dq, nq, dt, nt, dout, partial, nsplit, nsm, s);
+    if (e == cudaSuccess) e = akz_match_tc_launch(dq, nq, dt, nt, dout, partial, nsplit, nsm, s, 0, 0);
     if (e != cudaSuccess || nsplit == 1) return e;
     k_match_merge<<<(nq + 255) / 256, 256, 0, s>>>((const akz_top2 *)partial, nq, nsplit, (int4 *)dout);
     return cudaGetLastError();
@@ -239,6 +239,37 @@ extern "C" AKZ_API akz_status akz_matcher_set_tensor_cores(int on)
 {
   if (on != 0 && on != 1) return akz_report(AKZ_ERR_INVALID_ARG, "akz_matcher_set_tensor_cores: on must be 0 or 1");
   g_akz_match_tc_on = on;
+  return AKZ_OK;
+}
+
+/* Self-check of the tensor-core matcher's failure path: one launch on 256
+ * query and 128 train rows whose MMA warp issues nothing, with `spin` polls
+ * per wait, so the epilogue's wait for the first batch runs out.  The
+ * kernel must flag it, free its tensor memory and return. */
+extern "C" AKZ_API akz_status akz_selfcheck_matcher_timeout(int spin, int *timed_out)
+{
+  if (!timed_out || spin < 1) return akz_report(AKZ_ERR_INVALID_ARG, "akz_selfcheck_matcher_timeout: bad arguments");
+  *timed_out = -1;
+  int v = 0;
+  cudaError_t e = akz_match_tc_status(&v); /* clear a flag left by an earlier call */
+  void *dq = nullptr, *dt = nullptr, *dout = nullptr;
+  const int nq = 256, nt = 128;
+  if (e == cudaSuccess) e = cudaMalloc(&dq, (size_t)nq * 64);
+  if (e == cudaSuccess) e = cudaMalloc(&dt, (size_t)nt * 64);
+  if (e == cudaSuccess) e = cudaMalloc(&dout, (size_t)nq * 2 * sizeof(int4));
+  if (e == cudaSuccess) e = cudaMemset(dq, 0x5a, (size_t)nq * 64);
+  if (e == cudaSuccess) e = cudaMemset(dt, 0xa5, (size_t)nt * 64);
+  int dev = 0, nsm = 0;
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = akz_match_tc_launch(dq, nq, dt, nt, dout, nullptr, 1, nsm, 0, spin, 1);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = akz_match_tc_status(&v);
+  cudaFree(dq);
+  cudaFree(dt);
+  cudaFree(dout);
+  if (e != cudaSuccess) return akz_report(AKZ_ERR_CUDA, cudaGetErrorString(e));
+  *timed_out = v;
   return AKZ_OK;
 }
 

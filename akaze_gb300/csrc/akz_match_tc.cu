@@ -154,9 +154,9 @@ __device__ __forceinline__ void tc_expand_words(const uint32_t (&w)[NW], int r, 
 /* Waits (bounded) for phase `parity` of the mbarrier at mb; gives up early
  * when another thread of the CTA has flagged a failure, and flags one when
  * its own limit runs out. */
-__device__ __forceinline__ bool tc_wait(uint32_t mb, uint32_t parity, volatile int *bad)
+__device__ __forceinline__ bool tc_wait(uint32_t mb, uint32_t parity, volatile int *bad, int spin)
 {
-  for (int it = 0; it < AKZ_TC_SPIN; it++) {
+  for (int it = 0; it < spin; it++) {
     uint32_t done;
     asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
                  : "=r"(done)
@@ -267,7 +267,7 @@ __device__ __forceinline__ void tc_scan32(const uint32_t (&r)[32], uint32_t col0
  * the previous item. */
 __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__restrict__ q, const uint4 *__restrict__ t,
                                                              int nq, int nt, int split_len, int nsplit,
-                                                             akz_tc_top2 *partial, int4 *out)
+                                                             akz_tc_top2 *partial, int4 *out, int spin, int no_mma)
 {
   extern __shared__ __align__(1024) unsigned char tcsm[];
   unsigned char *base = tcsm + ((1024u - ((uint32_t)__cvta_generic_to_shared(tcsm) & 1023u)) & 1023u);
@@ -315,10 +315,11 @@ __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__r
       const int ntile = j1 > j0 ? (j1 - j0 + AKZ_TC_N - 1) / AKZ_TC_N : 0;
       for (int k = 0; k < ntile; k++, c++) {
         const uint32_t st = c % AKZ_TC_STAGES, ph = (c / AKZ_TC_STAGES) & 1u;
-        ok = __all_sync(0xffffffffu, tc_wait(mfull + 8u * st, ph, &sBad));
-        if (ok && c >= AKZ_TC_STAGES) ok = __all_sync(0xffffffffu, tc_wait(mfree + 8u * st, ph ^ 1u, &sBad));
+        ok = __all_sync(0xffffffffu, tc_wait(mfull + 8u * st, ph, &sBad, spin));
+        if (ok && c >= AKZ_TC_STAGES) ok = __all_sync(0xffffffffu, tc_wait(mfree + 8u * st, ph ^ 1u, &sBad, spin));
+        if (no_mma) ok = false; /* self-check: no batch is ever committed */
         if (!ok) {
-          sBad = 1;
+          if (!no_mma) sBad = 1; /* (the self-check leaves the timeout to the epilogue's wait) */
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
@@ -397,7 +398,7 @@ __global__ void __launch_bounds__(AKZ_TC_THREADS, 1) k_match_tc(const uint4 *__r
       auto epilogue = [&](uint32_t cb, int k) -> bool { /* batch cb = tile k of this item */
         const uint32_t st = cb % AKZ_TC_STAGES;
         /* tcgen05.ld is warp-collective: the warp goes on only if every lane saw the batch done */
-        if (!__all_sync(0xffffffffu, tc_wait(mdone + 8u * st, (cb / AKZ_TC_STAGES) & 1u, &sBad))) {
+        if (!__all_sync(0xffffffffu, tc_wait(mdone + 8u * st, (cb / AKZ_TC_STAGES) & 1u, &sBad, spin))) {
           sBad = 1;
           return false;
         }
@@ -502,7 +503,7 @@ int akz_match_tc_splits(int nq, int nt, int nsm)
  * caller merges partial (nq x nsplit records in the popc kernel's akz_top2
  * layout). */
 cudaError_t akz_match_tc_launch(const void *dq, int nq, const void *dt, int nt, void *dout, void *partial, int nsplit,
-                                int nsm, cudaStream_t s)
+                                int nsm, cudaStream_t s, int spin, int no_mma)
 {
   const int split_len = (nt + nsplit - 1) / nsplit;
   if (split_len >= (1 << 21)) return cudaErrorInvalidValue;
@@ -511,8 +512,9 @@ cudaError_t akz_match_tc_launch(const void *dq, int nq, const void *dt, int nt, 
   cudaError_t e =
       cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AKZ_TC_SMEM_LAUNCH);
   if (e != cudaSuccess) return e;
-  k_match_tc<<<grid, AKZ_TC_THREADS, AKZ_TC_SMEM_LAUNCH, s>>>((const uint4 *)dq, (const uint4 *)dt, nq, nt, split_len, nsplit,
-                                                      (akz_tc_top2 *)partial, (int4 *)dout);
+  k_match_tc<<<grid, AKZ_TC_THREADS, AKZ_TC_SMEM_LAUNCH, s>>>((const uint4 *)dq, (const uint4 *)dt, nq, nt, split_len,
+                                                             nsplit, (akz_tc_top2 *)partial, (int4 *)dout,
+                                                             spin > 0 ? spin : AKZ_TC_SPIN, no_mma);
   return cudaGetLastError();
 }
 

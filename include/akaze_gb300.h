@@ -276,6 +276,14 @@ AKZ_API akz_status akz_measure_popc_rate(int iters, double *triples_per_s, void 
  * 0).  Synchronous; no fault, no hang. */
 AKZ_API akz_status akz_selfcheck_bounded_wait(int arrive, int spin, int *timed_out);
 
+/* Self-check of the tensor-core matcher's failure path (no counterpart in
+ * the reference): one launch whose MMA warp issues nothing, with at most
+ * spin polls per wait, so the wait for the first MMA batch runs out.
+ * *timed_out = 1 when the kernel flagged it (and freed its tensor memory);
+ * later matcher calls work as before.  Synchronous; allocates 40 KB; no
+ * fault, no hang. */
+AKZ_API akz_status akz_selfcheck_matcher_timeout(int spin, int *timed_out);
+
 /* ------------------------------------------------------------------------ */
 /* Learned FED surrogate (no counterpart in the reference; it replaces the
  * FED cycle of AKAZE.cpp:244-270 for octaves >= 1 when enabled).  A 5-layer

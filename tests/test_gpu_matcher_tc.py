@@ -89,3 +89,17 @@ def test_few_train_rows_take_the_popc_kernel(gpu_lib, oracle):
     q, t = synth.matcher_rows(32, 20000, 100)
     got = _match(gpu_lib, q, t, True)
     assert got.tobytes() == oracle.bfmatch(q, t).tobytes()
+
+
+def test_tensor_matcher_timeout_is_reported_and_recovers(gpu_lib, oracle):
+    """Failure detection without a fault: a launch whose MMA warp issues
+    nothing makes the epilogue's bounded wait run out; the kernel flags it,
+    frees its tensor memory and returns, and the next calls work."""
+    L = gpu_lib.load()
+    t = ctypes.c_int(-1)
+    assert L.akz_selfcheck_matcher_timeout(1 << 12, ctypes.byref(t)) == 0
+    assert t.value == 1
+    assert _status(gpu_lib) == 0  # read and cleared by the self-check
+    q, tr = synth.matcher_rows(41, 2048, 3000)
+    assert _match(gpu_lib, q, tr, True).tobytes() == oracle.bfmatch(q, tr).tobytes()
+    assert _status(gpu_lib) == 0
