@@ -382,21 +382,26 @@ class Batch:
 
     def submit(self, imgs):
         """First half of detect_describe_packed: enqueues the upload, the
-        graph and the count read-back, and returns at once; the images must
-        stay unchanged until collect_packed."""
-        self._sub = [np.ascontiguousarray(im, np.uint8) for im in imgs]
-        ptrs = (ctypes.c_void_p * self.n)(*[im.ctypes.data for im in self._sub])
-        strides = (ctypes.c_size_t * self.n)(*[im.strides[0] for im in self._sub])
+        graph, the device-side packing and the count read-back, and returns
+        at once.  Up to two runs may be outstanding; the images of a run must
+        stay unchanged until it is collected."""
+        sub = [np.ascontiguousarray(im, np.uint8) for im in imgs]
+        ptrs = (ctypes.c_void_p * self.n)(*[im.ctypes.data for im in sub])
+        strides = (ctypes.c_size_t * self.n)(*[im.strides[0] for im in sub])
         check(self._lib.akz_batch_submit(self._h, ptrs, strides))
+        self._subs = getattr(self, "_subs", []) + [sub]  # kept until collected
 
     def collect_packed(self, kp_out, d_out):
-        """Second half: waits for this batch, writes its results packed into
-        kp_out / d_out; returns (per-image counts, total)."""
+        """Second half: waits for the oldest submitted run of this batch,
+        writes its results packed into kp_out / d_out; returns (per-image
+        counts, total)."""
         counts = np.zeros(self.n, np.int32)
         total = ctypes.c_int()
-        check(self._lib.akz_batch_collect_packed(self._h, _ptr(kp_out), _ptr(d_out), len(kp_out), _ptr(counts),
-                                                 ctypes.byref(total)))
-        self._sub = None
+        try:
+            check(self._lib.akz_batch_collect_packed(self._h, _ptr(kp_out), _ptr(d_out), len(kp_out), _ptr(counts),
+                                                     ctypes.byref(total)))
+        finally:
+            self._subs = getattr(self, "_subs", [])[1:]
         return counts, total.value
 
     def plane(self, i, level, name="Lt", shape=None):
@@ -474,13 +479,17 @@ class BatchGroup:
 
     def detect_describe_packed_steps(self, steps, kp_out, d_out, on_step=None):
         """Several whole-job calls in a row (`steps`: one image list per
-        step), pipelined: group g's next step is submitted as soon as its
-        current one is collected, while the other groups are still running.
-        Each step's results are packed into kp_out / d_out (overwritten by
-        the next step); on_step(step_index, counts), if given, runs after a
-        step is collected.  Returns the last step's per-image counts."""
-        for g, b in enumerate(self.parts):
-            b.submit(steps[0][self.bounds[g]:self.bounds[g + 1]])
+        step), pipelined two deep: every group has its next step submitted
+        while its current one computes, and a step is collected (packed
+        results copied out beside the next step's graph) before the step
+        after the next is submitted.  Each step's results are packed into
+        kp_out / d_out (overwritten by the next step); on_step(step_index,
+        counts), if given, runs after a step is collected.  Returns the last
+        step's per-image counts."""
+        part = lambda si, g: steps[si][self.bounds[g]:self.bounds[g + 1]]
+        for si in range(min(2, len(steps))):
+            for g, b in enumerate(self.parts):
+                b.submit(part(si, g))
         counts = None
         for si in range(len(steps)):
             at, parts = 0, []
@@ -488,8 +497,8 @@ class BatchGroup:
                 c, n = b.collect_packed(kp_out[at:], d_out[at:])
                 parts.append(c)
                 at += n
-                if si + 1 < len(steps):
-                    b.submit(steps[si + 1][self.bounds[g]:self.bounds[g + 1]])
+                if si + 2 < len(steps):
+                    b.submit(part(si + 2, g))
             counts = np.concatenate(parts)
             if on_step:
                 on_step(si, counts)

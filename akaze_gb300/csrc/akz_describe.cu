@@ -463,28 +463,51 @@ cudaError_t akz_launch_describe(const akz_describe_params &p, int nblocks, cudaS
 
 /* Packs every image's keypoints and descriptor rows (rb <= 64 bytes each)
  * contiguously (image i at offset sum_{j<i} nkp_j): blockIdx.x is the image,
- * blockIdx.y a slice of its rows; a thread copies whole rows. */
+ * blockIdx.y a slice of its words.  The keypoint records are copied as
+ * words; the descriptor rows are written as the 4-byte words of the packed
+ * byte stream, consecutive threads on consecutive words (coalesced), each
+ * word gathered from the one or two 64-byte source rows it spans.  An
+ * image's first and last words may hold its neighbours' bytes too: those
+ * two go byte by byte, every byte by the CTAs of its own image. */
 __global__ void k_pack_results(akz_tables t, const akz_kp *kp, const uint32_t *desc, akz_kp *kp_out, uint8_t *desc_out,
                                int rb)
 {
+  static_assert(sizeof(akz_kp) % 4 == 0, "keypoint records are whole words");
+  constexpr int KW = sizeof(akz_kp) / 4;
   const int img = blockIdx.x;
-  int off = 0;
+  long long off = 0;
   for (int j = 0; j < img; j++) off += t.stats[j].nkp;
   const int n = t.stats[img].nkp;
+  if (n <= 0) return;
   const akz_image_desc I = t.im[img];
-  for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < n; k += gridDim.y * blockDim.x) {
-    kp_out[off + k] = kp[I.kp_base + k];
-    const uint4 *src = (const uint4 *)(desc + (long long)(I.kp_base + k) * 16);
-    __align__(16) uint8_t row[64];
-    uint4 *rw = (uint4 *)row;
+  const long long tid = (long long)blockIdx.y * blockDim.x + threadIdx.x, nt = (long long)gridDim.y * blockDim.x;
+  const uint32_t *ks = reinterpret_cast<const uint32_t *>(kp + I.kp_base);
+  uint32_t *kd = reinterpret_cast<uint32_t *>(kp_out + off);
+  for (long long w = tid; w < (long long)n * KW; w += nt) kd[w] = ks[w];
+  const uint8_t *ds = reinterpret_cast<const uint8_t *>(desc) + (long long)I.kp_base * 64;
+  const long long b0 = off * rb, b1 = b0 + (long long)n * rb; /* this image's bytes of the stream */
+  for (long long w = (b0 >> 2) + tid; w < (b1 + 3) >> 2; w += nt) {
+    const long long b = w << 2;
+    if (b >= b0 && b + 4 <= b1) {
+      long long r = (b - b0) / rb;
+      int c = (int)(b - b0 - r * rb);
+      uint32_t v = 0;
 #pragma unroll
-    for (int c = 0; c < 4; c++) rw[c] = src[c];
-    uint8_t *dst = desc_out + (long long)(off + k) * rb;
-    if (rb == 61) {
-#pragma unroll
-      for (int c = 0; c < 61; c++) dst[c] = row[c];
+      for (int k = 0; k < 4; k++) {
+        v |= (uint32_t)ds[r * 64 + c] << (8 * k);
+        if (++c == rb) {
+          c = 0;
+          r++;
+        }
+      }
+      reinterpret_cast<uint32_t *>(desc_out)[w] = v;
     } else {
-      for (int c = 0; c < rb; c++) dst[c] = row[c];
+      for (int k = 0; k < 4; k++) {
+        const long long bb = b + k;
+        if (bb < b0 || bb >= b1) continue;
+        const long long r = (bb - b0) / rb;
+        desc_out[bb] = ds[r * 64 + (bb - b0 - r * rb)];
+      }
     }
   }
 }
@@ -493,6 +516,7 @@ cudaError_t akz_launch_pack_results(const akz_tables &t, const akz_kp *kp, const
                                     uint8_t *desc_out, int row_bytes, cudaStream_t s)
 {
   if (row_bytes < 1 || row_bytes > 64) return cudaErrorInvalidValue;
+  if (((uintptr_t)kp_out | (uintptr_t)desc_out) & 3) return cudaErrorInvalidValue; /* word stores */
   k_pack_results<<<dim3(t.nimg, 8), 256, 0, s>>>(t, kp, desc, kp_out, desc_out, row_bytes);
   return cudaGetLastError();
 }

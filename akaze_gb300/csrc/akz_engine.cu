@@ -433,19 +433,40 @@ struct akz_batch {
   unsigned char *d_nbc = nullptr;
   unsigned char *d_cmp = nullptr; /* M-LDB bit table: 512 first then 512 second value indices */
   int nbits = 486, row_bytes = 61;
-  void *d_pack = nullptr; /* packed results of akz_batch_collect_packed, grown on demand */
-  bool submitted = false; /* akz_batch_submit issued, akz_batch_collect_packed not yet */
-  size_t cap_pack = 0;    /* rows */
+  /* akz_batch_submit / akz_batch_collect_packed: two result slots, each with
+   * the packed keypoints and descriptor rows of one submitted run (room for
+   * every image at its keypoint capacity), its counts read back into pinned
+   * memory, and an event; up to two runs outstanding, collected in order */
+  void *d_slot[2] = {nullptr, nullptr};
+  akz_image_stats *h_slot_stats[2] = {nullptr, nullptr};
+  cudaEvent_t ev_slot[2] = {nullptr, nullptr};
+  cudaStream_t copy_stream = nullptr;
+  /* submitted runs alternate between two input staging buffers (the
+   * arena's and d_stage2), each with its own graph: a run's images go up on
+   * up_stream while the run before it computes */
+  uint8_t *d_stage2 = nullptr;
+  cudaStream_t up_stream = nullptr;
+  cudaEvent_t ev_stage_full[2] = {nullptr, nullptr}, ev_stage_free[2] = {nullptr, nullptr};
+  int stage_next = 0;
+  bool slots_ready = false;
+  int sub_first = 0, sub_n = 0; /* slot of the oldest outstanding run, runs outstanding */
   size_t raw_all = 0;
   int input_f32 = 0;
   cudaStream_t stream = nullptr, own_stream = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  int graph_f32 = -1;
-  cudaStream_t graph_stream = nullptr;
+  /* captured graphs of the whole run, one per input staging buffer (0: the
+   * arena's, 1: the submit path's second one), for the input kind and
+   * stream they were captured with */
+  struct akz_graph_entry {
+    cudaGraphExec_t g = nullptr;
+    int f32 = -1;
+    cudaStream_t s = nullptr;
+  };
+  akz_graph_entry graphs[2];
+  uint8_t *u8_arena = nullptr; /* the arena's staging buffer (u8 points to it outside akz_batch_submit) */
   akz_image_stats *h_stats = nullptr;
   int nsm = 152;
   int nms_round_cap = 1 << 20; /* suppression rounds before AKZ_ERR_TIMEOUT */
-  cudaEvent_t ev[9] = {}; /* 0-7 stage timing, 8 submit/collect */
+  cudaEvent_t ev[8] = {}; /* stage timing */
 };
 
 static size_t akz_align(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -467,13 +488,22 @@ static akz_tables akz_make_tables(const akz_batch *b)
 static void akz_batch_free(akz_batch *b)
 {
   if (!b) return;
-  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (auto &ge : b->graphs)
+    if (ge.g) cudaGraphExecDestroy(ge.g);
   if (b->arena) cudaFree(b->arena);
-  for (void *q : {(void *)b->d_sg_w, b->d_sg_scratch, (void *)b->d_sg_b, (void *)b->d_sg_chk, (void *)b->d_sg_err, b->d_pack,
-                  b->d_tmaps})
+  for (void *q : {(void *)b->d_sg_w, b->d_sg_scratch, (void *)b->d_sg_b, (void *)b->d_sg_chk, (void *)b->d_sg_err,
+                  b->d_slot[0], b->d_slot[1], (void *)b->d_stage2, b->d_tmaps})
     if (q) cudaFree(q);
   if (b->f32) cudaFree(b->f32);
   if (b->h_stats) cudaFreeHost(b->h_stats);
+  for (int k = 0; k < 2; k++) {
+    if (b->h_slot_stats[k]) cudaFreeHost(b->h_slot_stats[k]);
+    if (b->ev_slot[k]) cudaEventDestroy(b->ev_slot[k]);
+  }
+  if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
+  if (b->up_stream) cudaStreamDestroy(b->up_stream);
+  for (cudaEvent_t e : {b->ev_stage_full[0], b->ev_stage_full[1], b->ev_stage_free[0], b->ev_stage_free[1]})
+    if (e) cudaEventDestroy(e);
   for (auto &e : b->ev)
     if (e) cudaEventDestroy(e);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
@@ -836,6 +866,7 @@ static akz_status akz_batch_build(const akz_options *opt, int n, const int *Ws, 
   char *a = b->arena;
   b->planes = (float *)(a + o_planes);
   b->u8 = (uint8_t *)(a + o_u8);
+  b->u8_arena = b->u8;
   b->d_lv = (akz_level_desc *)(a + o_lv);
   b->d_im = (akz_image_desc *)(a + o_im);
   b->d_stats = (akz_image_stats *)(a + o_stats);
@@ -1081,14 +1112,24 @@ static akz_status akz_run_all(akz_batch *b, cudaStream_t s)
 }
 
 /* Whole-batch run, captured once into a CUDA graph and replayed. */
+/* drops the captured graphs (after a change of the launches they hold) */
+static void akz_drop_graphs(akz_batch *b)
+{
+  for (auto &ge : b->graphs) {
+    if (ge.g) cudaGraphExecDestroy(ge.g);
+    ge.g = nullptr;
+  }
+}
+
 static akz_status akz_batch_launch(akz_batch *b)
 {
   cudaStream_t s = b->stream;
-  if (b->graph && (b->graph_f32 != b->input_f32 || b->graph_stream != s)) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
+  akz_batch::akz_graph_entry &ge = b->graphs[b->u8 == b->u8_arena ? 0 : 1];
+  if (ge.g && (ge.f32 != b->input_f32 || ge.s != s)) {
+    cudaGraphExecDestroy(ge.g);
+    ge.g = nullptr;
   }
-  if (!b->graph) {
+  if (!ge.g) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     akz_status st = akz_run_all(b, s);
@@ -1098,16 +1139,16 @@ static akz_status akz_batch_launch(akz_batch *b)
       return st;
     }
     if (e != cudaSuccess) return akz_fail_cuda(e, "cudaStreamEndCapture", __FILE__, __LINE__);
-    e = cudaGraphInstantiate(&b->graph, g, 0);
+    e = cudaGraphInstantiate(&ge.g, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
-      b->graph = nullptr;
+      ge.g = nullptr;
       return akz_fail_cuda(e, "cudaGraphInstantiate", __FILE__, __LINE__);
     }
-    b->graph_f32 = b->input_f32;
-    b->graph_stream = s;
+    ge.f32 = b->input_f32;
+    ge.s = s;
   }
-  CK(cudaGraphLaunch(b->graph, s));
+  CK(cudaGraphLaunch(ge.g, s));
   return AKZ_OK;
 }
 
@@ -1540,12 +1581,56 @@ AKZ_API akz_status akz_batch_image_info(akz_batch *b, int i, int *nraw, int *nkp
 AKZ_API akz_status akz_batch_submit(akz_batch *b, const uint8_t *const *images, const size_t *strides)
 {
   AKZ_GUARD(b);
-  akz_status st = akz_batch_upload(b, images, strides, 0);
-  if (st == AKZ_OK) st = akz_batch_launch(b);
+  if (b->sub_n == 2) return akz_fail(AKZ_ERR_STATE, "akz_batch_submit: two runs outstanding, collect one first");
+  if (!b->slots_ready) { /* first use */
+    const size_t bytes = b->raw_all * (sizeof(akz_kp) + (size_t)b->row_bytes);
+    for (int k = 0; k < 2; k++) {
+      if (!b->d_slot[k]) CK(cudaMalloc(&b->d_slot[k], std::max<size_t>(bytes, 1)));
+      if (!b->h_slot_stats[k]) CK(cudaMallocHost(&b->h_slot_stats[k], (size_t)b->nimg * sizeof(akz_image_stats)));
+      if (!b->ev_slot[k]) CK(cudaEventCreateWithFlags(&b->ev_slot[k], cudaEventDisableTiming));
+    }
+    if (!b->copy_stream) CK(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+    if (!b->up_stream) CK(cudaStreamCreateWithFlags(&b->up_stream, cudaStreamNonBlocking));
+    if (!b->d_stage2) CK(cudaMalloc(&b->d_stage2, std::max<size_t>(b->staging_elems, 1)));
+    for (int k = 0; k < 2; k++) {
+      if (!b->ev_stage_full[k]) CK(cudaEventCreateWithFlags(&b->ev_stage_full[k], cudaEventDisableTiming));
+      if (!b->ev_stage_free[k]) CK(cudaEventCreateWithFlags(&b->ev_stage_free[k], cudaEventDisableTiming));
+    }
+    b->slots_ready = true;
+  }
+  if (!images || !strides) return akz_fail(AKZ_ERR_INVALID_ARG, "images/strides are NULL");
+  for (int i = 0; i < b->nimg; i++)
+    if (!images[i] || strides[i] < (size_t)b->W[i]) return akz_fail(AKZ_ERR_INVALID_ARG, "image %d: bad pointer or stride", i);
+  const int slot = (b->sub_first + b->sub_n) & 1;
+  /* the host images go up into staging buffer q once the graph that last
+   * read it (two runs back) is done, beside the previous run's graph; this
+   * run's graph, captured for buffer q, waits for them and, in the batch's
+   * stream order, for the previous run's pack, which has read the keypoints
+   * and descriptors */
+  const int q = b->stage_next;
+  uint8_t *stage = q ? b->d_stage2 : b->u8_arena;
+  CK(cudaStreamWaitEvent(b->up_stream, b->ev_stage_free[q], 0));
+  for (int i = 0; i < b->nimg; i++) {
+    const akz_image_desc &I = b->im[i];
+    CK(cudaMemcpy2DAsync(stage + I.u8_off, I.u8_pitch, images[i], strides[i], b->W[i], b->H[i], cudaMemcpyHostToDevice,
+                         b->up_stream));
+  }
+  CK(cudaEventRecord(b->ev_stage_full[q], b->up_stream));
+  CK(cudaStreamWaitEvent(b->stream, b->ev_stage_full[q], 0));
+  b->input_f32 = 0;
+  b->u8 = stage;
+  const akz_status st = akz_batch_launch(b);
+  b->u8 = b->u8_arena;
   if (st != AKZ_OK) return st;
-  CK(cudaMemcpyAsync(b->h_stats, b->d_stats, (size_t)b->nimg * sizeof(akz_image_stats), cudaMemcpyDeviceToHost, b->stream));
-  CK(cudaEventRecord(b->ev[8], b->stream));
-  b->submitted = true;
+  CK(cudaEventRecord(b->ev_stage_free[q], b->stream));
+  b->stage_next = q ^ 1;
+  akz_kp *pk = (akz_kp *)b->d_slot[slot];
+  uint8_t *pd = (uint8_t *)(pk + b->raw_all);
+  CK(akz_launch_pack_results(akz_make_tables(b), b->d_kp, b->d_desc, pk, pd, b->row_bytes, b->stream));
+  CK(cudaMemcpyAsync(b->h_slot_stats[slot], b->d_stats, (size_t)b->nimg * sizeof(akz_image_stats), cudaMemcpyDeviceToHost,
+                     b->stream));
+  CK(cudaEventRecord(b->ev_slot[slot], b->stream));
+  b->sub_n++;
   return AKZ_OK;
 }
 
@@ -1554,37 +1639,32 @@ AKZ_API akz_status akz_batch_collect_packed(akz_batch *b, akz_keypoint *kpts, ui
 {
   AKZ_GUARD(b);
   if (!counts || !total || capacity < 0) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_batch_collect_packed: bad arguments");
-  if (!b->submitted) return akz_fail(AKZ_ERR_STATE, "akz_batch_collect_packed: nothing submitted");
-  b->submitted = false;
-  CK(cudaEventSynchronize(b->ev[8]));
+  if (b->sub_n == 0) return akz_fail(AKZ_ERR_STATE, "akz_batch_collect_packed: nothing submitted");
+  const int slot = b->sub_first;
+  b->sub_first ^= 1;
+  b->sub_n--;
+  CK(cudaEventSynchronize(b->ev_slot[slot]));
+  const akz_image_stats *hs = b->h_slot_stats[slot];
   for (int i = 0; i < b->nimg; i++) {
-    if (b->h_stats[i].overflow)
-      return akz_fail(AKZ_ERR_OVERFLOW, "image %d: %d raw extrema exceed maxkeypoints=%d", i, b->h_stats[i].nraw, b->opt.maxkeypoints);
-    if (b->h_stats[i].status == AKZ_ERR_TIMEOUT) return akz_fail(AKZ_ERR_TIMEOUT, "image %d: suppression did not settle", i);
+    if (hs[i].overflow)
+      return akz_fail(AKZ_ERR_OVERFLOW, "image %d: %d raw extrema exceed maxkeypoints=%d", i, hs[i].nraw, b->opt.maxkeypoints);
+    if (hs[i].status == AKZ_ERR_TIMEOUT) return akz_fail(AKZ_ERR_TIMEOUT, "image %d: suppression did not settle", i);
   }
   long long n = 0;
   for (int i = 0; i < b->nimg; i++) {
-    counts[i] = b->h_stats[i].nkp;
+    counts[i] = hs[i].nkp;
     n += counts[i];
   }
   *total = (int)n;
   if (n > capacity)
     return akz_fail(AKZ_ERR_OVERFLOW, "akz_batch_collect_packed: %lld keypoints exceed the capacity %d", n, capacity);
   if (n == 0) return AKZ_OK;
-  if ((size_t)n > b->cap_pack) {
-    if (b->d_pack) cudaFree(b->d_pack);
-    b->d_pack = nullptr;
-    b->cap_pack = 0;
-    const size_t rows = (size_t)n + (size_t)n / 4;
-    CK(cudaMalloc(&b->d_pack, rows * (sizeof(akz_kp) + 64)));
-    b->cap_pack = rows;
-  }
-  akz_kp *pk = (akz_kp *)b->d_pack;
-  uint8_t *pd = (uint8_t *)(pk + b->cap_pack);
-  CK(akz_launch_pack_results(akz_make_tables(b), b->d_kp, b->d_desc, pk, pd, b->row_bytes, b->stream));
-  if (kpts) CK(cudaMemcpyAsync(kpts, pk, (size_t)n * sizeof(akz_kp), cudaMemcpyDeviceToHost, b->stream));
-  if (desc) CK(cudaMemcpyAsync(desc, pd, (size_t)n * b->row_bytes, cudaMemcpyDeviceToHost, b->stream));
-  CK(cudaStreamSynchronize(b->stream));
+  /* on the copy stream, beside the next run's graph */
+  const akz_kp *pk = (const akz_kp *)b->d_slot[slot];
+  const uint8_t *pd = (const uint8_t *)(pk + b->raw_all);
+  if (kpts) CK(cudaMemcpyAsync(kpts, pk, (size_t)n * sizeof(akz_kp), cudaMemcpyDeviceToHost, b->copy_stream));
+  if (desc) CK(cudaMemcpyAsync(desc, pd, (size_t)n * b->row_bytes, cudaMemcpyDeviceToHost, b->copy_stream));
+  CK(cudaStreamSynchronize(b->copy_stream));
   return AKZ_OK;
 }
 
@@ -1594,6 +1674,7 @@ AKZ_API akz_status akz_batch_detect_describe_packed(akz_batch *b, const uint8_t 
 {
   AKZ_GUARD(b);
   if (!counts || !total || capacity < 0) return akz_fail(AKZ_ERR_INVALID_ARG, "akz_batch_detect_describe_packed: bad arguments");
+  if (b->sub_n) return akz_fail(AKZ_ERR_STATE, "akz_batch_detect_describe_packed: a submitted run is not collected");
   const akz_status st = akz_batch_submit(b, images, strides);
   if (st != AKZ_OK) return st;
   return akz_batch_collect_packed(b, kpts, desc, capacity, counts, total);
@@ -1759,10 +1840,7 @@ AKZ_API akz_status akz_matcher_bfmatch_device(akz_matcher *m, const uint8_t *q64
 static void akz_use_fed_depths(akz_batch *b)
 {
   for (int l = 1; l < b->maxlev; l++) b->fed[l] = b->fed_alt[b->fed_depth[l] - AKZ_DEPTH_MIN][l];
-  if (b->graph) { /* the captured graph holds the old launches */
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  akz_drop_graphs(b); /* the captured graphs hold the old launches */
 }
 
 AKZ_API akz_status akz_batch_set_nms_round_cap(akz_batch *b, int cap)
@@ -1770,10 +1848,7 @@ AKZ_API akz_status akz_batch_set_nms_round_cap(akz_batch *b, int cap)
   AKZ_GUARD(b);
   if (cap < 1) return akz_report(AKZ_ERR_INVALID_ARG, "akz_batch_set_nms_round_cap: cap must be >= 1");
   b->nms_round_cap = cap;
-  if (b->graph) { /* the captured graph holds the old cap */
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  akz_drop_graphs(b); /* the captured graphs hold the old cap */
   return AKZ_OK;
 }
 
@@ -1839,10 +1914,7 @@ AKZ_API akz_status akz_batch_set_surrogate(akz_batch *b, const uint16_t *weights
                                            int first_octave, float check_tol)
 {
   AKZ_GUARD(b);
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  akz_drop_graphs(b);
   if (!weights_bf16) {
     b->sg_on = 0;
     return AKZ_OK;

@@ -29,6 +29,12 @@ import sys
 import threading
 import time
 
+# Every group of the batch runs on three streams (compute, upload, result
+# copy); with the driver's default number of hardware queues, streams share
+# queues and the group streams wait behind one another's copies (end to end
+# about 3% slower).  It must be set before the CUDA context exists.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))

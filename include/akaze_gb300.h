@@ -367,13 +367,19 @@ AKZ_API akz_status akz_batch_image_info(akz_batch *b, int i, int *nraw, int *nkp
 AKZ_API akz_status akz_batch_set_nms_round_cap(akz_batch *b, int cap);
 
 /* The two halves of akz_batch_detect_describe_packed, for overlapping
- * several batches (each on its own stream) from one host thread:
- * akz_batch_submit enqueues the upload of the host images, the batch's
- * graph and the read-back of the per-image counts, and returns at once;
- * akz_batch_collect_packed waits for that batch only, then packs and copies
- * its keypoints and descriptors as akz_batch_detect_describe_packed does.
- * A collect without a submit is AKZ_ERR_STATE; the host images must stay
- * unchanged until the collect returns. */
+ * several batches (each on its own stream) and consecutive runs of one
+ * batch from one host thread: akz_batch_submit enqueues the upload of the
+ * host images, the batch's graph, the packing of its keypoints and
+ * descriptor rows on the device and the read-back of the per-image counts,
+ * and returns at once; akz_batch_collect_packed waits for the oldest
+ * submitted run only and copies its packed results (on a copy stream of
+ * the batch, so that a run submitted after it keeps computing).  Up to two
+ * runs may be outstanding: the second one's upload and graph queue behind
+ * the first on the batch's stream.  A third submit, or a collect without a
+ * submit, is AKZ_ERR_STATE; akz_batch_detect_describe_packed needs no run
+ * outstanding.  The host images of a run must stay unchanged until it is
+ * collected.  The first submit allocates two result slots of maxkeypoints
+ * rows per image (keypoint record + descriptor row each). */
 AKZ_API akz_status akz_batch_submit(akz_batch *b, const uint8_t *const *images, const size_t *strides);
 AKZ_API akz_status akz_batch_collect_packed(akz_batch *b, akz_keypoint *kpts, uint8_t *desc, int capacity, int *counts,
                                             int *total);

@@ -119,16 +119,22 @@ def test_uneven_batch_equals_single_images(gpu_lib, oracle):
         assert np.array_equal(d, od), (i, w, h)
 
 
-def test_packed_output_equals_per_image_results(gpu_lib):
+@pytest.mark.parametrize("opts,rb", [({}, 61), ({"descriptor_channels": 1}, 21), ({"descriptor_size": 100}, 13),
+                                     ({"descriptor_size": 64}, 8)])
+def test_packed_output_equals_per_image_results(gpu_lib, opts, rb):
+    """Packed rows of every width: word stores of the packed byte stream,
+    images meeting inside a word."""
     sizes = synth.uneven_sizes(9, 5)
     imgs = [synth.synth_image(900 + i, w, h) for i, (w, h) in enumerate(sizes)]
-    b = gpu_lib.Batch(gpu_lib.AKAZEOptions(), sizes)
+    o = gpu_lib.AKAZEOptions(**opts)
+    assert gpu_lib.descriptor_bytes(o) == rb
+    b = gpu_lib.Batch(o, sizes)
     b.upload(imgs)
     b.run()
     per = [b.results(i) for i in range(len(sizes))]
     total = sum(len(k) for k, _ in per)
     kp = np.zeros(total, gpu_lib.KEYPOINT_DTYPE)
-    d = np.zeros((total, 61), np.uint8)
+    d = np.zeros((total, rb), np.uint8)
     counts = b.detect_describe_packed(imgs, kp, d)
     assert list(counts) == [len(k) for k, _ in per]
     off = 0
@@ -219,3 +225,35 @@ def test_batch_group_pipelined_steps(gpu_lib):
     grp.detect_describe_packed_steps([a, b, a], kp, d, on_step=keep)
     for (wc, wk, wd), (gc, gk, gd) in zip(want + [want[0]], got):
         assert np.array_equal(wc, gc) and wk == gk and np.array_equal(wd, gd)
+
+
+def test_two_runs_outstanding(gpu_lib):
+    """submit, submit, collect, collect: each collect returns its own run's
+    results, in order; a third submit, a whole-job call with a run
+    outstanding and a collect with none are refused."""
+    sizes = synth.uneven_sizes(19, 3)
+    a = [synth.synth_image(1900 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    b = [synth.synth_image(1950 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    bt = gpu_lib.Batch(gpu_lib.AKAZEOptions(), sizes)
+    cap = 200000
+    kp = np.zeros(cap, gpu_lib.KEYPOINT_DTYPE)
+    d = np.zeros((cap, 61), np.uint8)
+    want = []
+    for imgs in (a, b):
+        c = bt.detect_describe_packed(imgs, kp, d)
+        n = int(c.sum())
+        want.append((c.copy(), kp[:n].tobytes(), d[:n].copy()))
+    assert want[0][1] != want[1][1]
+    bt.submit(a)
+    bt.submit(b)
+    with pytest.raises(gpu_lib.AkazeError):
+        bt.submit(a)
+    with pytest.raises(gpu_lib.AkazeError):
+        bt.detect_describe_packed(a, kp, d)
+    for wc, wk, wd in want:
+        c, n = bt.collect_packed(kp, d)
+        assert np.array_equal(c, wc) and kp[:n].tobytes() == wk and np.array_equal(d[:n], wd)
+    with pytest.raises(gpu_lib.AkazeError):
+        bt.collect_packed(kp, d)
+    c = bt.detect_describe_packed(b, kp, d)  # usable again
+    assert np.array_equal(c, want[1][0])
