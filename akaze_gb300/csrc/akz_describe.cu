@@ -517,6 +517,8 @@ cudaError_t akz_launch_pack_results(const akz_tables &t, const akz_kp *kp, const
 {
   if (row_bytes < 1 || row_bytes > 64) return cudaErrorInvalidValue;
   if (((uintptr_t)kp_out | (uintptr_t)desc_out) & 3) return cudaErrorInvalidValue; /* word stores */
-  k_pack_results<<<dim3(t.nimg, 8), 256, 0, s>>>(t, kp, desc, kp_out, desc_out, row_bytes);
+  /* 64 slices per image: a few words per thread, so the gathers of a
+   * thread's loop iterations do not queue behind one another */
+  k_pack_results<<<dim3(t.nimg, 64), 256, 0, s>>>(t, kp, desc, kp_out, desc_out, row_bytes);
   return cudaGetLastError();
 }
