@@ -379,7 +379,9 @@ AKZ_API akz_status akz_batch_set_nms_round_cap(akz_batch *b, int cap);
  * submit, is AKZ_ERR_STATE; akz_batch_detect_describe_packed needs no run
  * outstanding.  The host images of a run must stay unchanged until it is
  * collected.  The first submit allocates two result slots of maxkeypoints
- * rows per image (keypoint record + descriptor row each). */
+ * rows per image (keypoint record + descriptor row each) and a second input
+ * staging buffer: consecutive runs alternate between the two, each with its
+ * own captured graph, so that a run's upload overlaps the run before it. */
 AKZ_API akz_status akz_batch_submit(akz_batch *b, const uint8_t *const *images, const size_t *strides);
 AKZ_API akz_status akz_batch_collect_packed(akz_batch *b, akz_keypoint *kpts, uint8_t *desc, int capacity, int *counts,
                                             int *total);
