@@ -391,6 +391,17 @@ class Batch:
         check(self._lib.akz_batch_submit(self._h, ptrs, strides))
         self._subs = getattr(self, "_subs", []) + [sub]  # kept until collected
 
+    def discard_outstanding(self):
+        """Waits for and drops every submitted run not yet collected (after
+        an error part way through a pipeline)."""
+        kp = np.zeros(0, KEYPOINT_DTYPE)
+        d = np.zeros((0, max(descriptor_bytes(self.options), 1)), np.uint8)
+        while getattr(self, "_subs", []):
+            try:
+                self.collect_packed(kp, d)
+            except AkazeError:
+                pass  # the run is dropped whatever the collect reports
+
     def collect_packed(self, kp_out, d_out):
         """Second half: waits for the oldest submitted run of this batch,
         writes its results packed into kp_out / d_out; returns (per-image
@@ -487,21 +498,26 @@ class BatchGroup:
         counts), if given, runs after a step is collected.  Returns the last
         step's per-image counts."""
         part = lambda si, g: steps[si][self.bounds[g]:self.bounds[g + 1]]
-        for si in range(min(2, len(steps))):
-            for g, b in enumerate(self.parts):
-                b.submit(part(si, g))
         counts = None
-        for si in range(len(steps)):
-            at, parts = 0, []
-            for g, b in enumerate(self.parts):
-                c, n = b.collect_packed(kp_out[at:], d_out[at:])
-                parts.append(c)
-                at += n
-                if si + 2 < len(steps):
-                    b.submit(part(si + 2, g))
-            counts = np.concatenate(parts)
-            if on_step:
-                on_step(si, counts)
+        try:
+            for si in range(min(2, len(steps))):
+                for g, b in enumerate(self.parts):
+                    b.submit(part(si, g))
+            for si in range(len(steps)):
+                at, parts = 0, []
+                for g, b in enumerate(self.parts):
+                    c, n = b.collect_packed(kp_out[at:], d_out[at:])
+                    parts.append(c)
+                    at += n
+                    if si + 2 < len(steps):
+                        b.submit(part(si + 2, g))
+                counts = np.concatenate(parts)
+                if on_step:
+                    on_step(si, counts)
+        except BaseException:
+            for b in self.parts:  # leave every group usable
+                b.discard_outstanding()
+            raise
         return counts
 
 

@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile-e2e", action="store_true",
+                    help="run two pipelined end-to-end steps of the headline batch (pinned host images in, "
+                         "packed results out) and print the counts, for an ncu launch list of the per-run kernels")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: --batch images, one graph-less run of every stage, no timing line")
     ap.add_argument("--weights", default=os.path.join(ROOT, "akaze_gb300", "surrogate_weights.npz"),
@@ -573,6 +576,19 @@ def main():
     B, W, H = args.batch, args.width, args.height
     imgs = [synth.synth_image(s, W, H) for s in replicas.rank_seeds(rank, B)]
     opt = akz.AKAZEOptions(fast_math=1 if args.arith == "fused" else 0)
+    if args.profile_e2e:
+        batch = akz.BatchGroup(opt, [(W, H)] * B, groups=args.groups)
+        _pick_fed_depth(batch, args, "8")
+        pin = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(B)]
+        for pp, im in zip(pin, imgs):
+            pp.numpy()[:] = im
+        cap = B * 20000
+        kp_out = torch.empty(cap * 28, dtype=torch.uint8).pin_memory().numpy().view(akz.KEYPOINT_DTYPE)
+        d_out = torch.empty(cap * 61, dtype=torch.uint8).pin_memory().numpy().reshape(cap, 61)
+        c = batch.detect_describe_packed_steps([[pp.numpy() for pp in pin]] * 2, kp_out, d_out)
+        print(json.dumps({"profile_e2e": f"{B} x {W}x{H}, {len(batch.parts)} groups, 2 steps",
+                          "keypoints": int(c.sum())}))
+        return 0
     if args.profile_case:
         batch = akz.Batch(opt, [(W, H)] * B)
         batch.upload(imgs)

@@ -257,3 +257,20 @@ def test_two_runs_outstanding(gpu_lib):
         bt.collect_packed(kp, d)
     c = bt.detect_describe_packed(b, kp, d)  # usable again
     assert np.array_equal(c, want[1][0])
+
+
+def test_pipelined_steps_recover_from_a_failed_collect(gpu_lib):
+    """An output buffer too small for a step raises; the runs still in
+    flight are dropped, and the group then works as before."""
+    sizes = synth.uneven_sizes(23, 4)
+    a = [synth.synth_image(2300 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    grp = gpu_lib.BatchGroup(gpu_lib.AKAZEOptions(), sizes, groups=2)
+    cap = 200000
+    kp = np.zeros(cap, gpu_lib.KEYPOINT_DTYPE)
+    d = np.zeros((cap, 61), np.uint8)
+    want = grp.detect_describe_packed(a, kp, d).copy()
+    assert want.sum() > 2
+    with pytest.raises(gpu_lib.AkazeError):
+        grp.detect_describe_packed_steps([a, a, a], kp[:1], d[:1])
+    assert all(not getattr(b, "_subs", []) for b in grp.parts)
+    assert np.array_equal(grp.detect_describe_packed(a, kp, d), want)
