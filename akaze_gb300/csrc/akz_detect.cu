@@ -14,7 +14,7 @@
  *              extrema come out in (level, y, x) order, which is the order
  *              the reference's per-level bitonic sort gives (:884-939),
  *              with no per-level cap.
- *   k_extract  one warp per row: the raw extrema's positions in (level, y, x)
+ *   k_extract  one warp per 4 rows: the raw extrema's positions in (level, y, x)
  *              order at their scanned indices.
  *   k_extract_fit  one thread per raw extremum of the batch: subpixel fit and
  *              record (:744-769), the determinant recomputed from Lx, Ly at
@@ -619,43 +619,69 @@ __global__ void __launch_bounds__(1024) k_rowscan(akz_tables t, const int *rowcn
 
 /* ------------------------------------------------------------------------ */
 
+/* Raw extrema positions in (image, level, row, column) order: a warp takes
+ * AKZ_EXTRACT_RPW consecutive rows of the row list (one per level row of
+ * every image) and writes each set bit of their bitmap rows at its rank
+ * (the row's exclusive scan plus the bits before it).  Every row's
+ * descriptors, rank and first two 32-word chunks of bitmap are loaded before
+ * the first row is written, so the rows' load chains overlap. */
+#define AKZ_EXTRACT_RPW 4
 __global__ void __launch_bounds__(256) k_extract(akz_extract_params p, int nrows)
 {
+  constexpr int R = AKZ_EXTRACT_RPW;
   const int lane = threadIdx.x & 31;
-  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (r >= nrows) return;
-  const int si = akz_find_seg_warp(p.segs, p.nsegs, r);
-  const akz_tile_seg sg = p.segs[si];
-  const akz_level_desc L = p.t.lv[sg.level_desc];
-  const akz_image_desc I = p.t.im[L.image];
-  const int y = r - sg.tile_begin;
-  const int words = L.bitmap_pitch;
-  const uint32_t *row = p.bitmap + L.bitmap + (long long)y * words;
-  const int rank0 = p.rowscan[L.rows + y];
-  akz_raw *out = p.raw + I.raw_base;
-  int running = 0;
-  for (int w0 = 0; w0 < words; w0 += 32) {
-    const int w = w0 + lane;
-    uint32_t bits = w < words ? row[w] : 0u;
-    const int cnt = __popc(bits);
-    int pre = cnt;
-    for (int d = 1; d < 32; d <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, pre, d);
-      if (lane >= d) pre += t;
+  const int r0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * R;
+  if (r0 >= nrows) return;
+  int si = akz_find_seg_warp(p.segs, p.nsegs, r0);
+  int y[R], words[R], rank0[R], level[R], cap[R];
+  long long raw_base[R];
+  const uint32_t *row[R];
+  uint32_t b0[R], b1[R];
+#pragma unroll
+  for (int k = 0; k < R; k++) {
+    const int r = min(r0 + k, nrows - 1); /* rows past the list: a copy of the last, skipped below */
+    while (si + 1 < p.nsegs && __ldg(&p.segs[si + 1].tile_begin) <= r) si++;
+    const akz_tile_seg sg = p.segs[si];
+    const akz_level_desc &L = p.t.lv[sg.level_desc];
+    y[k] = r - sg.tile_begin;
+    words[k] = L.bitmap_pitch;
+    level[k] = L.level;
+    const akz_image_desc &I = p.t.im[L.image];
+    raw_base[k] = I.raw_base;
+    cap[k] = I.raw_cap;
+    row[k] = p.bitmap + L.bitmap + (long long)y[k] * words[k];
+    rank0[k] = p.rowscan[L.rows + y[k]];
+    b0[k] = lane < words[k] ? row[k][lane] : 0u;
+    b1[k] = 32 + lane < words[k] ? row[k][32 + lane] : 0u;
+  }
+#pragma unroll
+  for (int k = 0; k < R; k++) {
+    if (r0 + k >= nrows) break;
+    akz_raw *out = p.raw + raw_base[k];
+    int running = 0;
+    for (int w0 = 0; w0 < words[k]; w0 += 32) {
+      const int w = w0 + lane;
+      uint32_t bits = w0 == 0 ? b0[k] : (w0 == 32 ? b1[k] : (w < words[k] ? row[k][w] : 0u));
+      const int cnt = __popc(bits);
+      int pre = cnt;
+      for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, pre, d);
+        if (lane >= d) pre += t;
+      }
+      const int total = __shfl_sync(0xffffffffu, pre, 31);
+      int j = running + pre - cnt;
+      while (bits) {
+        const int bt = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const int idx = rank0[k] + j++;
+        if (idx >= cap[k]) continue;
+        /* position only; k_extract_fit completes the record */
+        out[idx].x = w * 32 + bt;
+        out[idx].y = y[k];
+        out[idx].level = level[k];
+      }
+      running += total;
     }
-    const int total = __shfl_sync(0xffffffffu, pre, 31);
-    int k = running + pre - cnt;
-    while (bits) {
-      const int b = __ffs(bits) - 1;
-      bits &= bits - 1;
-      const int idx = rank0 + k++;
-      if (idx >= I.raw_cap) continue;
-      /* position only; k_extract_fit completes the record */
-      out[idx].x = w * 32 + b;
-      out[idx].y = y;
-      out[idx].level = L.level;
-    }
-    running += total;
   }
 }
 
@@ -1030,8 +1056,8 @@ cudaError_t akz_launch_rowscan(const akz_tables &t, const int *rowcnt, int *rows
 cudaError_t akz_launch_extract(const akz_extract_params &p, int nrows, cudaStream_t s)
 {
   if (nrows <= 0) return cudaSuccess;
-  const int warps_per_block = 8;
-  k_extract<<<(nrows + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, s>>>(p, nrows);
+  const int rows_per_block = 8 * AKZ_EXTRACT_RPW; /* 8 warps */
+  k_extract<<<(nrows + rows_per_block - 1) / rows_per_block, 256, 0, s>>>(p, nrows);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (p.t.nimg > AKZ_FIT_MAXIMG) return cudaErrorInvalidValue;
