@@ -729,9 +729,10 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
 
   /* 2. rows of the Gaussian on columns R0 - 2 .. R0 + 129 (sT column c is
    *    x = ox - 2 + c, its taps sP c .. c + 4): column pairs 0..63 by
-   *    (tid & 63) on rows (tid >> 6) + 8k, pairs 64 and 65 by the first
-   *    2 PH threads (an even spread over all threads costs more in index
-   *    arithmetic than it saves) */
+   *    (tid & 63) on rows (tid >> 6) + 8k, pairs 64 and 65 by the last
+   *    2 PH threads, whose row groups 6 and 7 have one row fewer (so no
+   *    thread has more than 7 rows; an even spread over all threads costs
+   *    more in index arithmetic than it saves) */
   const float k0 = p.taps1[0], k1 = p.taps1[1], k2 = p.taps1[2];
   auto hrow = [&](int row, int c) {
     const float *r = sP + row * PS + c;
@@ -748,7 +749,11 @@ __device__ __forceinline__ bool akz_fed_prologue(const akz_fed_params &p, const 
 #pragma unroll
     for (int k = 0; k < (PH + 7) / 8; k++)
       if (r0 + 8 * k < PH) hrow(r0 + 8 * k, c);
-    if (tid < 2 * PH) hrow(tid >> 1, 2 * (64 + (tid & 1)));
+    static_assert(NT - 2 * PH >= 6 * 64 && (PH + 7) / 8 == 7 && PH % 8 == 6, "k_fed rows pass: extra pairs on the 6-row groups");
+    if (tid >= NT - 2 * PH) {
+      const int e = tid - (NT - 2 * PH);
+      hrow(e >> 1, 2 * (64 + (e & 1)));
+    }
   }
   __syncthreads();
 
