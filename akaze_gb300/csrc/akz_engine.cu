@@ -1111,7 +1111,6 @@ static akz_status akz_run_all(akz_batch *b, cudaStream_t s)
   return st;
 }
 
-/* Whole-batch run, captured once into a CUDA graph and replayed. */
 /* drops the captured graphs (after a change of the launches they hold) */
 static void akz_drop_graphs(akz_batch *b)
 {
@@ -1121,6 +1120,8 @@ static void akz_drop_graphs(akz_batch *b)
   }
 }
 
+/* Whole-batch run, captured once per input staging buffer into a CUDA graph
+ * and replayed. */
 static akz_status akz_batch_launch(akz_batch *b)
 {
   cudaStream_t s = b->stream;
