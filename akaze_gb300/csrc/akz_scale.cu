@@ -122,14 +122,25 @@ __global__ void __launch_bounds__(256) k_contrast(akz_contrast_params p)
 
 /* Percentile and per-octave factors, with the reference's types: histogram
  * and point count as float (exact up to 2^24), counters as size_t. */
-__global__ void k_contrast_final(akz_tables t, const unsigned int *hist, int nbins, float perc, float2 *kc)
+__global__ void __launch_bounds__(32) k_contrast_final(akz_tables t, const unsigned int *hist, int nbins, float perc,
+                                                        float2 *kc)
 {
-  const int img = blockIdx.x * blockDim.x + threadIdx.x;
-  if (img >= t.nimg) return;
-  const float hmax = sqrtf(__uint_as_float(t.stats[img].hmax2_bits));
-  const unsigned int *h = hist + (long long)img * nbins;
+  /* one warp per image: the histogram staged in shared memory by the warp
+   * and its (integer) total summed across the lanes, then lane 0 walks the
+   * bins in order with the reference's float accumulation */
+  extern __shared__ unsigned int h[]; /* nbins words: a CTA this small fits beside the other groups' kernels */
+  const int img = blockIdx.x, lane = threadIdx.x;
+  const unsigned int *hg = hist + (long long)img * nbins;
   unsigned long long tot = 0;
-  for (int b = 0; b < nbins; b++) tot += h[b];
+  for (int b = lane; b < nbins; b += 32) {
+    const unsigned int v = hg[b];
+    h[b] = v;
+    tot += v;
+  }
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  __syncwarp();
+  if (lane != 0) return;
+  const float hmax = sqrtf(__uint_as_float(t.stats[img].hmax2_bits));
   const float npoints = tot >= (1ull << 24) ? 16777216.0f : (float)tot;
   const unsigned long long nthreshold = (unsigned long long)(npoints * perc);
   unsigned long long nelements = 0;
@@ -1266,7 +1277,8 @@ cudaError_t akz_launch_contrast(const akz_contrast_params &p, int ntiles, int pa
 
 cudaError_t akz_launch_contrast_final(const akz_tables &t, const unsigned int *hist, int nbins, float perc, float2 *kc, cudaStream_t s)
 {
-  k_contrast_final<<<(t.nimg + 127) / 128, 128, 0, s>>>(t, hist, nbins, perc, kc);
+  if (nbins < 1 || nbins > AKZ_MAX_NBINS) return cudaErrorInvalidValue;
+  k_contrast_final<<<t.nimg, 32, (size_t)nbins * sizeof(unsigned int), s>>>(t, hist, nbins, perc, kc);
   return cudaGetLastError();
 }
 
